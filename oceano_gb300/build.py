@@ -1,0 +1,80 @@
+"""In-tree build of liboceano_gpu.so for sm_103a (nvcc, no cmake).
+
+The four degree instantiations of the fused stage kernel, the auxiliary
+kernels and the C ABI compile as separate translation units in parallel and
+link into one shared library next to this file.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "liboceano_gpu.so")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+         "--expt-relaxed-constexpr", "-I" + INCLUDE]
+
+
+def _nvcc() -> str:
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found")
+
+
+def _sources():
+    units = []
+    for p in (1, 2, 3, 4):
+        units.append((os.path.join(CSRC, "oc_stage_inst.cu"), f"oc_stage_p{p}.o",
+                      [f"-DOC_DEGREE={p}"]))
+    units.append((os.path.join(CSRC, "oc_aux.cu"), "oc_aux.o", []))
+    units.append((os.path.join(CSRC, "oc_api.cu"), "oc_api.o", []))
+    return units
+
+
+def _newest_source() -> float:
+    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    files.append(os.path.join(INCLUDE, "oceano_gpu.h"))
+    files.append(os.path.abspath(__file__))
+    return max(os.path.getmtime(f) for f in files)
+
+
+def build(force: bool = False, verbose: bool = False, extra=()) -> str:
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _newest_source():
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    nvcc = _nvcc()
+    jobs = []
+    for src, obj, defs in _sources():
+        cmd = [nvcc, *ARCH, *FLAGS, *defs, *extra, "-c", src, "-o", os.path.join(BUILD, obj)]
+        jobs.append(cmd)
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        return cmd, r
+
+    with cf.ThreadPoolExecutor(max_workers=min(6, os.cpu_count() or 2)) as ex:
+        for cmd, r in ex.map(run, jobs):
+            if verbose or r.returncode:
+                print(" ".join(cmd))
+                print(r.stdout[-4000:], r.stderr[-8000:])
+            if r.returncode:
+                raise RuntimeError(f"nvcc failed: {cmd[-3]}")
+    objs = [os.path.join(BUILD, o) for _, o, _ in _sources()]
+    tmp = LIB + ".tmp"
+    subprocess.check_call([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    import sys
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv,
+                extra=["-Xptxas", "-v"] if "--ptxas" in sys.argv else []))

@@ -1,0 +1,898 @@
+// C ABI of the GB300 operator (include/oceano_gpu.h): handle, mesh tables,
+// static data, stage and time-step drivers with host or device vectors.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/oceano_gpu.h"
+#include "oc_layout.h"
+#include "oc_tables.hpp"
+
+namespace oc {
+cudaError_t launch_stage_p1(const StageArgs &, int, int, int, cudaStream_t);
+cudaError_t launch_stage_p2(const StageArgs &, int, int, int, cudaStream_t);
+cudaError_t launch_stage_p3(const StageArgs &, int, int, int, cudaStream_t);
+cudaError_t launch_stage_p4(const StageArgs &, int, int, int, cudaStream_t);
+cudaError_t configure_stage_p1();
+cudaError_t configure_stage_p2();
+cudaError_t configure_stage_p3();
+cudaError_t configure_stage_p4();
+int stage_cells_per_warp_p1();
+int stage_cells_per_warp_p2();
+int stage_cells_per_warp_p3();
+int stage_cells_per_warp_p4();
+cudaError_t upload_tables_p1(const DegTables<double> *, const DegTables<float> *);
+cudaError_t upload_tables_p2(const DegTables<double> *, const DegTables<float> *);
+cudaError_t upload_tables_p3(const DegTables<double> *, const DegTables<float> *);
+cudaError_t upload_tables_p4(const DegTables<double> *, const DegTables<float> *);
+
+cudaError_t aux_upload_tables(const DegTables<double> *, const DegTables<float> *);
+cudaError_t launch_transport_speed(const AuxArgs &, const double *, const double *,
+                                   unsigned long long *, cudaStream_t);
+cudaError_t launch_velocity_field(const AuxArgs &, const double *, const double *, double *,
+                                  cudaStream_t);
+cudaError_t launch_vorticity(const AuxArgs &, const double *, int, const double *,
+                             const double *, float *, cudaStream_t);
+cudaError_t launch_project_vortex(const AuxArgs &, double, double *, double *, cudaStream_t);
+}  // namespace oc
+
+using namespace oc;
+
+static const int kWarpsPerBlock = 4;
+
+// Butcher tableaux of time_stepping.h:136-379 (a rows, b, c; d~ for TR-BDF2)
+struct Scheme {
+  int s;
+  double a[OC_MAXSTAGES][OC_MAXSTAGES], b[OC_MAXSTAGES], c[OC_MAXSTAGES];
+  double at[OC_MAXSTAGES][OC_MAXSTAGES], dt[OC_MAXSTAGES];
+  bool ark;
+};
+
+static bool make_scheme(int id, Scheme &sc) {
+  std::memset(&sc, 0, sizeof(sc));
+  const double chi = 2.0 - std::sqrt(2.0);
+  switch (id) {
+    case OC_ERK_FORWARD_EULER:
+      sc.s = 1; sc.b[0] = 1; break;
+    case OC_ERK_SSP22:
+      sc.s = 2; sc.a[0][0] = 1; sc.b[0] = sc.b[1] = 0.5; sc.c[1] = 1; break;
+    case OC_ERK_SSP33:
+      sc.s = 3; sc.a[0][0] = 1; sc.a[1][0] = sc.a[1][1] = 0.25;
+      sc.b[0] = sc.b[1] = 1.0 / 6.0; sc.b[2] = 2.0 / 3.0; sc.c[1] = 1; sc.c[2] = 0.5; break;
+    case OC_ERK_RK4:
+      sc.s = 4; sc.a[0][0] = 0.5; sc.a[1][1] = 0.5; sc.a[2][2] = 1;
+      sc.b[0] = 1.0 / 6.0; sc.b[1] = sc.b[2] = 1.0 / 3.0; sc.b[3] = 1.0 / 6.0;
+      sc.c[1] = sc.c[2] = 0.5; sc.c[3] = 1; break;
+    case OC_ERK_STAGE3_ORDER2:
+    case OC_ARK_STAGE3_ORDER2:
+      sc.s = 3; sc.a[0][0] = chi; sc.a[1][0] = sc.a[1][1] = 0.5;
+      sc.b[0] = sc.b[1] = 0.5 - chi / 4.0; sc.b[2] = chi / 2.0; sc.c[1] = chi; sc.c[2] = 1;
+      if (id == OC_ARK_STAGE3_ORDER2) {
+        sc.ark = true;
+        sc.at[0][0] = chi / 2.0;
+        sc.at[1][0] = sc.at[1][1] = 1.0 / (2.0 * std::sqrt(2.0));
+        sc.dt[0] = chi / 2.0; sc.dt[1] = 1.0 - 1.0 / std::sqrt(2.0);
+      }
+      break;
+    default: return false;
+  }
+  return true;
+}
+
+struct oc_op {
+  int n_cells = 0, n_inner = 0, n_bnd = 0;
+  int64_t n_dofs = 0;
+  oc_params prm{};
+  std::string err;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+  // host copies
+  std::vector<int> deg, off, slots, fcm, fcp, fpack, fsd, bbid, sdo[3];
+  std::vector<double> geo, fnrm, flen;
+  int64_t sd_size[5] = {0, 0, 0, 0, 0};
+  // device copies
+  int *d_deg = nullptr, *d_off = nullptr, *d_slots = nullptr, *d_fcm = nullptr,
+      *d_fcp = nullptr, *d_fpack = nullptr, *d_fsd = nullptr, *d_bbid = nullptr;
+  int *d_sdo[3] = {nullptr, nullptr, nullptr};
+  double *d_geo = nullptr, *d_fnrm = nullptr, *d_flen = nullptr;
+  double *d_sd[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  float *d_sde[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  // degree groups
+  int group_n[OC_MAXDEG + 1] = {0, 0, 0, 0, 0};
+  int *d_group[OC_MAXDEG + 1] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  int uniform_deg = 0;
+  // boundary conditions
+  int bc_kind[OC_MAXBID] = {0}, bc_fn[OC_MAXBID] = {0};
+  double bc_c[OC_MAXBID][3] = {{0}};
+  double vortex[8] = {0};
+  // scratch
+  int *d_err = nullptr;
+  unsigned long long *d_speed = nullptr;
+  StageDyn *d_dyn = nullptr;    // per-stage coefficient blocks (OC_MAXSTAGES + 1)
+  StageDyn *h_dyn = nullptr;    // pageable host mirror (safe to reuse once a copy is enqueued)
+  // host-memory staging and time-step registers
+  std::vector<void *> bufs;
+  double *st_rz = nullptr, *st_rq = nullptr, *st_rv = nullptr, *st_sz = nullptr, *st_sq = nullptr,
+         *st_nz = nullptr, *st_nq = nullptr;
+  double *st_kz[OC_MAXSTAGES + 1] = {nullptr}, *st_kq[2 * OC_MAXSTAGES] = {nullptr};
+  void *ts_kz[OC_MAXSTAGES + 1] = {nullptr}, *ts_kq[2 * OC_MAXSTAGES] = {nullptr};
+  void *ts_rz[2] = {nullptr, nullptr}, *ts_rq[2] = {nullptr, nullptr};
+  double *ts_z = nullptr, *ts_q = nullptr;  // solution when the caller passes host memory
+  double *ts_aux = nullptr;
+  // graph cache of oc_perform_time_step
+  cudaGraphExec_t graph = nullptr;
+  int graph_scheme = -1;
+  const void *graph_z = nullptr, *graph_q = nullptr;
+};
+
+#define OC_TRY(call)                                                              \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess) {                                                      \
+      op->err = std::string(#call) + ": " + cudaGetErrorString(e_);               \
+      return OC_ERR_CUDA;                                                         \
+    }                                                                             \
+  } while (0)
+
+static oc_status fail(oc_op *op, oc_status s, const std::string &msg) {
+  if (op) op->err = msg;
+  return s;
+}
+
+template <typename T>
+static cudaError_t upload(oc_op *op, T **dst, const T *src, size_t n) {
+  if (n == 0) { *dst = nullptr; return cudaSuccess; }
+  cudaError_t e = cudaMalloc((void **)dst, n * sizeof(T));
+  if (e != cudaSuccess) return e;
+  op->bufs.push_back(*dst);
+  return cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+static cudaError_t alloc(oc_op *op, void **dst, size_t bytes) {
+  cudaError_t e = cudaMalloc(dst, bytes);
+  if (e == cudaSuccess) op->bufs.push_back(*dst);
+  return e;
+}
+
+static int cells_per_warp(int p) {
+  switch (p) {
+    case 1: return stage_cells_per_warp_p1();
+    case 2: return stage_cells_per_warp_p2();
+    case 3: return stage_cells_per_warp_p3();
+    default: return stage_cells_per_warp_p4();
+  }
+}
+
+static cudaError_t launch_stage(int p, const StageArgs &a, int variant, int grid, cudaStream_t s) {
+  switch (p) {
+    case 1: return launch_stage_p1(a, variant, grid, kWarpsPerBlock, s);
+    case 2: return launch_stage_p2(a, variant, grid, kWarpsPerBlock, s);
+    case 3: return launch_stage_p3(a, variant, grid, kWarpsPerBlock, s);
+    default: return launch_stage_p4(a, variant, grid, kWarpsPerBlock, s);
+  }
+}
+
+extern "C" {
+
+const char *oc_last_error(const oc_op *op) { return op ? op->err.c_str() : "null handle"; }
+int64_t oc_n_dofs(const oc_op *op) { return op ? op->n_dofs : -1; }
+int64_t oc_launch_count(const oc_op *op) { return op ? op->launches : -1; }
+void *oc_stream(oc_op *op) { return op ? (void *)op->stream : nullptr; }
+
+oc_status oc_synchronize(oc_op *op) {
+  if (!op) return OC_ERR_INVALID_ARG;
+  OC_TRY(cudaStreamSynchronize(op->stream));
+  return OC_OK;
+}
+
+void oc_destroy(oc_op *op) {
+  if (!op) return;
+  if (op->stream) cudaStreamSynchronize(op->stream);
+  if (op->graph) cudaGraphExecDestroy(op->graph);
+  for (void *p : op->bufs) cudaFree(p);
+  delete[] op->h_dyn;
+  if (op->stream) cudaStreamDestroy(op->stream);
+  delete op;
+}
+
+oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
+  if (!out) return OC_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (!m || !prm || m->n_cells <= 0 || !m->degree || !m->vertices || m->n_inner_faces < 0 ||
+      m->n_boundary_faces < 0)
+    return OC_ERR_INVALID_ARG;
+  oc_op *op = new oc_op();
+  op->prm = *prm;
+  if (op->prm.batch_width <= 0) op->prm.batch_width = 1;
+  if (op->prm.max_iteration_height < 0) op->prm.max_iteration_height = 0;
+  const int nc = m->n_cells, ni = m->n_inner_faces, nb = m->n_boundary_faces;
+  op->n_cells = nc; op->n_inner = ni; op->n_bnd = nb;
+  auto bad = [&](oc_status s, const std::string &msg) {
+    oc_status r = fail(op, s, msg);
+    *out = op;  // keep the handle so that the caller can read the message
+    return r;
+  };
+  if (prm->horizontal_viscosity != 0.0)
+    return bad(OC_ERR_UNSUPPORTED, "horizontal_viscosity != 0 is not implemented on the GPU");
+  if (prm->precision != OC_PREC_FP64 && prm->precision != OC_PREC_MIXED)
+    return bad(OC_ERR_INVALID_ARG, "unknown precision");
+  // cells: degree, offsets, affine geometry
+  op->deg.assign(m->degree, m->degree + nc);
+  op->off.resize(nc);
+  op->geo.resize(11 * (size_t)nc);
+  for (int k = 0; k < 3; ++k) op->sdo[k].resize(nc);
+  int64_t off = 0, s0 = 0, s1 = 0, s2 = 0;
+  int first_deg = m->degree[0];
+  bool uniform = true;
+  for (int c = 0; c < nc; ++c) {
+    const int p = m->degree[c];
+    if (p < 1 || p > OC_MAXDEG) return bad(OC_ERR_UNSUPPORTED, "degree must be 1..4");
+    uniform = uniform && p == first_deg;
+    const int Q = (3 * p) / 2 + 1;
+    op->off[c] = (int)off;
+    op->sdo[0][c] = (int)s0; op->sdo[1][c] = (int)s1; op->sdo[2][c] = (int)s2;
+    off += (p + 1) * (p + 1);
+    s0 += 5 * Q * Q; s1 += (p + 2) * (p + 2); s2 += 2 * (p + 1) * (p + 1);
+    const double *v = m->vertices + 8 * (size_t)c;
+    double *J = &op->geo[11 * (size_t)c];
+    J[0] = v[0]; J[1] = v[1];
+    J[2] = v[2] - v[0]; J[3] = v[4] - v[0];
+    J[4] = v[3] - v[1]; J[5] = v[5] - v[1];
+    const double scale = std::fabs(J[2]) + std::fabs(J[3]) + std::fabs(J[4]) + std::fabs(J[5]);
+    const double ex = v[6] - (v[2] + v[4] - v[0]), ey = v[7] - (v[3] + v[5] - v[1]);
+    if (std::fabs(ex) + std::fabs(ey) > 1e-12 * scale)
+      return bad(OC_ERR_UNSUPPORTED, "cell " + std::to_string(c) + " is not affine");
+    const double det = J[2] * J[5] - J[3] * J[4];
+    if (!(det > 0)) return bad(OC_ERR_INVALID_ARG, "cell " + std::to_string(c) + " has det <= 0");
+    J[6] = J[5] / det; J[7] = -J[3] / det; J[8] = -J[4] / det; J[9] = J[2] / det; J[10] = det;
+  }
+  if (off >= (int64_t)1 << 30) return bad(OC_ERR_UNSUPPORTED, "more than 2^30 DoFs per variable");
+  op->n_dofs = off;
+  op->sd_size[0] = s0; op->sd_size[1] = s1; op->sd_size[2] = s2;
+  op->uniform_deg = uniform ? first_deg : 0;
+  // faces
+  const int nf = ni + nb;
+  op->fcm.resize(nf); op->fcp.assign(std::max(ni, 1), 0); op->fpack.resize(nf);
+  op->fsd.resize(nf); op->bbid.assign(std::max(nb, 1), 0);
+  op->fnrm.resize(2 * (size_t)nf); op->flen.resize(nf);
+  op->slots.assign(8 * (size_t)nc, -1);
+  int64_t sf = 0, sb = 0;
+  static const double rn[4][2] = {{-1, 0}, {1, 0}, {0, -1}, {0, 1}};
+  for (int f = 0; f < nf; ++f) {
+    const int cm = m->cell_m[f];
+    const int fm = m->face_m[f];
+    if (cm < 0 || cm >= nc || fm < 0 || fm > 3) return bad(OC_ERR_INVALID_ARG, "bad face " + std::to_string(f));
+    const double *J = &op->geo[11 * (size_t)cm];
+    double nx = J[6] * rn[fm][0] + J[8] * rn[fm][1], ny = J[7] * rn[fm][0] + J[9] * rn[fm][1];
+    const double nn = std::sqrt(nx * nx + ny * ny);
+    op->fnrm[2 * f] = nx / nn; op->fnrm[2 * f + 1] = ny / nn;
+    const double t0 = fm < 2 ? 0 : 1, t1 = fm < 2 ? 1 : 0;
+    const double tx = J[2] * t0 + J[3] * t1, ty = J[4] * t0 + J[5] * t1;
+    op->flen[f] = std::sqrt(tx * tx + ty * ty);
+    op->fcm[f] = cm;
+    if (f < ni) {
+      const int cp = m->cell_p[f], fp = m->face_p[f], sub = m->subface[f];
+      const int orient = m->orientation ? m->orientation[f] : 0;
+      if (cp < 0 || cp >= nc || fp < 0 || fp > 3 || sub < -1 || sub > 1 || orient < 0 || orient > 1)
+        return bad(OC_ERR_INVALID_ARG, "bad inner face " + std::to_string(f));
+      const int nfq = std::max(m->degree[cm], m->degree[cp]) + 2;
+      op->fcp[f] = cp;
+      op->fpack[f] = fm | (fp << 4) | ((sub + 1) << 8) | (orient << 12) | (nfq << 16);
+      op->fsd[f] = (int)sf;
+      sf += 2 * nfq;
+      int *sm = &op->slots[8 * (size_t)cm + 2 * fm];
+      if (sm[0] != -1) return bad(OC_ERR_INVALID_ARG, "cell face listed twice (minus side)");
+      sm[0] = 2 * f;
+      int *sp = &op->slots[8 * (size_t)cp + 2 * fp];
+      const int pos = sub < 0 ? 0 : sub;
+      if (sp[pos] != -1) return bad(OC_ERR_INVALID_ARG, "cell face listed twice (plus side)");
+      sp[pos] = 2 * f + 1;
+    } else {
+      const int b = f - ni;
+      const int bid = m->boundary_id[b];
+      if (bid < 0 || bid >= OC_MAXBID) return bad(OC_ERR_UNKNOWN_BOUNDARY_ID, "boundary id out of range");
+      op->bbid[b] = bid;
+      op->fpack[f] = fm;
+      op->fsd[f] = (int)sb;
+      sb += (3 * m->degree[cm]) / 2 + 1;
+      int *sm = &op->slots[8 * (size_t)cm + 2 * fm];
+      if (sm[0] != -1) return bad(OC_ERR_INVALID_ARG, "cell face listed twice (boundary)");
+      sm[0] = -(b + 2);
+    }
+  }
+  for (int c = 0; c < nc; ++c)
+    for (int fno = 0; fno < 4; ++fno) {
+      const int *sl = &op->slots[8 * (size_t)c + 2 * fno];
+      if (sl[0] == -1 && sl[1] == -1)
+        return bad(OC_ERR_INVALID_ARG, "cell " + std::to_string(c) + " face " + std::to_string(fno) + " has no face");
+      if (sl[0] == -1) return bad(OC_ERR_INVALID_ARG, "hanging face without subface 0");
+    }
+  op->sd_size[3] = sf; op->sd_size[4] = sb;
+  // device
+  OC_TRY(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
+  OC_TRY(upload(op, &op->d_deg, op->deg.data(), nc));
+  OC_TRY(upload(op, &op->d_off, op->off.data(), nc));
+  OC_TRY(upload(op, &op->d_geo, op->geo.data(), op->geo.size()));
+  OC_TRY(upload(op, &op->d_slots, op->slots.data(), op->slots.size()));
+  OC_TRY(upload(op, &op->d_fcm, op->fcm.data(), op->fcm.size()));
+  OC_TRY(upload(op, &op->d_fcp, op->fcp.data(), op->fcp.size()));
+  OC_TRY(upload(op, &op->d_fpack, op->fpack.data(), op->fpack.size()));
+  OC_TRY(upload(op, &op->d_fsd, op->fsd.data(), op->fsd.size()));
+  OC_TRY(upload(op, &op->d_bbid, op->bbid.data(), op->bbid.size()));
+  OC_TRY(upload(op, &op->d_fnrm, op->fnrm.data(), op->fnrm.size()));
+  OC_TRY(upload(op, &op->d_flen, op->flen.data(), op->flen.size()));
+  for (int k = 0; k < 3; ++k) OC_TRY(upload(op, &op->d_sdo[k], op->sdo[k].data(), nc));
+  for (int p = 1; p <= OC_MAXDEG; ++p) {
+    std::vector<int> g;
+    for (int c = 0; c < nc; ++c)
+      if (m->degree[c] == p) g.push_back(c);
+    op->group_n[p] = (int)g.size();
+    if (!uniform && !g.empty()) OC_TRY(upload(op, &op->d_group[p], g.data(), g.size()));
+  }
+  // tables
+  std::vector<DegTables<double>> td(OC_MAXDEG);
+  std::vector<DegTables<float>> tf(OC_MAXDEG);
+  for (int p = 1; p <= OC_MAXDEG; ++p) {
+    fill_tables(p, op->prm.max_iteration_height, td[p - 1]);
+    cast_tables(td[p - 1], tf[p - 1]);
+  }
+  OC_TRY(upload_tables_p1(td.data(), tf.data()));
+  OC_TRY(upload_tables_p2(td.data(), tf.data()));
+  OC_TRY(upload_tables_p3(td.data(), tf.data()));
+  OC_TRY(upload_tables_p4(td.data(), tf.data()));
+  OC_TRY(aux_upload_tables(td.data(), tf.data()));
+  OC_TRY(alloc(op, (void **)&op->d_err, sizeof(int)));
+  OC_TRY(alloc(op, (void **)&op->d_speed, sizeof(unsigned long long)));
+  OC_TRY(alloc(op, (void **)&op->d_dyn, sizeof(StageDyn) * (OC_MAXSTAGES + 1)));
+  op->h_dyn = new StageDyn[OC_MAXSTAGES + 1];
+  OC_TRY(configure_stage_p1());
+  OC_TRY(configure_stage_p2());
+  OC_TRY(configure_stage_p3());
+  OC_TRY(configure_stage_p4());
+  OC_TRY(cudaMemset(op->d_err, 0, sizeof(int)));
+  OC_TRY(cudaDeviceSynchronize());
+  *out = op;
+  return OC_OK;
+}
+
+oc_status oc_set_boundary(oc_op *op, int32_t bid, int32_t kind, int32_t fn, const double *v) {
+  if (!op) return OC_ERR_INVALID_ARG;
+  if (bid < 0 || bid >= OC_MAXBID) return fail(op, OC_ERR_UNKNOWN_BOUNDARY_ID, "boundary id out of range");
+  if (kind < OC_BC_NONE || kind > OC_BC_ABSORBING_OUTFLOW || fn < 0 || fn > 1)
+    return fail(op, OC_ERR_INVALID_ARG, "bad boundary kind or function");
+  op->bc_kind[bid] = kind;
+  op->bc_fn[bid] = fn;
+  for (int k = 0; k < 3; ++k) op->bc_c[bid][k] = v ? v[k] : 0.0;
+  op->graph_scheme = -1;
+  return OC_OK;
+}
+
+oc_status oc_set_vortex(oc_op *op, const double *v) {
+  if (!op || !v) return OC_ERR_INVALID_ARG;
+  for (int k = 0; k < 6; ++k) op->vortex[k] = v[k];
+  op->graph_scheme = -1;
+  return OC_OK;
+}
+
+int64_t oc_static_data_size(const oc_op *op, int32_t which) {
+  if (!op || which < 0 || which > 4) return -1;
+  return op->sd_size[which];
+}
+
+oc_status oc_quadrature_points(const oc_op *op, int32_t which, double *xy) {
+  if (!op || !xy || which < 0 || which > 4) return OC_ERR_INVALID_ARG;
+  int64_t k = 0;
+  auto map = [&](int c, double e0, double e1, double *o) {
+    const double *J = &op->geo[11 * (size_t)c];
+    o[0] = J[0] + J[2] * e0 + J[3] * e1;
+    o[1] = J[1] + J[4] * e0 + J[5] * e1;
+  };
+  auto fpoint = [](int f, double s, double &e0, double &e1) {
+    e0 = f == 0 ? 0. : f == 1 ? 1. : s;
+    e1 = f < 2 ? s : f == 2 ? 0. : 1.;
+  };
+  double x[16], w[16];
+  if (which <= 2) {
+    for (int c = 0; c < op->n_cells; ++c) {
+      const int p = op->deg[c];
+      const int n = which == 0 ? (3 * p) / 2 + 1 : which == 1 ? p + 2 : p + 1;
+      if (which == 1) lobatto_rule(n, x, w); else gauss_rule(n, x, w);
+      for (int qy = 0; qy < n; ++qy)
+        for (int qx = 0; qx < n; ++qx) { map(c, x[qx], x[qy], xy + 2 * k); ++k; }
+    }
+  } else if (which == 3) {
+    for (int f = 0; f < op->n_inner; ++f) {
+      const int nfq = (op->fpack[f] >> 16) & 15, fm = op->fpack[f] & 15;
+      lobatto_rule(nfq, x, w);
+      for (int q = 0; q < nfq; ++q) {
+        double e0, e1, pt[2];
+        fpoint(fm, x[q], e0, e1);
+        map(op->fcm[f], e0, e1, pt);
+        const double nx = op->fnrm[2 * f], ny = op->fnrm[2 * f + 1];
+        xy[2 * k] = pt[0] - 1e-12 * nx; xy[2 * k + 1] = pt[1] - 1e-12 * ny; ++k;
+        xy[2 * k] = pt[0] + 1e-12 * nx; xy[2 * k + 1] = pt[1] + 1e-12 * ny; ++k;
+      }
+    }
+  } else {
+    for (int b = 0; b < op->n_bnd; ++b) {
+      const int f = op->n_inner + b, c = op->fcm[f], fm = op->fpack[f] & 15;
+      const int n = (3 * op->deg[c]) / 2 + 1;
+      gauss_rule(n, x, w);
+      for (int q = 0; q < n; ++q) {
+        double e0, e1;
+        fpoint(fm, x[q], e0, e1);
+        map(c, e0, e1, xy + 2 * k);
+        ++k;
+      }
+    }
+  }
+  return OC_OK;
+}
+
+oc_status oc_set_static_data(oc_op *op, const double *c0, const double *c1, const double *c2,
+                             const double *fc, const double *bn) {
+  if (!op) return OC_ERR_INVALID_ARG;
+  const double *src[5] = {c0, c1, c2, fc, bn};
+  const double zref = op->prm.precision == OC_PREC_MIXED ? op->prm.zeta_reference : 0.0;
+  OC_TRY(cudaStreamSynchronize(op->stream));
+  for (int k = 0; k < 5; ++k) {
+    if (op->d_sd[k]) { cudaFree(op->d_sd[k]); op->bufs.erase(std::find(op->bufs.begin(), op->bufs.end(), (void *)op->d_sd[k])); op->d_sd[k] = nullptr; }
+    if (op->d_sde[k]) { cudaFree(op->d_sde[k]); op->bufs.erase(std::find(op->bufs.begin(), op->bufs.end(), (void *)op->d_sde[k])); op->d_sde[k] = nullptr; }
+    if (!src[k] || op->sd_size[k] == 0) continue;
+    const int64_t n = op->sd_size[k];
+    OC_TRY(upload(op, &op->d_sd[k], src[k], n));
+    // FP32 copy with zeta_reference folded into zb (the mixed form works on zeta - zref)
+    std::vector<float> e(n);
+    const int stride = k == 0 ? 5 : k == 2 ? 2 : 1;
+    for (int64_t i = 0; i < n; ++i) {
+      const bool is_zb = k == 3 || (i % stride) == 0;
+      e[i] = (float)(is_zb ? src[k][i] + zref : src[k][i]);
+    }
+    OC_TRY(upload(op, &op->d_sde[k], e.data(), n));
+  }
+  op->graph_scheme = -1;
+  return OC_OK;
+}
+
+}  // extern "C"
+
+// --------------------------------------------------------------------------
+// stage launches
+// --------------------------------------------------------------------------
+
+static void fill_common(oc_op *op, StageArgs &a) {
+  std::memset(&a, 0, sizeof(a));
+  a.deg = op->d_deg; a.off = op->d_off; a.geo = op->d_geo; a.slots = op->d_slots;
+  a.fcm = op->d_fcm; a.fcp = op->d_fcp; a.fpack = op->d_fpack; a.fnrm = op->d_fnrm;
+  a.flen = op->d_flen; a.fsd = op->d_fsd; a.bbid = op->d_bbid; a.n_inner = op->n_inner;
+  a.sd0 = op->d_sd[0]; a.sd1 = op->d_sd[1]; a.sd2 = op->d_sd[2]; a.sdf = op->d_sd[3];
+  a.sdb = op->d_sd[4];
+  a.sd0e = op->d_sde[0]; a.sd1e = op->d_sde[1]; a.sd2e = op->d_sde[2]; a.sdfe = op->d_sde[3];
+  a.sdbe = op->d_sde[4];
+  a.sdo0 = op->d_sdo[0]; a.sdo1 = op->d_sdo[1]; a.sdo2 = op->d_sdo[2];
+  const double cu = op->prm.threshold_wetdry;
+  a.g = op->prm.g; a.cu4 = cu * cu * cu * cu; a.nu = op->prm.horizontal_viscosity;
+  a.zeta_ref = op->prm.precision == OC_PREC_MIXED ? op->prm.zeta_reference : 0.0;
+  a.wet_threshold = 1e-3;
+  a.friction = op->prm.friction_model; a.max_iter = op->prm.max_iteration_height;
+  a.batch = op->prm.batch_width;
+  for (int b = 0; b < OC_MAXBID; ++b) {
+    a.bc_kind[b] = op->bc_kind[b]; a.bc_fn[b] = op->bc_fn[b];
+    for (int k = 0; k < 3; ++k) a.bc_c[b][k] = op->bc_c[b][k];
+  }
+  for (int k = 0; k < 8; ++k) a.vortex[k] = op->vortex[k];
+  a.err = op->d_err;
+}
+
+static oc_status check_boundaries(oc_op *op) {
+  for (int b = 0; b < op->n_bnd; ++b)
+    if (op->bc_kind[op->bbid[b]] == OC_BC_NONE)
+      return fail(op, OC_ERR_UNKNOWN_BOUNDARY_ID,
+                  "Unknown boundary id " + std::to_string(op->bbid[b]) +
+                      ", did you set a boundary condition for this part of the domain boundary?");
+  return OC_OK;
+}
+
+// launch the fused kernel over every degree group
+static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
+  const int batch = op->prm.batch_width;
+  for (int p = 1; p <= OC_MAXDEG; ++p) {
+    const int n = op->group_n[p];
+    if (n == 0) continue;
+    const int cpw = (cells_per_warp(p) / batch) * batch;
+    if (cpw == 0) return fail(op, OC_ERR_UNSUPPORTED, "batch_width larger than the cells of a warp");
+    a.n_group = n;
+    a.group_cells = op->uniform_deg ? nullptr : op->d_group[p];
+    a.group_first = 0;
+    const int grid = (n + kWarpsPerBlock * cpw - 1) / (kWarpsPerBlock * cpw);
+    OC_TRY(launch_stage(p, a, variant, grid, op->stream));
+    op->launches++;
+  }
+  return OC_OK;
+}
+
+static oc_status read_error(oc_op *op) {
+  int e = 0;
+  OC_TRY(cudaMemcpyAsync(&e, op->d_err, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
+  OC_TRY(cudaStreamSynchronize(op->stream));
+  if (e) {
+    OC_TRY(cudaMemset(op->d_err, 0, sizeof(int)));
+    if (e & (1 << 2)) return fail(op, OC_ERR_UNKNOWN_BOUNDARY_ID, "unknown boundary id in a kernel");
+    if (e & (1 << 3)) return fail(op, OC_ERR_NONFINITE, "non-finite value detected");
+    return fail(op, OC_ERR_CUDA, "device error flag " + std::to_string(e));
+  }
+  return OC_OK;
+}
+
+static oc_status ensure(oc_op *op, double **p, size_t n) {
+  if (*p) return OC_OK;
+  OC_TRY(alloc(op, (void **)p, n * sizeof(double)));
+  return OC_OK;
+}
+
+extern "C" oc_status oc_perform_stage_hydro(oc_op *op, uint32_t stage, uint32_t n_stages,
+                                            double time, const double *fr, const double *ftr,
+                                            double fmat, const oc_stage_vectors *v,
+                                            int32_t memory) {
+  if (!op || !v || !fr) return OC_ERR_INVALID_ARG;
+  if (n_stages < 1 || n_stages > OC_MAXSTAGES || stage >= n_stages)
+    return fail(op, OC_ERR_INVALID_ARG, "stage out of range");
+  const bool ark = ftr != nullptr;
+  const int nkz = n_stages + 1, nkq = ark ? 2 * n_stages : n_stages + 1;
+  if (v->n_ki_height < nkz || v->n_ki_discharge < nkq || !v->ki_height || !v->ki_discharge)
+    return fail(op, OC_ERR_INVALID_ARG, "too few k vectors");
+  if (!v->ri_height || !v->ri_discharge || !v->solution_height || !v->solution_discharge ||
+      !v->next_height || !v->next_discharge)
+    return fail(op, OC_ERR_INVALID_ARG, "null vector");
+  oc_status st = check_boundaries(op);
+  if (st != OC_OK) return st;
+  const bool last = stage == n_stages - 1;
+  const size_t nz = op->n_dofs, nq = 2 * nz;
+  const bool mixed = op->prm.precision == OC_PREC_MIXED;
+  StageArgs a;
+  fill_common(op, a);
+  StageDyn &dy = op->h_dyn[0];
+  std::memset(&dy, 0, sizeof(dy));
+  for (uint32_t j = 0; j <= stage; ++j) { dy.f[j] = fr[j]; dy.ft[j] = ark ? ftr[j] : 0.0; }
+  dy.fm = fmat;
+  dy.time = time;
+  a.dyn = op->d_dyn;
+  a.stage = (int)stage; a.n_stages = (int)n_stages; a.ark = ark; a.last = last;
+  a.write_kq_last = 1;
+  a.r_is_float = 0;
+  // vectors: device pointers as given, or staged copies of host vectors
+  const double *rz = v->ri_height, *rq = v->ri_discharge;
+  double *sz = v->solution_height, *sq = v->solution_discharge;
+  double *nzp = v->next_height, *nqp = v->next_discharge;
+  double *kz[OC_MAXSTAGES + 1], *kq[2 * OC_MAXSTAGES];
+  for (int j = 0; j < nkz; ++j) kz[j] = v->ki_height[j];
+  for (int j = 0; j < nkq; ++j) kq[j] = v->ki_discharge[j];
+  const bool host = memory == OC_MEM_HOST;
+  if (host) {
+    if (ensure(op, &op->st_rz, nz) || ensure(op, &op->st_rq, nq) || ensure(op, &op->st_sz, nz) ||
+        ensure(op, &op->st_sq, nq) || ensure(op, &op->st_nz, nz) || ensure(op, &op->st_nq, nq))
+      return OC_ERR_CUDA;
+    for (int j = 0; j < nkz; ++j) if (ensure(op, &op->st_kz[j], nz)) return OC_ERR_CUDA;
+    for (int j = 0; j < nkq; ++j) if (ensure(op, &op->st_kq[j], nq)) return OC_ERR_CUDA;
+    cudaStream_t s = op->stream;
+    OC_TRY(cudaMemcpyAsync(op->st_rz, rz, nz * 8, cudaMemcpyHostToDevice, s));
+    OC_TRY(cudaMemcpyAsync(op->st_rq, rq, nq * 8, cudaMemcpyHostToDevice, s));
+    OC_TRY(cudaMemcpyAsync(op->st_sz, sz, nz * 8, cudaMemcpyHostToDevice, s));
+    OC_TRY(cudaMemcpyAsync(op->st_sq, sq, nq * 8, cudaMemcpyHostToDevice, s));
+    if (ark && last) OC_TRY(cudaMemcpyAsync(op->st_nq, nqp, nq * 8, cudaMemcpyHostToDevice, s));
+    // only the registers the stage reads are copied in
+    for (uint32_t j = 1; j <= stage; ++j) {
+      OC_TRY(cudaMemcpyAsync(op->st_kz[j], kz[j], nz * 8, cudaMemcpyHostToDevice, s));
+      if (!ark) OC_TRY(cudaMemcpyAsync(op->st_kq[j], kq[j], nq * 8, cudaMemcpyHostToDevice, s));
+    }
+    if (ark)
+      for (int j = 1; j < (int)(2 * stage + 1); ++j)
+        OC_TRY(cudaMemcpyAsync(op->st_kq[j], kq[j], nq * 8, cudaMemcpyHostToDevice, s));
+    rz = op->st_rz; rq = op->st_rq; sz = op->st_sz; sq = op->st_sq;
+    nzp = op->st_nz; nqp = op->st_nq;
+    for (int j = 0; j < nkz; ++j) kz[j] = op->st_kz[j];
+    for (int j = 0; j < nkq; ++j) kq[j] = op->st_kq[j];
+  }
+  OC_TRY(cudaMemcpyAsync(op->d_dyn, &dy, sizeof(StageDyn), cudaMemcpyHostToDevice, op->stream));
+  a.rz = rz; a.rq = rq;
+  a.un_z = sz; a.un_q = sq;
+  for (int j = 0; j < nkz; ++j) a.kz[j] = kz[j];
+  for (int j = 0; j < nkq; ++j) a.kq[j] = kq[j];
+  a.out_z = last ? sz : nzp;
+  a.out_q = (last && !ark) ? sq : (ark && last ? sq : nqp);
+  a.aux_q = (ark && last) ? nqp : nullptr;
+  a.out_rz = nullptr; a.out_rq = nullptr;
+  st = launch_groups(op, a, mixed ? 2 : 0);
+  if (st != OC_OK) return st;
+  if (host) {
+    cudaStream_t s = op->stream;
+    OC_TRY(cudaMemcpyAsync(v->ki_height[stage + 1], op->st_kz[stage + 1], nz * 8,
+                           cudaMemcpyDeviceToHost, s));
+    if (!ark) {
+      OC_TRY(cudaMemcpyAsync(v->ki_discharge[stage + 1], op->st_kq[stage + 1], nq * 8, cudaMemcpyDeviceToHost, s));
+    } else {
+      OC_TRY(cudaMemcpyAsync(v->ki_discharge[2 * stage + 1], op->st_kq[2 * stage + 1], nq * 8, cudaMemcpyDeviceToHost, s));
+      if (!last) OC_TRY(cudaMemcpyAsync(v->ki_discharge[2 * stage + 2], op->st_kq[2 * stage + 2], nq * 8, cudaMemcpyDeviceToHost, s));
+    }
+    if (last) {
+      OC_TRY(cudaMemcpyAsync(v->solution_height, op->st_sz, nz * 8, cudaMemcpyDeviceToHost, s));
+      OC_TRY(cudaMemcpyAsync(v->solution_discharge, op->st_sq, nq * 8, cudaMemcpyDeviceToHost, s));
+      if (ark) OC_TRY(cudaMemcpyAsync(v->next_discharge, op->st_nq, nq * 8, cudaMemcpyDeviceToHost, s));
+    } else {
+      OC_TRY(cudaMemcpyAsync(v->next_height, op->st_nz, nz * 8, cudaMemcpyDeviceToHost, s));
+      OC_TRY(cudaMemcpyAsync(v->next_discharge, op->st_nq, nq * 8, cudaMemcpyDeviceToHost, s));
+    }
+  }
+  return read_error(op);
+}
+
+// ---------------------------------------------------------------------------
+// whole time steps with handle-owned registers, replayed as a CUDA graph
+// ---------------------------------------------------------------------------
+
+static oc_status ensure_ts(oc_op *op, const Scheme &sc) {
+  const size_t nz = op->n_dofs, nq = 2 * nz;
+  const bool mixed = op->prm.precision == OC_PREC_MIXED;
+  const size_t ks = mixed ? 4 : 8;
+  const int nkq = sc.ark ? 2 * sc.s : sc.s + 1;
+  for (int j = 1; j <= sc.s; ++j)
+    if (!op->ts_kz[j]) OC_TRY(alloc(op, &op->ts_kz[j], nz * ks));
+  for (int j = 1; j < nkq; ++j)
+    if (!op->ts_kq[j]) OC_TRY(alloc(op, &op->ts_kq[j], nq * ks));
+  const size_t rs = mixed ? 4 : 8;
+  for (int j = 0; j < 2; ++j) {
+    if (!op->ts_rz[j]) OC_TRY(alloc(op, &op->ts_rz[j], nz * rs));
+    if (!op->ts_rq[j]) OC_TRY(alloc(op, &op->ts_rq[j], nq * rs));
+  }
+  if (sc.ark && !op->ts_aux) OC_TRY(alloc(op, (void **)&op->ts_aux, nq * 8));
+  return OC_OK;
+}
+
+// enqueue the stages of one time step on op->stream (capturable)
+static oc_status enqueue_step(oc_op *op, const Scheme &sc, double *z, double *q) {
+  const bool mixed = op->prm.precision == OC_PREC_MIXED;
+  StageArgs a;
+  fill_common(op, a);
+  for (int st = 0; st < sc.s; ++st) {
+    const bool last = st == sc.s - 1;
+    a.dyn = op->d_dyn + st;
+    a.stage = st; a.n_stages = sc.s; a.ark = sc.ark; a.last = last; a.write_kq_last = 0;
+    if (st == 0) {
+      a.rz = z; a.rq = q; a.r_is_float = 0;
+    } else {
+      a.rz = op->ts_rz[(st - 1) & 1]; a.rq = op->ts_rq[(st - 1) & 1];
+      a.r_is_float = mixed ? 1 : 0;
+    }
+    a.un_z = z; a.un_q = q;
+    for (int j = 0; j <= sc.s; ++j) a.kz[j] = op->ts_kz[j];
+    for (int j = 0; j < 2 * OC_MAXSTAGES; ++j) a.kq[j] = op->ts_kq[j];
+    if (last) {
+      a.out_z = z; a.out_q = q; a.out_rz = nullptr; a.out_rq = nullptr;
+      a.aux_q = sc.ark ? op->ts_aux : nullptr;
+    } else if (mixed) {
+      a.out_z = nullptr; a.out_q = nullptr;
+      a.out_rz = (float *)op->ts_rz[st & 1]; a.out_rq = (float *)op->ts_rq[st & 1];
+      a.aux_q = nullptr;
+    } else {
+      a.out_z = (double *)op->ts_rz[st & 1]; a.out_q = (double *)op->ts_rq[st & 1];
+      a.out_rz = nullptr; a.out_rq = nullptr; a.aux_q = nullptr;
+    }
+    oc_status s = launch_groups(op, a, mixed ? 1 : 0);
+    if (s != OC_OK) return s;
+  }
+  return OC_OK;
+}
+
+extern "C" oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time, double dt,
+                                          double *z, double *q, int32_t memory) {
+  if (!op || !z || !q) return OC_ERR_INVALID_ARG;
+  Scheme sc;
+  if (!make_scheme(scheme, sc)) return fail(op, OC_ERR_INVALID_ARG, "unknown scheme");
+  oc_status st = check_boundaries(op);
+  if (st != OC_OK) return st;
+  st = ensure_ts(op, sc);
+  if (st != OC_OK) return st;
+  const size_t nz = op->n_dofs, nq = 2 * nz;
+  double *dz = z, *dq = q;
+  if (memory == OC_MEM_HOST) {
+    if (ensure(op, &op->ts_z, nz) || ensure(op, &op->ts_q, nq)) return OC_ERR_CUDA;
+    OC_TRY(cudaMemcpyAsync(op->ts_z, z, nz * 8, cudaMemcpyHostToDevice, op->stream));
+    OC_TRY(cudaMemcpyAsync(op->ts_q, q, nq * 8, cudaMemcpyHostToDevice, op->stream));
+    dz = op->ts_z; dq = op->ts_q;
+  }
+  // coefficients: rows a_i[stage] (b_i at the last stage) times dt
+  for (int s = 0; s < sc.s; ++s) {
+    StageDyn &d = op->h_dyn[s];
+    std::memset(&d, 0, sizeof(d));
+    const bool last = s == sc.s - 1;
+    for (int j = 0; j <= s; ++j) {
+      d.f[j] = (last ? sc.b[j] : sc.a[s][j]) * dt;
+      d.ft[j] = sc.ark ? (last ? sc.b[j] : sc.at[s][j]) * dt : 0.0;
+    }
+    d.fm = sc.ark && s < 2 ? sc.dt[s] * dt : 0.0;
+    d.time = time + sc.c[s] * dt;
+  }
+  OC_TRY(cudaMemcpyAsync(op->d_dyn, op->h_dyn, sizeof(StageDyn) * sc.s, cudaMemcpyHostToDevice,
+                         op->stream));
+  if (!op->graph || op->graph_scheme != scheme || op->graph_z != dz || op->graph_q != dq) {
+    if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
+    cudaGraph_t g;
+    OC_TRY(cudaStreamBeginCapture(op->stream, cudaStreamCaptureModeThreadLocal));
+    const int64_t before = op->launches;
+    st = enqueue_step(op, sc, dz, dq);
+    cudaError_t ce = cudaStreamEndCapture(op->stream, &g);
+    op->launches = before;
+    if (st != OC_OK) return st;
+    if (ce != cudaSuccess) return fail(op, OC_ERR_CUDA, cudaGetErrorString(ce));
+    OC_TRY(cudaGraphInstantiate(&op->graph, g, 0));
+    cudaGraphDestroy(g);
+    op->graph_scheme = scheme; op->graph_z = dz; op->graph_q = dq;
+  }
+  OC_TRY(cudaGraphLaunch(op->graph, op->stream));
+  for (int p = 1; p <= OC_MAXDEG; ++p) op->launches += op->group_n[p] ? sc.s : 0;
+  if (memory == OC_MEM_HOST) {
+    OC_TRY(cudaMemcpyAsync(z, op->ts_z, nz * 8, cudaMemcpyDeviceToHost, op->stream));
+    OC_TRY(cudaMemcpyAsync(q, op->ts_q, nq * 8, cudaMemcpyDeviceToHost, op->stream));
+    return read_error(op);
+  }
+  return OC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// auxiliary entry points
+// ---------------------------------------------------------------------------
+
+static AuxArgs aux_args(oc_op *op) {
+  AuxArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.n_cells = op->n_cells; a.deg = op->d_deg; a.off = op->d_off; a.geo = op->d_geo;
+  a.sd1 = op->d_sd[1]; a.sd2 = op->d_sd[2]; a.sdo1 = op->d_sdo[1]; a.sdo2 = op->d_sdo[2];
+  const double cu = op->prm.threshold_wetdry;
+  a.g = op->prm.g; a.cu4 = cu * cu * cu * cu;
+  for (int k = 0; k < 8; ++k) a.vortex[k] = op->vortex[k];
+  a.err = op->d_err;
+  return a;
+}
+
+extern "C" oc_status oc_transport_speed(oc_op *op, const double *z, const double *q,
+                                        int32_t memory, double *speed) {
+  if (!op || !z || !q || !speed) return OC_ERR_INVALID_ARG;
+  const size_t nz = op->n_dofs, nq = 2 * nz;
+  const double *dz = z, *dq = q;
+  if (memory == OC_MEM_HOST) {
+    if (ensure(op, &op->st_rz, nz) || ensure(op, &op->st_rq, nq)) return OC_ERR_CUDA;
+    OC_TRY(cudaMemcpyAsync(op->st_rz, z, nz * 8, cudaMemcpyHostToDevice, op->stream));
+    OC_TRY(cudaMemcpyAsync(op->st_rq, q, nq * 8, cudaMemcpyHostToDevice, op->stream));
+    dz = op->st_rz; dq = op->st_rq;
+  }
+  OC_TRY(cudaMemsetAsync(op->d_speed, 0, sizeof(unsigned long long), op->stream));
+  OC_TRY(launch_transport_speed(aux_args(op), dz, dq, op->d_speed, op->stream));
+  op->launches++;
+  unsigned long long bits = 0;
+  OC_TRY(cudaMemcpyAsync(&bits, op->d_speed, 8, cudaMemcpyDeviceToHost, op->stream));
+  oc_status st = read_error(op);
+  double v;
+  std::memcpy(&v, &bits, 8);
+  *speed = v;
+  return st;
+}
+
+extern "C" oc_status oc_apply(oc_op *op, double time, const double *sz, const double *sq,
+                              double *dz, double *dq, int32_t memory) {
+  if (!op || !sz || !sq || !dz || !dq) return OC_ERR_INVALID_ARG;
+  oc_status st = check_boundaries(op);
+  if (st != OC_OK) return st;
+  const size_t nz = op->n_dofs, nq = 2 * nz;
+  const double *isz = sz, *isq = sq;
+  double *odz = dz, *odq = dq;
+  if (memory == OC_MEM_HOST) {
+    if (ensure(op, &op->st_rz, nz) || ensure(op, &op->st_rq, nq) || ensure(op, &op->st_nz, nz) ||
+        ensure(op, &op->st_nq, nq))
+      return OC_ERR_CUDA;
+    OC_TRY(cudaMemcpyAsync(op->st_rz, sz, nz * 8, cudaMemcpyHostToDevice, op->stream));
+    OC_TRY(cudaMemcpyAsync(op->st_rq, sq, nq * 8, cudaMemcpyHostToDevice, op->stream));
+    isz = op->st_rz; isq = op->st_rq; odz = op->st_nz; odq = op->st_nq;
+  }
+  StageArgs a;
+  fill_common(op, a);
+  StageDyn &dy = op->h_dyn[OC_MAXSTAGES];
+  std::memset(&dy, 0, sizeof(dy));
+  dy.time = time;
+  OC_TRY(cudaMemcpyAsync(op->d_dyn + OC_MAXSTAGES, &dy, sizeof(dy), cudaMemcpyHostToDevice, op->stream));
+  a.dyn = op->d_dyn + OC_MAXSTAGES;
+  a.apply_mode = 1; a.n_stages = 1;
+  a.rz = isz; a.rq = isq; a.un_z = isz; a.un_q = isq; a.out_z = odz; a.out_q = odq;
+  // FP64 variant: apply() is the plain operator
+  const int saved = op->prm.precision;
+  st = launch_groups(op, a, saved == OC_PREC_MIXED ? 2 : 0);
+  if (st != OC_OK) return st;
+  if (memory == OC_MEM_HOST) {
+    OC_TRY(cudaMemcpyAsync(dz, odz, nz * 8, cudaMemcpyDeviceToHost, op->stream));
+    OC_TRY(cudaMemcpyAsync(dq, odq, nq * 8, cudaMemcpyDeviceToHost, op->stream));
+  }
+  return read_error(op);
+}
+
+extern "C" oc_status oc_velocity_field(oc_op *op, const double *z, const double *q, double *u,
+                                       int32_t memory) {
+  if (!op || !z || !q || !u) return OC_ERR_INVALID_ARG;
+  const size_t nz = op->n_dofs, nq = 2 * nz;
+  const double *dz = z, *dq = q;
+  double *du = u;
+  if (memory == OC_MEM_HOST) {
+    if (ensure(op, &op->st_rz, nz) || ensure(op, &op->st_rq, nq) || ensure(op, &op->st_nq, nq))
+      return OC_ERR_CUDA;
+    OC_TRY(cudaMemcpyAsync(op->st_rz, z, nz * 8, cudaMemcpyHostToDevice, op->stream));
+    OC_TRY(cudaMemcpyAsync(op->st_rq, q, nq * 8, cudaMemcpyHostToDevice, op->stream));
+    dz = op->st_rz; dq = op->st_rq; du = op->st_nq;
+  }
+  OC_TRY(launch_velocity_field(aux_args(op), dz, dq, du, op->stream));
+  op->launches++;
+  if (memory == OC_MEM_HOST)
+    OC_TRY(cudaMemcpyAsync(u, du, nq * 8, cudaMemcpyDeviceToHost, op->stream));
+  return read_error(op);
+}
+
+extern "C" oc_status oc_vorticity_indicator(oc_op *op, const double *u, int32_t nq1d,
+                                            float *ind, int32_t memory) {
+  if (!op || !u || !ind || nq1d < 1 || nq1d > 8) return OC_ERR_INVALID_ARG;
+  const size_t nq = 2 * op->n_dofs;
+  // basis values/derivatives at QGauss(nq1d) for every degree
+  std::vector<double> B(OC_MAXDEG * 8 * OC_MAXN, 0.0), Dm(OC_MAXDEG * 8 * OC_MAXN, 0.0);
+  double xq[16], wq[16], xn[16], wn[16];
+  gauss_rule(nq1d, xq, wq);
+  for (int p = 1; p <= OC_MAXDEG; ++p) {
+    lobatto_rule(p + 1, xn, wn);
+    for (int k = 0; k < nq1d; ++k)
+      for (int i = 0; i <= p; ++i) {
+        B[((p - 1) * 8 + k) * OC_MAXN + i] = lag(p + 1, xn, i, xq[k]);
+        Dm[((p - 1) * 8 + k) * OC_MAXN + i] = lag_d(p + 1, xn, i, xq[k]);
+      }
+  }
+  double *dB = nullptr, *dD = nullptr;
+  OC_TRY(cudaMalloc((void **)&dB, B.size() * 8));
+  OC_TRY(cudaMalloc((void **)&dD, Dm.size() * 8));
+  OC_TRY(cudaMemcpyAsync(dB, B.data(), B.size() * 8, cudaMemcpyHostToDevice, op->stream));
+  OC_TRY(cudaMemcpyAsync(dD, Dm.data(), Dm.size() * 8, cudaMemcpyHostToDevice, op->stream));
+  const double *du = u;
+  float *dind = ind;
+  float *tmp = nullptr;
+  if (memory == OC_MEM_HOST) {
+    if (ensure(op, &op->st_nq, nq)) return OC_ERR_CUDA;
+    OC_TRY(cudaMemcpyAsync(op->st_nq, u, nq * 8, cudaMemcpyHostToDevice, op->stream));
+    du = op->st_nq;
+    OC_TRY(cudaMalloc((void **)&tmp, op->n_cells * sizeof(float)));
+    dind = tmp;
+  }
+  OC_TRY(launch_vorticity(aux_args(op), du, nq1d, dB, dD, dind, op->stream));
+  op->launches++;
+  if (memory == OC_MEM_HOST)
+    OC_TRY(cudaMemcpyAsync(ind, tmp, op->n_cells * sizeof(float), cudaMemcpyDeviceToHost, op->stream));
+  oc_status st = read_error(op);
+  cudaFree(dB); cudaFree(dD);
+  if (tmp) cudaFree(tmp);
+  return st;
+}
+
+extern "C" oc_status oc_project_vortex(oc_op *op, double time, double *z, double *q,
+                                       int32_t memory) {
+  if (!op || !z || !q) return OC_ERR_INVALID_ARG;
+  const size_t nz = op->n_dofs, nq = 2 * nz;
+  double *dz = z, *dq = q;
+  if (memory == OC_MEM_HOST) {
+    if (ensure(op, &op->st_nz, nz) || ensure(op, &op->st_nq, nq)) return OC_ERR_CUDA;
+    dz = op->st_nz; dq = op->st_nq;
+  }
+  OC_TRY(launch_project_vortex(aux_args(op), time, dz, dq, op->stream));
+  op->launches++;
+  if (memory == OC_MEM_HOST) {
+    OC_TRY(cudaMemcpyAsync(z, dz, nz * 8, cudaMemcpyDeviceToHost, op->stream));
+    OC_TRY(cudaMemcpyAsync(q, dq, nq * 8, cudaMemcpyDeviceToHost, op->stream));
+  }
+  return read_error(op);
+}

@@ -1,0 +1,228 @@
+// Cell-local kernels around the stage: transport speed (dt), velocity
+// projection, vorticity indicator and L2 projection of the vortex.  One
+// thread per cell, FP64, runtime degree; tables from this unit's constant copy.
+#include "oc_kernels.cuh"
+
+namespace oc {
+
+// values of the nodal tile u (N x N) at the n x n points of the 1D matrix B[n][N]
+__device__ inline void eval_tile(int N, int n, const double (*B)[OC_MAXN], const double *u,
+                                 double *out /* n*n */) {
+  double t[OC_MAXN * (OC_MAXQ + 2)];
+  for (int iy = 0; iy < N; ++iy)
+    for (int qx = 0; qx < n; ++qx) {
+      double s = 0;
+      for (int ix = 0; ix < N; ++ix) s += B[qx][ix] * u[iy * N + ix];
+      t[iy * n + qx] = s;
+    }
+  for (int qy = 0; qy < n; ++qy)
+    for (int qx = 0; qx < n; ++qx) {
+      double s = 0;
+      for (int iy = 0; iy < N; ++iy) s += B[qy][iy] * t[iy * n + qx];
+      out[qy * n + qx] = s;
+    }
+}
+
+// out = (Sinv (x) Sinv) in  (transform_from_q_points_to_basis on Gauss p+1)
+__device__ inline void from_points(int N, const double (*Si)[OC_MAXN], const double *in,
+                                   double *out) {
+  double t[OC_MAXN * OC_MAXN];
+  for (int qy = 0; qy < N; ++qy)
+    for (int ix = 0; ix < N; ++ix) {
+      double s = 0;
+      for (int qx = 0; qx < N; ++qx) s += Si[ix][qx] * in[qy * N + qx];
+      t[qy * N + ix] = s;
+    }
+  for (int iy = 0; iy < N; ++iy)
+    for (int ix = 0; ix < N; ++ix) {
+      double s = 0;
+      for (int qy = 0; qy < N; ++qy) s += Si[iy][qy] * t[qy * N + ix];
+      out[iy * N + ix] = s;
+    }
+}
+
+// OceanDG.h:2505-2580: max over cells and Gauss-Lobatto p+2 points of
+// sigma_max(J^-1) sqrt(g h) + |J^-1 u|_inf; positive doubles are ordered like
+// their bit patterns, so the grid maximum is an atomicMax on 64-bit words.
+__global__ void transport_speed_kernel(const AuxArgs a, const double *z, const double *q,
+                                       unsigned long long *out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  double local = 0;
+  if (c < a.n_cells) {
+    const int p = a.deg[c], N = p + 1, G = p + 2, n = N * N;
+    const DegTables<double> &tb = tab<double>(p);
+    const double *J = a.geo + 11 * (int64_t)c;
+    const int64_t zo = a.off[c];
+    double u[OC_MAXN * OC_MAXN], zv[OC_MAXF * OC_MAXF], q0[OC_MAXF * OC_MAXF],
+        q1[OC_MAXF * OC_MAXF];
+    for (int i = 0; i < n; ++i) u[i] = z[zo + i];
+    eval_tile(N, G, tb.BG, u, zv);
+    for (int i = 0; i < n; ++i) u[i] = q[2 * zo + i];
+    eval_tile(N, G, tb.BG, u, q0);
+    for (int i = 0; i < n; ++i) u[i] = q[2 * zo + n + i];
+    eval_tile(N, G, tb.BG, u, q1);
+    const double *zb1 = a.sd1 ? a.sd1 + a.sdo1[c] : nullptr;
+    for (int k = 0; k < G * G; ++k) {
+      const double zb = zb1 ? zb1[k] : 0.;
+      double v0, v1;
+      velocity<double>(zv[k], q0[k], q1[k], zb, a.cu4, v0, v1);
+      const double cs0 = J[6] * v0 + J[7] * v1, cs1 = J[8] * v0 + J[9] * v1;
+      double conv = 0;
+      conv = mx<double>(conv, fabs(cs0));
+      conv = mx<double>(conv, fabs(cs1));
+      const double sos = sqrt(a.g * depth<double>(zv[k], zb));
+      double e0 = 1., e1 = 1.;
+      for (int it = 0; it < 5; ++it) {
+        const double a0 = J[6] * e0 + J[7] * e1, a1 = J[8] * e0 + J[9] * e1;
+        e0 = J[6] * a0 + J[8] * a1;
+        e1 = J[7] * a0 + J[9] * a1;
+        double nrm = 0;
+        nrm = mx<double>(nrm, fabs(e0));
+        nrm = mx<double>(nrm, fabs(e1));
+        e0 /= nrm;
+        e1 /= nrm;
+      }
+      const double j0 = J[6] * e0 + J[7] * e1, j1 = J[8] * e0 + J[9] * e1;
+      const double mev = sqrt((j0 * j0 + j1 * j1) / (e0 * e0 + e1 * e1));
+      local = mx<double>(local, mev * sos + conv);
+    }
+    if (!isfinite(local)) {
+      atomicOr(a.err, ERR_NONFINITE);
+      local = 0;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) local = fmax(local, __shfl_xor_sync(OC_FULL, local, o));
+  if ((threadIdx.x & 31) == 0 && local > 0)
+    atomicMax(out, (unsigned long long)__double_as_longlong(local));
+}
+
+// OceanDG.h:2599-2662 (degree >= 1 path): u = S^-1 (velocity at Gauss p+1),
+// accumulated point by point into the cell's own output
+__global__ void velocity_field_kernel(const AuxArgs a, const double *z, const double *q,
+                                      double *u) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.n_cells) return;
+  const int p = a.deg[c], N = p + 1, n = N * N;
+  const DegTables<double> &tb = tab<double>(p);
+  const int64_t zo = a.off[c];
+  const double *zc = z + zo, *q0c = q + 2 * zo, *q1c = q + 2 * zo + n;
+  double *u0 = u + 2 * zo, *u1 = u + 2 * zo + n;
+  const double *sd = a.sd2 ? a.sd2 + a.sdo2[c] : nullptr;
+  for (int i = 0; i < 2 * n; ++i) u0[i] = 0.;
+  for (int qy = 0; qy < N; ++qy)
+    for (int qx = 0; qx < N; ++qx) {
+      double zv = 0, v0 = 0, v1 = 0;
+      for (int iy = 0; iy < N; ++iy)
+        for (int ix = 0; ix < N; ++ix) {
+          const double b = tb.BM[qy][iy] * tb.BM[qx][ix];
+          zv += b * zc[iy * N + ix];
+          v0 += b * q0c[iy * N + ix];
+          v1 += b * q1c[iy * N + ix];
+        }
+      double w0, w1;
+      velocity<double>(zv, v0, v1, sd ? sd[2 * (qy * N + qx)] : 0., a.cu4, w0, w1);
+      for (int iy = 0; iy < N; ++iy)
+        for (int ix = 0; ix < N; ++ix) {
+          const double s = tb.Sinv[iy][qy] * tb.Sinv[ix][qx];
+          u0[iy * N + ix] += s * w0;
+          u1[iy * N + ix] += s * w1;
+        }
+    }
+}
+
+// hpTuner.h:247-305: max over QGauss(nq) points of |dv/dx - du/dy|;
+// B/D: [degree-1][nq*OC_MAXN] values/derivatives of the basis at the points
+__global__ void vorticity_kernel(const AuxArgs a, const double *u, int nq, const double *B,
+                                 const double *Dm, float *out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.n_cells) return;
+  const int p = a.deg[c], N = p + 1, n = N * N;
+  const double *Bp = B + (p - 1) * 8 * OC_MAXN, *Dp = Dm + (p - 1) * 8 * OC_MAXN;
+  const double *J = a.geo + 11 * (int64_t)c;
+  const double *uc = u + 2 * (int64_t)a.off[c];
+  float mv = 0.f;
+  for (int qy = 0; qy < nq; ++qy)
+    for (int qx = 0; qx < nq; ++qx) {
+      double ux = 0, uy = 0, vx = 0, vy = 0;
+      for (int iy = 0; iy < N; ++iy)
+        for (int ix = 0; ix < N; ++ix) {
+          const double bx = Bp[qx * OC_MAXN + ix], by = Bp[qy * OC_MAXN + iy];
+          const double dx = Dp[qx * OC_MAXN + ix], dy = Dp[qy * OC_MAXN + iy];
+          const double uu = uc[iy * N + ix], vv = uc[n + iy * N + ix];
+          ux += dx * by * uu;
+          uy += bx * dy * uu;
+          vx += dx * by * vv;
+          vy += bx * dy * vv;
+        }
+      const double du_dy = J[7] * ux + J[9] * uy;  // physical d/dy of u
+      const double dv_dx = J[6] * vx + J[8] * vy;  // physical d/dx of v
+      const float w = (float)fabs(dv_dx - du_dy);
+      mv = w > mv ? w : mv;
+    }
+  out[c] = mv;
+}
+
+// OceanDG.h:2241-2352 with the vortex exact solution as the projected function:
+// zeta = S^-1 f0, q = S^-1 (f_{1,2} depth(f0, zb)) on Gauss p+1, accumulated
+// point by point into the cell's own outputs
+__global__ void project_vortex_kernel(const AuxArgs a, double time, double *z, double *q) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.n_cells) return;
+  const int p = a.deg[c], N = p + 1, n = N * N;
+  const DegTables<double> &tb = tab<double>(p);
+  const double *J = a.geo + 11 * (int64_t)c;
+  const double *sd = a.sd2 ? a.sd2 + a.sdo2[c] : nullptr;
+  const int64_t zo = a.off[c];
+  const VortexParams vp = vortex_params(a.vortex);
+  double *zc = z + zo, *q0 = q + 2 * zo, *q1 = q + 2 * zo + n;
+  for (int i = 0; i < n; ++i) zc[i] = 0.;
+  for (int i = 0; i < 2 * n; ++i) q0[i] = 0.;
+  for (int qy = 0; qy < N; ++qy)
+    for (int qx = 0; qx < N; ++qx) {
+      const double e0 = tb.xM[qx], e1 = tb.xM[qy];
+      const double x = J[0] + J[2] * e0 + J[3] * e1, y = J[1] + J[4] * e0 + J[5] * e1;
+      const double fz = vortex_value(vp, a.g, x, y, time, 0);
+      const double hq = depth<double>(fz, sd ? sd[2 * (qy * N + qx)] : 0.);
+      const double f1 = vortex_value(vp, a.g, x, y, time, 1) * hq;
+      const double f2 = vortex_value(vp, a.g, x, y, time, 2) * hq;
+      for (int iy = 0; iy < N; ++iy)
+        for (int ix = 0; ix < N; ++ix) {
+          const double s = tb.Sinv[iy][qy] * tb.Sinv[ix][qx];
+          zc[iy * N + ix] += s * fz;
+          q0[iy * N + ix] += s * f1;
+          q1[iy * N + ix] += s * f2;
+        }
+    }
+}
+
+cudaError_t aux_upload_tables(const DegTables<double> *td, const DegTables<float> *tf) {
+  cudaError_t e = cudaMemcpyToSymbol(c_tabd, td, sizeof(DegTables<double>) * OC_MAXDEG);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(c_tabf, tf, sizeof(DegTables<float>) * OC_MAXDEG);
+}
+
+cudaError_t launch_transport_speed(const AuxArgs &a, const double *z, const double *q,
+                                   unsigned long long *out, cudaStream_t st) {
+  transport_speed_kernel<<<(a.n_cells + 127) / 128, 128, 0, st>>>(a, z, q, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_velocity_field(const AuxArgs &a, const double *z, const double *q, double *u,
+                                  cudaStream_t st) {
+  velocity_field_kernel<<<(a.n_cells + 127) / 128, 128, 0, st>>>(a, z, q, u);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vorticity(const AuxArgs &a, const double *u, int nq, const double *B,
+                             const double *D, float *out, cudaStream_t st) {
+  vorticity_kernel<<<(a.n_cells + 127) / 128, 128, 0, st>>>(a, u, nq, B, D, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_project_vortex(const AuxArgs &a, double time, double *z, double *q,
+                                  cudaStream_t st) {
+  project_vortex_kernel<<<(a.n_cells + 127) / 128, 128, 0, st>>>(a, time, z, q);
+  return cudaGetLastError();
+}
+
+}  // namespace oc

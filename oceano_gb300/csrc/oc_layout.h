@@ -1,0 +1,94 @@
+// Shared host/device layout of the GPU operator: table sizes, per-degree
+// shape tables and the argument block of the stage kernels.
+#pragma once
+#include <cstdint>
+
+#define OC_MAXN 5      // nodes per direction, p <= 4
+#define OC_MAXQ 7      // floor(1.5*4)+1 Gauss points per direction
+#define OC_MAXF 6      // Gauss-Lobatto points per face, max(p-,p+)+2 <= 6
+#define OC_MAXBID 16   // boundary ids
+#define OC_MAXSTAGES 4
+#define OC_MAXDEG 4
+
+// Per-degree tables; matrices are [point][node] on [0,1].
+template <typename R>
+struct DegTables {
+  R BQ[OC_MAXQ][OC_MAXN], DQ[OC_MAXQ][OC_MAXN], wQ[OC_MAXQ], xQ[OC_MAXQ];  // Gauss floor(1.5p)+1
+  R BG[OC_MAXF][OC_MAXN], wG[OC_MAXF];                        // Gauss-Lobatto p+2
+  R BM[OC_MAXN][OC_MAXN], Sinv[OC_MAXN][OC_MAXN], wM[OC_MAXN], xM[OC_MAXN];  // Gauss p+1
+  R F[3][OC_MAXF + 1][OC_MAXF][OC_MAXN];  // [0 full face | 1,2 subface 0,1][nf][k][node]
+  R wF[OC_MAXF + 1][OC_MAXF];             // Gauss-Lobatto nf weights
+  R lump[OC_MAXN];                        // 1D lumped GL(p+2) mass
+  R W1[OC_MAXN][OC_MAXN], W2[OC_MAXN][OC_MAXN], Gk[OC_MAXN][OC_MAXN];  // closed-form sweeps
+};
+
+template <typename R>
+inline void cast_tables(const DegTables<double> &a, DegTables<R> &b) {
+  const double *s = reinterpret_cast<const double *>(&a);
+  R *d = reinterpret_cast<R *>(&b);
+  for (unsigned i = 0; i < sizeof(DegTables<double>) / sizeof(double); ++i) d[i] = (R)s[i];
+}
+
+// Per-call coefficients, read by the kernels from device memory so that a
+// captured CUDA graph stays valid when dt or the time change.
+struct StageDyn {
+  double f[OC_MAXSTAGES], ft[OC_MAXSTAGES];
+  double fm, time;
+};
+
+// Face references of a cell slot: >= 0: 2*inner_face + side (0 minus, 1 plus);
+// < -1: boundary face b encoded as -(b+2); -1: empty.
+struct StageArgs {
+  // mesh
+  int n_group;                 // cells processed by this launch
+  const int *group_cells;      // their ids (NULL: identity starting at group_first)
+  int group_first;
+  const int *deg;              // [n_cells]
+  const int *off;              // [n_cells] zeta offset (discharge: 2*off)
+  const double *geo;           // [n_cells*11]: x0,y0,J00,J01,J10,J11,Ji00,Ji01,Ji10,Ji11,det
+  const int *slots;            // [n_cells*8]: 2 refs per face number
+  const int *fcm, *fcp;        // [n_inner+n_bnd], [n_inner]
+  const int *fpack;            // fm | fp<<4 | (sub+1)<<8 | orient<<12 | nf<<16
+  const double *fnrm;          // [n_faces*2] minus normal
+  const double *flen;          // [n_faces]
+  const int *fsd;              // inner: offset into sdf; boundary: offset into sdb
+  const int *bbid;             // [n_bnd] boundary id
+  int n_inner;
+  // static data (NULL = zero); *e arrays are FP32 copies with zeta_reference folded into zb
+  const double *sd0, *sd1, *sd2, *sdf, *sdb;
+  const float *sd0e, *sd1e, *sd2e, *sdfe, *sdbe;
+  const int *sdo0, *sdo1, *sdo2; // per cell offsets
+  // stage vectors
+  const void *rz, *rq, *rvel;  // stage input (double, or float deviations in mixed mode)
+  int r_is_float;
+  const double *un_z, *un_q;   // solution u^n (FP64)
+  void *kz[OC_MAXSTAGES + 1];  // residual registers (double or float)
+  void *kq[2 * OC_MAXSTAGES];
+  double *out_z, *out_q;       // next_ri or solution (FP64)
+  float *out_rz, *out_rq;      // mixed: FP32 stage input of the next stage (may be NULL)
+  double *aux_q;               // ARK last stage: next_ri_discharge receives M^-1 rhs
+  const struct StageDyn *dyn;  // device copy of the per-call coefficients
+  int stage, n_stages, ark, last, write_kq_last, apply_mode;
+  // model
+  double g, cu4, nu, zeta_ref, wet_threshold;
+  int friction, max_iter, batch;
+  // boundary conditions
+  int bc_kind[OC_MAXBID], bc_fn[OC_MAXBID];
+  double bc_c[OC_MAXBID][3];
+  double vortex[8];
+  // status word (bit flags of oc_status codes)
+  int *err;
+};
+
+// Arguments of the cell-local auxiliary kernels (transport speed, velocity,
+// vorticity, projection).
+struct AuxArgs {
+  int n_cells;
+  const int *deg, *off;
+  const double *geo;
+  const double *sd1, *sd2;  // zb at Gauss-Lobatto p+2; (zb, cf) at Gauss p+1
+  const int *sdo1, *sdo2;
+  double g, cu4;
+  double vortex[8];
+  int *err;
+};
