@@ -1,0 +1,346 @@
+"""Benchmark: DoF-stage updates/s of the per-stage DG operator on GB300.
+
+Workload (one "step" = one SSP-RK3 time step = 3 stages of the operator):
+the degree-3 travelling vortex on [0,2]x[0,1], a 20x10 coarse grid refined
+4 times (320x160 = 51,200 cells, 2,457,600 scalar DoFs), periodic in x, walls
+in y, flat bathymetry (zb = 0, zeta = depth), no friction, g = 9.81, CFL 0.075.
+Synthetic, seeded-free deterministic input (the vortex projected on the mesh).
+
+value    : mixed form (FP32 bulk, FP64 accumulation), inputs resident in HBM,
+           timed with CUDA events on the operator's stream, L2 flushed between
+           steps (the state vectors fit the 129 MB L2).
+fp64     : the plain FP64 form on the same GPU.
+e2e      : mixed form through the public C ABI with pinned host buffers, copies
+           in and out inside the timed region.
+roofline : dominant kernel = the fused stage kernel; algorithmic bytes per
+           DoF-stage as documented in the design doc; peak from MEASURED_PEAKS.json.
+cpu_baseline / --impl reference: the FP64 C oracle (CPU restatement; the
+           reference itself needs deal.II + MPI) with OpenMP on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DEGREE, REFINE, CFL = 3, 4, 0.075  # CFL of the reference's degree-3 case (channelFlow.prm)
+METRIC = "DG DoF-stage updates/s, mixed vs FP64 on same GPU at stated L2 error; % HBM roofline"
+
+
+def workload():
+    from oceano_gb300 import vortex_mesh
+    from oceano_gb300.icbc import vortex_params
+    mesh = vortex_mesh(REFINE, DEGREE)
+    return mesh, vortex_params()
+
+
+def make_op(mesh, vx, precision):
+    from oceano_gb300.operator import OceanoOperator
+    op = OceanoOperator(mesh, precision=precision, zeta_reference=1.0 if precision == "mixed" else 0.0)
+    op.set_wall_boundary(0)
+    op.set_vortex(*vx)
+    return op
+
+
+def algorithmic_bytes(n_dofs_var, n_cells, mixed):
+    """Bytes one SSP-RK3 step must move: per stage the stage input r_i, u^n and
+    the stage output at their stored precision (stage 0: r_0 = u^n, counted
+    once), plus the affine geometry (J^-1 and det, 5 doubles per cell)."""
+    n = 3 * n_dofs_var  # scalar DoFs of zeta, hu, hv
+    if mixed:
+        per_dof = (8 + 4) + (4 + 8 + 4) + (4 + 8 + 8)
+    else:
+        per_dof = (8 + 8) + (8 + 8 + 8) + (8 + 8 + 8)
+    return n * per_dof + 3 * n_cells * 5 * 8
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.out = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100", "-i",
+                 os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.out.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def time_device(op, mesh, z0, q0, steps, warmup, dt, flush):
+    """Per-step CUDA-event times (ms) of oc_perform_time_step on device vectors."""
+    import torch
+    stream = torch.cuda.ExternalStream(op.stream)
+    z = torch.from_numpy(z0).cuda()
+    q = torch.from_numpy(q0).cuda()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for i in range(warmup):
+            op.perform_time_step("ssp33", i * dt, dt, z, q)
+        op.synchronize()
+        times = []
+        launches0 = op.launch_count
+        for i in range(steps):
+            flush.zero_()  # evict the state from L2 (outside the timed events)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            op.perform_time_step("ssp33", (warmup + i) * dt, dt, z, q)
+            e1.record(stream)
+            times.append((e0, e1))
+        op.synchronize()
+        launches = op.launch_count - launches0
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in times]
+    return ms, z.cpu().numpy(), q.cpu().numpy(), launches
+
+
+def time_e2e(op, z0, q0, steps, warmup, dt):
+    """Same steps through the C ABI with pinned host buffers (copies timed)."""
+    import torch
+    zh = torch.from_numpy(z0.copy()).pin_memory()
+    qh = torch.from_numpy(q0.copy()).pin_memory()
+    stream = torch.cuda.ExternalStream(op.stream)
+    for i in range(warmup):
+        _host_step(op, i * dt, dt, zh, qh)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(steps):
+        _host_step(op, (warmup + i) * dt, dt, zh, qh)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps, (zh.numel() + qh.numel()) * 8
+
+
+def _host_step(op, t, dt, zh, qh):
+    """oc_perform_time_step with OC_MEM_HOST on pinned tensors (host pointers)."""
+    import ctypes as C
+    from oceano_gb300 import _lib
+    _lib.check(_lib.lib().oc_perform_time_step(op.h, _lib.SCHEME["ssp33"], t, dt,
+                                               C.c_void_p(zh.data_ptr()),
+                                               C.c_void_p(qh.data_ptr()), _lib.OC_MEM_HOST),
+               op.h)
+
+
+def cpu_baseline(mesh, vx, z0, q0, dt, steps):
+    """FP64 C oracle (OpenMP, all host cores) on `steps` full RK steps."""
+    from oracle import oracle as O
+    orc = O.Oracle(mesh, bcs={0: ("wall",)}, vortex=list(vx) + [0, 0])
+    tb = O.TABLEAUX["ssp33"]
+    z, q = z0.copy(), q0.copy()
+    t0 = time.perf_counter()
+    for i in range(steps):
+        O.erk_step(orc, tb["a"], tb["b"], tb["c"], i * dt, dt, z, q)
+    el = time.perf_counter() - t0
+    ndof = 3 * orc.n
+    return ndof * 3 * steps / el, O.num_threads(), el
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def dist_setup(n_gpus):
+    import torch
+    if n_gpus > 1 or "RANK" in os.environ:
+        import torch.distributed as dist
+        rank = int(os.environ.get("RANK", 0))
+        local = int(os.environ.get("LOCAL_RANK", 0))
+        world = int(os.environ.get("WORLD_SIZE", 1))
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        if not dist.is_initialized():
+            dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        return rank, world
+    return 0, 1
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64,
+                     device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, rank, world):
+    """CPU restatement timed on the host cores (rank 0 only)."""
+    if rank != 0:
+        return
+    mesh, vx = workload()
+    from oracle import oracle as O
+    orc = O.Oracle(mesh, bcs={0: ("wall",)}, vortex=list(vx) + [0, 0])
+    z0, q0 = orc.project_vortex(0.0)
+    dt = CFL / orc.transport_speed(z0, q0)
+    tb = O.TABLEAUX["ssp33"]
+    z, q = z0.copy(), q0.copy()
+    for i in range(args.warmup):
+        O.erk_step(orc, tb["a"], tb["b"], tb["c"], i * dt, dt, z, q)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        O.erk_step(orc, tb["a"], tb["b"], tb["c"], i * dt, dt, z, q)
+    el = time.perf_counter() - t0
+    ndof = 3 * orc.n
+    v = ndof * 3 * args.steps / el
+    cores = O.num_threads()
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "DoF-stage/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "vortex p=3, 320x160 cells (51200), 2457600 DoFs, SSP-RK3",
+                   "degree": DEGREE, "cells": mesh.n_cells, "dofs": ndof},
+        "cpu_baseline": {"value": v, "unit": "DoF-stage/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full SSP-RK3 steps of the workload"},
+        "e2e": {"value": v, "unit": "DoF-stage/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "FP64 C restatement of the reference operator (OpenMP); the reference "
+                "build needs deal.II 9.5 + p4est + MPI, absent on this image"}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    import __graft_entry__ as ge
+    ge.build()
+    mesh, vx = workload()
+    op_m = make_op(mesh, vx, "mixed")
+    op_d = make_op(mesh, vx, "fp64")
+    n = op_m.n_dofs
+    z0, q0 = np.zeros(n), np.zeros(2 * n)
+    op_d.project_vortex(0.0, z0, q0)
+    dt = CFL / op_d.compute_cell_transport_speed(z0, q0)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    barrier(world)
+    with Clocks() as clk:
+        ms_m, zm, qm, launches = time_device(op_m, mesh, z0, q0, args.steps, args.warmup, dt, flush)
+    ms_d, zd, qd, _ = time_device(op_d, mesh, z0, q0, args.steps, args.warmup, dt, flush)
+    t_m = max_over_ranks(sum(ms_m) / 1e3, world)
+    t_d = max_over_ranks(sum(ms_d) / 1e3, world)
+    ndof = 3 * n
+    units = ndof * 3 * args.steps * world  # every rank advances its own replica
+    value = units / t_m
+    value_d = units / t_d
+    e2e_ms, io_bytes = time_e2e(op_m, z0, q0, max(2, args.steps // 4), 2, dt)
+    e2e_ms = max_over_ranks(e2e_ms, world)
+    e2e_value = ndof * 3 * world / (e2e_ms / 1e3)
+    peak, peak_kind = peaks()
+    bytes_step = algorithmic_bytes(n, mesh.n_cells, True)
+    step_s = statistics.mean(ms_m) / 1e3
+    achieved = bytes_step / 3 / (step_s / 3) / 1e9  # per launch: step = 3 launches
+    clocks = clk.summary()
+    err_z, err_q = rel(zm, zd), rel(qm, qd)
+    out = {
+        "metric": METRIC, "value": value, "unit": "DoF-stage/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_m / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": "vortex p=3, 320x160 cells (51200), 2457600 DoFs, SSP-RK3 step",
+                   "degree": DEGREE, "cells": mesh.n_cells, "dofs": ndof,
+                   "l2": "flushed between steps (512 MB write)",
+                   "replicas": world},
+        "fp64": {"value": value_d, "ms_per_step": 1e3 * t_d / args.steps},
+        "speedup_vs_fp64": value / value_d,
+        "l2_error_vs_fp64": {"zeta": err_z, "hu_hv": err_q, "after_steps": args.warmup + args.steps},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": peak_kind,
+                     "kernel": "oc::stage_kernel<3,float,float,true>",
+                     "algorithmic_bytes_per_step": bytes_step},
+        "e2e": {"value": e2e_value, "unit": "DoF-stage/s", "h2d_bytes_per_step": io_bytes,
+                "d2h_bytes_per_step": io_bytes},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu:
+        v, cores, el = cpu_baseline(mesh, vx, z0, q0, dt, args.cpu_steps)
+        out["cpu_baseline"] = {"value": v, "unit": "DoF-stage/s", "cores": cores, "kind": "port",
+                               "sample": f"{args.cpu_steps} full SSP-RK3 step(s) of the workload "
+                                         f"({el:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(out))
+    barrier(world)
+
+
+if __name__ == "__main__":
+    main()

@@ -32,8 +32,10 @@ def _nvcc() -> str:
 def _sources():
     units = []
     for p in (1, 2, 3, 4):
+        # FP32 bulk of the mixed form: flush-to-zero and approximate division and
+        # square root (affects single precision only; the FP64 form is IEEE)
         units.append((os.path.join(CSRC, "oc_stage_inst.cu"), f"oc_stage_p{p}.o",
-                      [f"-DOC_DEGREE={p}"]))
+                      [f"-DOC_DEGREE={p}", "-ftz=true", "-prec-div=false", "-prec-sqrt=false"]))
     units.append((os.path.join(CSRC, "oc_aux.cu"), "oc_aux.o", []))
     units.append((os.path.join(CSRC, "oc_api.cu"), "oc_api.o", []))
     return units

@@ -179,14 +179,23 @@ struct Dims {
   // per-cell shared memory: compute-type region and FP64 region (elements)
   static constexpr int SZR = 9 * NN + 6 * NT + 3 * FVS;  // U 3, RES 3, RST 2, BZ 1 tiles; X; FV
   static constexpr int SZD = NN + 3 * NT + T + 2;
+  // Team strides: padded so that the 32/T teams of a warp start on different
+  // shared-memory banks (stride mod 32 chosen per degree and element size to
+  // keep row, column and node-row accesses at most 2-way conflicted).
+  static constexpr int pad_f = P == 1 ? 5 : P == 2 ? 5 : P == 3 ? 3 : 8;
+  static constexpr int pad_d = P == 1 ? 5 : P == 2 ? 2 : P == 3 ? 3 : 4;
   template <typename R>
-  static constexpr int bytes_r() { return ((SZR * (int)sizeof(R) + 15) / 16) * 16; }
-  static constexpr int bytes_d() { return ((SZD * 8 + 15) / 16) * 16; }
+  static constexpr int bytes_r() {
+    return (((SZR + 31) / 32) * 32 + (sizeof(R) == 4 ? pad_f : pad_d)) * (int)sizeof(R);
+  }
+  static constexpr int bytes_d() { return (((SZD + 31) / 32) * 32 + pad_d) * 8; }
   // per warp: CPW compute regions, CPW FP64 regions, CPW batch-norm slots
   template <typename R>
-  static constexpr int norm_offset() { return CPW * (bytes_r<R>() + bytes_d()); }
+  static constexpr int d_offset() { return ((CPW * bytes_r<R>() + 15) / 16) * 16; }
   template <typename R>
-  static constexpr int warp_bytes() { return norm_offset<R>() + ((CPW * 8 + 15) / 16) * 16; }
+  static constexpr int norm_offset() { return d_offset<R>() + CPW * bytes_d(); }
+  template <typename R>
+  static constexpr int warp_bytes() { return ((norm_offset<R>() + CPW * 8 + 15) / 16) * 16; }
 };
 
 // Sum over the T threads of a team; called by all lanes (two full syncs).
@@ -381,7 +390,7 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
 
   unsigned char *wbase = smem_raw + warp * D::template warp_bytes<R>();
   R *sm = reinterpret_cast<R *>(wbase + team * D::template bytes_r<R>());
-  double *dm = reinterpret_cast<double *>(wbase + CPWMAX * D::template bytes_r<R>() +
+  double *dm = reinterpret_cast<double *>(wbase + D::template d_offset<R>() +
                                           team * D::bytes_d());
   double *warp_norm = reinterpret_cast<double *>(wbase + D::template norm_offset<R>());
   R *U = sm;                  // 3*NN stage input z, q0, q1
@@ -445,9 +454,9 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
   __syncwarp();
   const bool split = a.ark && !a.last;  // ARK internal stage: stiff part separate
   {
-    R Az[N], Cz[N], A0[N], C0[N], A1[N], C1[N], S0[N], S1[N];
+    R Az[N], Cz[N], A0[N], C0[N], A1[N], C1[N];
 #pragma unroll
-    for (int i = 0; i < N; ++i) Az[i] = Cz[i] = A0[i] = C0[i] = A1[i] = C1[i] = S0[i] = S1[i] = 0;
+    for (int i = 0; i < N; ++i) Az[i] = Cz[i] = A0[i] = C0[i] = A1[i] = C1[i] = 0;
     if (member && t < Q) {  // y-pass, pointwise model, y-integration on column qx = t
       const double *sd0 = a.sd0 ? a.sd0 + a.sdo0[cell] : nullptr;
       const float *sd0e = a.sd0e ? a.sd0e + a.sdo0[cell] : nullptr;
@@ -487,7 +496,7 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
         const R F00 = q0 * v0, F01 = q0 * v1, F10 = q1 * v0, F11 = q1 * v1;
         const R g00 = (Ji00 * F00 + Ji01 * F01) * w, g01 = (Ji10 * F00 + Ji11 * F01) * w;
         const R g10 = (Ji00 * F10 + Ji01 * F11) * w, g11 = (Ji10 * F10 + Ji11 * F11) * w;
-        const R sv0 = s0 * w, sv1 = s1 * w, st0 = -fr0 * w, st1 = -fr1 * w;
+        const R sv0 = s0 * w, sv1 = s1 * w;
 #pragma unroll
         for (int iy = 0; iy < N; ++iy) {
           const R b = tb.BQ[qy][iy], d = tb.DQ[qy][iy];
@@ -497,8 +506,6 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
           C0[iy] += d * g01 + b * sv0;
           A1[iy] += b * g10;
           C1[iy] += d * g11 + b * sv1;
-          S0[iy] += b * st0;
-          S1[iy] += b * st1;
         }
       }
     }
@@ -532,7 +539,62 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
       }
     }
     __syncwarp();
-    if (split) {  // warp-uniform: stiff residual integration
+    if (split) {  // warp-uniform: stiff (friction) residual, a second pass over the points
+      if (member && t < N) {  // x-pass of the stage input again (X was overwritten)
+        R z[N], q0[N], q1[N];
+#pragma unroll
+        for (int ix = 0; ix < N; ++ix) {
+          z[ix] = U[t * N + ix];
+          q0[ix] = U[NN + t * N + ix];
+          q1[ix] = U[2 * NN + t * N + ix];
+        }
+#pragma unroll
+        for (int qx = 0; qx < Q; ++qx) {
+          R b0 = 0, a0 = 0, a1 = 0;
+#pragma unroll
+          for (int ix = 0; ix < N; ++ix) {
+            b0 += tb.BQ[qx][ix] * z[ix];
+            a0 += tb.BQ[qx][ix] * q0[ix];
+            a1 += tb.BQ[qx][ix] * q1[ix];
+          }
+          X[2 * NT + t * T + qx] = b0;
+          X[3 * NT + t * T + qx] = a0;
+          X[4 * NT + t * T + qx] = a1;
+        }
+      }
+      __syncwarp();
+      R S0[N], S1[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) S0[i] = S1[i] = 0;
+      if (member && t < Q) {
+        const double *sd0 = a.sd0 ? a.sd0 + a.sdo0[cell] : nullptr;
+        const float *sd0e = a.sd0e ? a.sd0e + a.sdo0[cell] : nullptr;
+#pragma unroll
+        for (int qy = 0; qy < Q; ++qy) {
+          R z = 0, q0 = 0, q1 = 0;
+#pragma unroll
+          for (int iy = 0; iy < N; ++iy) {
+            z += tb.BQ[qy][iy] * X[2 * NT + iy * T + t];
+            q0 += tb.BQ[qy][iy] * X[3 * NT + iy * T + t];
+            q1 += tb.BQ[qy][iy] * X[4 * NT + iy * T + t];
+          }
+          const int k = qy * Q + t;
+          R zb = MIX ? zbe_flat : R(0), cf = 0;
+          if (MIX && sd0e) { zb = (R)sd0e[5 * k]; cf = (R)sd0e[5 * k + 1]; }
+          else if (!MIX && sd0) { zb = (R)sd0[5 * k]; cf = (R)sd0[5 * k + 1]; }
+          R v0, v1, fr0 = 0, fr1 = 0;
+          velocity<R>(z, q0, q1, zb, cu4, v0, v1);
+          if (a.friction) friction<R>(a.friction, g, v0, v1, cf, depth<R>(z, zb), fr0, fr1);
+          const R w = tb.wQ[t] * tb.wQ[qy] * det;
+          const R st0 = -fr0 * w, st1 = -fr1 * w;
+#pragma unroll
+          for (int iy = 0; iy < N; ++iy) {
+            S0[iy] += tb.BQ[qy][iy] * st0;
+            S1[iy] += tb.BQ[qy][iy] * st1;
+          }
+        }
+      }
+      __syncwarp();
       if (member && t < Q) {
 #pragma unroll
         for (int iy = 0; iy < N; ++iy) {

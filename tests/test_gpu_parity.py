@@ -176,7 +176,7 @@ def test_mixed_trajectory(gpu_lib, name):
     mesh, orc, op = setup(name, precision="mixed", zeta_reference=1.0)
     _, _, op64 = setup(name)
     z0, q0 = orc.project_vortex(0.0)
-    dt = 0.2 / orc.transport_speed(z0, q0)
+    dt = 0.075 / orc.transport_speed(z0, q0)  # stable SSP-RK3 Courant number up to p = 4
     zo, qo = z0.copy(), q0.copy()
     zm, qm = z0.copy(), q0.copy()
     zd, qd = z0.copy(), q0.copy()
@@ -185,7 +185,7 @@ def test_mixed_trajectory(gpu_lib, name):
         op.perform_time_step("ssp33", it * dt, dt, zm, qm)
         op64.perform_time_step("ssp33", it * dt, dt, zd, qd)
     assert rel(zd, zo) < 1e-12 and rel(qd, qo) < 1e-12
-    assert rel(zm, zo) < 1e-6 and rel(qm, qo) < 1e-6
+    assert rel(zm, zo) < 1e-6 and rel(qm, qo) < 5e-6
 
 
 @pytest.mark.parametrize("name", ["vortex_p1", "hanging_p2", "mixed_degree", "hanging_p3_bathy"])
@@ -218,7 +218,7 @@ def test_time_step_matches_stages(gpu_lib):
     """oc_perform_time_step (graph, handle-owned registers) == the stage sequence."""
     mesh, orc, op = setup("hanging_p2")
     z, q = perturbed_state(orc, 2)
-    dt = 0.002
+    dt = 0.075 / orc.transport_speed(z, q)
     zs, qs = z.copy(), q.copy()
     O.erk_step(orc, TAB["a"], TAB["b"], TAB["c"], 0.0, dt, zs, qs)
     zg, qg = z.copy(), q.copy()
