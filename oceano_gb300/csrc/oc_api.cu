@@ -9,7 +9,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/oceano_gpu.h"
+#include "oceano_gpu.h"
 #include "oc_layout.h"
 #include "oc_tables.hpp"
 
@@ -99,7 +99,10 @@ struct oc_op {
   int *d_deg = nullptr, *d_off = nullptr, *d_slots = nullptr, *d_fcm = nullptr,
       *d_fcp = nullptr, *d_fpack = nullptr, *d_fsd = nullptr, *d_bbid = nullptr;
   int *d_sdo[3] = {nullptr, nullptr, nullptr};
+  std::vector<int> cfrec, cfsdo;               // per-cell face records for the kernels
+  int *d_cfrec = nullptr, *d_cfsdo = nullptr;
   double *d_geo = nullptr, *d_fnrm = nullptr, *d_flen = nullptr;
+  float *d_geof = nullptr;
   double *d_sd[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   float *d_sde[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   // degree groups
@@ -124,6 +127,7 @@ struct oc_op {
   void *ts_rz[2] = {nullptr, nullptr}, *ts_rq[2] = {nullptr, nullptr};
   double *ts_z = nullptr, *ts_q = nullptr;  // solution when the caller passes host memory
   double *ts_aux = nullptr;
+  float *ts_unzf = nullptr, *ts_unqf = nullptr;  // FP32 copies of u^n (mixed time step)
   // graph cache of oc_perform_time_step
   cudaGraphExec_t graph = nullptr;
   int graph_scheme = -1;
@@ -313,11 +317,42 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
       if (sl[0] == -1) return bad(OC_ERR_INVALID_ARG, "hanging face without subface 0");
     }
   op->sd_size[3] = sf; op->sd_size[4] = sb;
+  // per-cell face records: (other zeta offset | boundary index, packed description)
+  op->cfrec.assign(16 * (size_t)nc, 0);
+  op->cfsdo.assign(8 * (size_t)nc, 0);
+  for (int c = 0; c < nc; ++c)
+    for (int sl = 0; sl < 8; ++sl) {
+      const int ref = op->slots[8 * (size_t)c + sl];
+      int other = -1, pk = 0, sdo = 0;
+      if (ref >= 0) {
+        const int f = ref >> 1, side = ref & 1;
+        const int fpk = op->fpack[f];
+        const int fm = fpk & 15, fp = (fpk >> 4) & 15, sub1 = (fpk >> 8) & 15,
+                  orient = (fpk >> 12) & 15, nfq = (fpk >> 16) & 15;
+        const int oc = side ? op->fcm[f] : op->fcp[f];
+        other = op->off[oc];
+        pk = (side ? fp : fm) | ((side ? fm : fp) << 2) | (op->deg[oc] << 4) | (sub1 << 7) |
+             (orient << 9) | (side << 10) | (nfq << 11) | (1 << 14);
+        sdo = op->fsd[f];
+      } else if (ref < -1) {
+        const int b = -ref - 2, f = ni + b;
+        other = b;
+        pk = (op->fpack[f] & 15) | (2 << 14) | (op->bbid[b] << 16);
+        sdo = op->fsd[f];
+      }
+      op->cfrec[16 * (size_t)c + 2 * sl] = other;
+      op->cfrec[16 * (size_t)c + 2 * sl + 1] = pk;
+      op->cfsdo[8 * (size_t)c + sl] = sdo;
+    }
   // device
   OC_TRY(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
   OC_TRY(upload(op, &op->d_deg, op->deg.data(), nc));
   OC_TRY(upload(op, &op->d_off, op->off.data(), nc));
   OC_TRY(upload(op, &op->d_geo, op->geo.data(), op->geo.size()));
+  {
+    std::vector<float> gf(op->geo.begin(), op->geo.end());
+    OC_TRY(upload(op, &op->d_geof, gf.data(), gf.size()));
+  }
   OC_TRY(upload(op, &op->d_slots, op->slots.data(), op->slots.size()));
   OC_TRY(upload(op, &op->d_fcm, op->fcm.data(), op->fcm.size()));
   OC_TRY(upload(op, &op->d_fcp, op->fcp.data(), op->fcp.size()));
@@ -327,6 +362,8 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   OC_TRY(upload(op, &op->d_fnrm, op->fnrm.data(), op->fnrm.size()));
   OC_TRY(upload(op, &op->d_flen, op->flen.data(), op->flen.size()));
   for (int k = 0; k < 3; ++k) OC_TRY(upload(op, &op->d_sdo[k], op->sdo[k].data(), nc));
+  OC_TRY(upload(op, &op->d_cfrec, op->cfrec.data(), op->cfrec.size()));
+  OC_TRY(upload(op, &op->d_cfsdo, op->cfsdo.data(), op->cfsdo.size()));
   for (int p = 1; p <= OC_MAXDEG; ++p) {
     std::vector<int> g;
     for (int c = 0; c < nc; ++c)
@@ -475,6 +512,9 @@ static void fill_common(oc_op *op, StageArgs &a) {
   a.sd0e = op->d_sde[0]; a.sd1e = op->d_sde[1]; a.sd2e = op->d_sde[2]; a.sdfe = op->d_sde[3];
   a.sdbe = op->d_sde[4];
   a.sdo0 = op->d_sdo[0]; a.sdo1 = op->d_sdo[1]; a.sdo2 = op->d_sdo[2];
+  a.cfrec = op->d_cfrec;
+  a.geof = op->prm.precision == OC_PREC_MIXED ? op->d_geof : nullptr;
+  a.cfsdo = (op->d_sd[3] || op->d_sd[4]) ? op->d_cfsdo : nullptr;
   const double cu = op->prm.threshold_wetdry;
   a.g = op->prm.g; a.cu4 = cu * cu * cu * cu; a.nu = op->prm.horizontal_viscosity;
   a.zeta_ref = op->prm.precision == OC_PREC_MIXED ? op->prm.zeta_reference : 0.0;
@@ -650,6 +690,10 @@ static oc_status ensure_ts(oc_op *op, const Scheme &sc) {
     if (!op->ts_rq[j]) OC_TRY(alloc(op, &op->ts_rq[j], nq * rs));
   }
   if (sc.ark && !op->ts_aux) OC_TRY(alloc(op, (void **)&op->ts_aux, nq * 8));
+  if (mixed && !op->ts_unzf) {
+    OC_TRY(alloc(op, (void **)&op->ts_unzf, nz * 4));
+    OC_TRY(alloc(op, (void **)&op->ts_unqf, nq * 4));
+  }
   return OC_OK;
 }
 
@@ -669,6 +713,11 @@ static oc_status enqueue_step(oc_op *op, const Scheme &sc, double *z, double *q)
       a.r_is_float = mixed ? 1 : 0;
     }
     a.un_z = z; a.un_q = q;
+    a.fast_mixed = mixed ? 1 : 0;
+    a.un_zf = (mixed && st > 0) ? op->ts_unzf : nullptr;
+    a.un_qf = (mixed && st > 0) ? op->ts_unqf : nullptr;
+    a.out_unzf = (mixed && st == 0) ? op->ts_unzf : nullptr;
+    a.out_unqf = (mixed && st == 0) ? op->ts_unqf : nullptr;
     for (int j = 0; j <= sc.s; ++j) a.kz[j] = op->ts_kz[j];
     for (int j = 0; j < 2 * OC_MAXSTAGES; ++j) a.kq[j] = op->ts_kq[j];
     if (last) {

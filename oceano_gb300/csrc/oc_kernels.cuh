@@ -38,7 +38,20 @@ template <>
 __device__ __forceinline__ const DegTables<float> &tab<float>(int p) { return c_tabf[p - 1]; }
 
 enum { ERR_UNKNOWN_BID = 1 << 2, ERR_NONFINITE = 1 << 3 };
+// boundary kinds (values of OC_BC_* in oceano_gpu.h)
+enum { OC_BC_WALL_ = 1, OC_BC_SUPIN_ = 2, OC_BC_SUPOUT_ = 3, OC_BC_HEIGHT_ = 4,
+       OC_BC_DISCHARGE_ = 5, OC_BC_ABSORB_ = 6 };
 #define OC_FULL 0xffffffffu
+
+// math in the compute type, with the single-precision functions named explicitly
+__device__ __forceinline__ float m_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double m_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float m_abs(float x) { return fabsf(x); }
+__device__ __forceinline__ double m_abs(double x) { return fabs(x); }
+__device__ __forceinline__ float m_exp(float x) { return expf(x); }
+__device__ __forceinline__ double m_exp(double x) { return exp(x); }
+__device__ __forceinline__ float m_log(float x) { return logf(x); }
+__device__ __forceinline__ double m_log(double x) { return log(x); }
 
 template <typename R>
 __device__ __forceinline__ R mx(R a, R b) { return a < b ? b : a; }  // std::max
@@ -54,7 +67,7 @@ template <typename R>
 __device__ __forceinline__ void velocity(R z, R q0, R q1, R zb, R cu4, R &v0, R &v1) {
   const R h = depth<R>(z, zb);
   const R h4 = h * h * h * h;
-  const R inv = sqrt(R(2.)) * h / sqrt(h4 + mx<R>(h4, cu4));
+  const R inv = R(1.4142135623730951) * h / m_sqrt(h4 + mx<R>(h4, cu4));
   v0 = q0 * inv;
   v1 = q1 * inv;
 }
@@ -65,8 +78,8 @@ __device__ __forceinline__ void friction(int model, R g, R v0, R v1, R cf, R h, 
   if (model == 1) {
     s0 = cf * h * v0; s1 = cf * h * v1;
   } else if (model == 2) {
-    const R inv_depth = R(1.) / (exp(log(h) * R(0.33333333333)));
-    const R hcf = g * cf * cf * inv_depth * sqrt(v0 * v0 + v1 * v1);
+    const R inv_depth = R(1.) / (m_exp(m_log(h) * R(0.33333333333)));
+    const R hcf = g * cf * cf * inv_depth * m_sqrt(v0 * v0 + v1 * v1);
     s0 = hcf * v0; s1 = hcf * v1;
   } else {
     s0 = 0; s1 = 0;
@@ -77,8 +90,8 @@ template <typename R>
 __device__ __forceinline__ R friction_jac(int model, R g, R v0, R v1, R cf, R h) {
   if (model == 1) return cf;
   if (model == 2) {
-    const R inv_depth = R(1.) / (exp(log(h) * R(1.33333333333)));
-    return g * cf * cf * inv_depth * sqrt(v0 * v0 + v1 * v1);
+    const R inv_depth = R(1.) / (m_exp(m_log(h) * R(1.33333333333)));
+    return g * cf * cf * inv_depth * m_sqrt(v0 * v0 + v1 * v1);
   }
   return 0;
 }
@@ -93,8 +106,8 @@ __device__ __forceinline__ void face_flux(R g, R cu4, R zm, R qm0, R qm1, R zp, 
   R vm0, vm1, vp0, vp1;
   velocity<R>(zm, qm0, qm1, zbm, cu4, vm0, vm1);
   velocity<R>(zp, qp0, qp1, zbp, cu4, vp0, vp1);
-  const R lm = fabs(vm0 * n0 + vm1 * n1) + sqrt(g * depth<R>(zm, zbm));
-  const R lp = fabs(vp0 * n0 + vp1 * n1) + sqrt(g * depth<R>(zp, zbp));
+  const R lm = m_abs(vm0 * n0 + vm1 * n1) + m_sqrt(g * depth<R>(zm, zbm));
+  const R lp = m_abs(vp0 * n0 + vp1 * n1) + m_sqrt(g * depth<R>(zp, zbp));
   const R lambda = mx<R>(lp, lm);
   const R zbs = mn<R>(zbm, zbp);
   const R hm = depth<R>(zm, zbs), hp = depth<R>(zp, zbs);
@@ -167,6 +180,17 @@ __device__ __forceinline__ R load_r(const void *p, int64_t i, int is_float, doub
   return (R)(static_cast<const double *>(p)[i] - ref);
 }
 
+// stage-input load with the input precision fixed at compile time (a runtime
+// switch would let the compiler evaluate both branches)
+template <typename RIN, typename R>
+__device__ __forceinline__ R load_in(const void *p, int64_t i, double ref) {
+  if constexpr (sizeof(RIN) == 4) {
+    return (R)(static_cast<const float *>(p)[i]);
+  } else {
+    return (R)(static_cast<const double *>(p)[i] - ref);
+  }
+}
+
 // stride of the per-variable face point values (>= OC_MAXF and OC_MAXQ)
 constexpr int FVS = 8;
 
@@ -176,8 +200,11 @@ struct Dims {
   static constexpr int T = Q > G ? Q : G;
   static constexpr int NN = N * N, NT = N * T;
   static constexpr int CPW = 32 / T;
+  // scratch tiles; during the face phase they hold the neighbour traces of the
+  // 8 face slots (3 variables x up to 5 nodes each)
+  static constexpr int XS = 6 * NT > 8 * 3 * OC_MAXN ? 6 * NT : 8 * 3 * OC_MAXN;
   // per-cell shared memory: compute-type region and FP64 region (elements)
-  static constexpr int SZR = 9 * NN + 6 * NT + 3 * FVS;  // U 3, RES 3, RST 2, BZ 1 tiles; X; FV
+  static constexpr int SZR = 10 * NN + XS + 3 * FVS;  // U 3, RES 3, RST 2, BZ 1, ZN 1; X; FV
   static constexpr int SZD = NN + 3 * NT + T + 2;
   // Team strides: padded so that the 32/T teams of a warp start on different
   // shared-memory banks (stride mod 32 chosen per degree and element size to
@@ -189,13 +216,16 @@ struct Dims {
     return (((SZR + 31) / 32) * 32 + (sizeof(R) == 4 ? pad_f : pad_d)) * (int)sizeof(R);
   }
   static constexpr int bytes_d() { return (((SZD + 31) / 32) * 32 + pad_d) * 8; }
-  // per warp: CPW compute regions, CPW FP64 regions, CPW batch-norm slots
+  // per warp: CPW compute regions, CPW FP64 regions, CPW batch-norm slots, int area
   template <typename R>
   static constexpr int d_offset() { return ((CPW * bytes_r<R>() + 15) / 16) * 16; }
   template <typename R>
   static constexpr int norm_offset() { return d_offset<R>() + CPW * bytes_d(); }
   template <typename R>
-  static constexpr int warp_bytes() { return ((norm_offset<R>() + CPW * 8 + 15) / 16) * 16; }
+  static constexpr int int_offset() { return norm_offset<R>() + CPW * 8; }
+  static constexpr int INTS = 2 + 16 + 8 + 1;  // cell, offset, 8 slot records, 8 sdo, flag
+  template <typename R>
+  static constexpr int warp_bytes() { return ((int_offset<R>() + CPW * INTS * 4 + 15) / 16) * 16; }
 };
 
 // Sum over the T threads of a team; called by all lanes (two full syncs).
@@ -364,12 +394,98 @@ __device__ void zeta_iteration_fp64(const StageArgs &a, int cell, double *DZ, do
   }
 }
 
+// Boundary face point (OceanDG.h:1105-1339): ghost state of the boundary kind
+// and the numerical fluxes.  Kept out of line so that none of its FP64 work
+// (boundary data functions at the point coordinates) is hoisted into the
+// face loop of the cells that have no boundary face.
+template <typename R, bool MIX>
+__device__ __noinline__ void boundary_flux(const StageArgs &a, int bid, int bkind, int fo,
+                                           double sx, const double *geo, double zref, int sdk,
+                                           R g, R cu4, R zm, R qm0, R qm1, R n0, R n1, R &F,
+                                           R &Fa0, R &Fa1) {
+  R zbm = MIX ? (R)zref : R(0);
+  if (MIX && a.sdbe) zbm = (R)a.sdbe[sdk];
+  else if (!MIX && a.sdb) zbm = (R)a.sdb[sdk];
+  const double e0 = fo == 0 ? 0. : fo == 1 ? 1. : sx;
+  const double e1 = fo < 2 ? sx : fo == 2 ? 0. : 1.;
+  const double px = geo[0] + geo[2] * e0 + geo[3] * e1;
+  const double py = geo[1] + geo[4] * e0 + geo[5] * e1;
+  const R un = qm0 * n0 + qm1 * n1;
+  R zp = zm, qp0 = qm0, qp1 = qm1;
+  bool at_outflow = false;
+  if (bkind == OC_BC_WALL_) {
+    qp0 = qm0 - R(2.) * un * n0;
+    qp1 = qm1 - R(2.) * un * n1;
+  } else if (bkind == OC_BC_SUPIN_) {
+    const double zd = bc_value(a, bid, px, py, 0);
+    zp = (R)(zd - zref);
+    const R hh = depth<R>(zp, zbm);
+    qp0 = (R)bc_value(a, bid, px, py, 1) * hh;
+    qp1 = (R)bc_value(a, bid, px, py, 2) * hh;
+  } else if (bkind == OC_BC_SUPOUT_) {
+    at_outflow = true;
+  } else if (bkind == OC_BC_HEIGHT_) {
+    zp = (R)(bc_value(a, bid, px, py, 0) - zref);
+  } else if (bkind == OC_BC_DISCHARGE_) {
+    const R qn = (R)bc_value(a, bid, px, py, 1);
+    qp0 = qn * -n0;
+    qp1 = qn * -n1;
+  } else if (bkind == OC_BC_ABSORB_) {
+    const R zf = (R)(bc_value(a, bid, px, py, 0) - zref);
+    const R hf = depth<R>(zf, zbm);
+    const R qf0 = (R)bc_value(a, bid, px, py, 1) * hf;
+    const R qf1 = (R)bc_value(a, bid, px, py, 2) * hf;
+    R v0, v1, u0, u1;
+    velocity<R>(zm, qm0, qm1, zbm, cu4, v0, v1);
+    const R rp = v0 * n0 + v1 * n1 + R(2.) * m_sqrt(g * depth<R>(zm, zbm));
+    velocity<R>(zf, qf0, qf1, zbm, cu4, u0, u1);
+    const R rm = u0 * n0 + u1 * n1 - R(2.) * m_sqrt(g * depth<R>(zf, zbm));
+    const R cb = R(0.25) * (rp - rm), hb = cb * cb / g, ub = R(0.5) * (rp + rm);
+    zp = hb - zbm;
+    const R hd = depth<R>(zp, zbm);
+    qp0 = ub * hd * n0;
+    qp1 = ub * hd * n1;
+  }
+  R Pm0, Pm1, Pp0, Pp1;
+  face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbm, F, Fa0, Fa1, Pm0, Pm1, Pp0,
+               Pp1);
+  Fa0 += Pm0;
+  Fa1 += Pm1;
+  if (at_outflow && un < R(-1e-12)) Fa0 = Fa1 = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Face records of a cell (built on the host, 8 per cell: 2 per face number):
+//   rec[0] inner: zeta offset of the other cell; boundary: boundary face index
+//   rec[1] bits 0-1 own face number, 2-3 other face number, 4-6 other degree,
+//          7-8 subface+1, 9 orientation, 10 side (0 minus, 1 plus),
+//          11-13 face points (inner), 14-15 kind (0 none, 1 inner, 2 boundary),
+//          16-19 boundary id
+// ---------------------------------------------------------------------------
+struct FaceRec {
+  int other, pk;
+  __device__ __forceinline__ int own_face() const { return pk & 3; }
+  __device__ __forceinline__ int nb_face() const { return (pk >> 2) & 3; }
+  __device__ __forceinline__ int nb_deg() const { return (pk >> 4) & 7; }
+  __device__ __forceinline__ int sub() const { return ((pk >> 7) & 3) - 1; }
+  __device__ __forceinline__ int orient() const { return (pk >> 9) & 1; }
+  __device__ __forceinline__ int side() const { return (pk >> 10) & 1; }
+  __device__ __forceinline__ int nf() const { return (pk >> 11) & 7; }
+  __device__ __forceinline__ int kind() const { return (pk >> 14) & 3; }
+  __device__ __forceinline__ int bid() const { return (pk >> 16) & 15; }
+};
+
 // ---------------------------------------------------------------------------
 // The fused stage kernel.
 //   MIX = false: FP64 plain form (R = KT = double).
 //   MIX = true : mixed form; R = float bulk, KT = type of the k registers.
+// Memory flow: warp-cooperative prologue (stage input, face records, partial
+// zeta right-hand side), neighbour traces of all face slots prefetched into
+// shared memory, team-local compute, warp-cooperative epilogue (RK update and
+// stores).  Global accesses of the prologue/epilogue are lane-contiguous over
+// the warp's cells.
 // ---------------------------------------------------------------------------
-template <int P, typename R, typename KT, bool MIX>
+template <int P, typename R, typename KT, bool MIX, typename RIN>
 __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
   using D = Dims<P>;
   constexpr int N = D::N, Q = D::Q, G = D::G, T = D::T, NN = D::NN, NT = D::NT;
@@ -379,53 +495,100 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int team_raw = lane / T, t = lane - team_raw * T;
-  const bool member = team_raw < CPWMAX;  // lanes past the last team only synchronise
+  const bool member = team_raw < CPWMAX;  // lanes past the last team only help and synchronise
   const int team = member ? team_raw : 0;
   const int W = a.batch;
   const int cpw = (CPWMAX / W) * W;
   const int wpb = blockDim.x >> 5;
-  const int gi = (blockIdx.x * wpb + warp) * cpw + team;
-  const bool valid = member && team < cpw && gi < a.n_group;
-  const int cell = a.group_cells ? a.group_cells[valid ? gi : 0] : a.group_first + (valid ? gi : 0);
+  const int gi0 = (blockIdx.x * wpb + warp) * cpw;
+  const int nvalid = max(0, min(cpw, a.n_group - gi0));  // cells of this warp
+  const bool valid = member && team < nvalid;
+  const int s = a.stage;
+  const StageDyn dy = *a.dyn;
+  R fR[OC_MAXSTAGES];  // coefficients in the compute type, converted once
+#pragma unroll
+  for (int j = 0; j < OC_MAXSTAGES; ++j) fR[j] = (R)dy.f[j];
+  // the mixed time-step path (FP32 registers) forms internal stage inputs in FP32
+  constexpr bool fast = MIX && sizeof(KT) == 4;
+  const double zref = MIX ? a.zeta_ref : 0.0;
+  const R g = (R)a.g, cu4 = (R)a.cu4;
+  const R zbe_flat = (R)zref;  // zb + zeta_ref where no bathymetry is given
 
   unsigned char *wbase = smem_raw + warp * D::template warp_bytes<R>();
-  R *sm = reinterpret_cast<R *>(wbase + team * D::template bytes_r<R>());
-  double *dm = reinterpret_cast<double *>(wbase + D::template d_offset<R>() +
-                                          team * D::bytes_d());
+  auto Rreg = [&](int j) { return reinterpret_cast<R *>(wbase + j * D::template bytes_r<R>()); };
+  int *ints = reinterpret_cast<int *>(wbase + D::template int_offset<R>());
+  int *w_cell = ints, *w_off = ints + CPWMAX, *w_rec = ints + 2 * CPWMAX,
+      *w_sdo = ints + 18 * CPWMAX, *w_flag = ints + 26 * CPWMAX;
   double *warp_norm = reinterpret_cast<double *>(wbase + D::template norm_offset<R>());
-  R *U = sm;                  // 3*NN stage input z, q0, q1
-  R *RES = U + 3 * NN;        // 3*NN residual
+  R *U = Rreg(team);          // 3*NN stage input z, q0, q1
+  R *RES = U + 3 * NN;        // 3*NN residual; later the discharge result
   R *RST = RES + 3 * NN;      // 2*NN stiff residual (ARK)
-  R *BZ = RST + 2 * NN;       // NN zeta right-hand side b = sum f k
-  R *X = BZ + NN;             // 6 tiles of N*T
-  R *FV = X + 6 * NT;         // 3*FVS face point values
+  R *BZ = RST + 2 * NN;       // NN zeta right-hand side b = sum f k (mixed: then delta)
+  R *ZN = BZ + NN;            // NN mixed form: zeta^n - zeta_ref
+  R *X = ZN + NN;             // scratch tiles / neighbour traces
+  R *FV = X + D::XS;          // 3*FVS face point values
+  double *dm = reinterpret_cast<double *>(wbase + D::template d_offset<R>() + team * D::bytes_d());
   double *DZ = dm;            // NN FP64 iterate
   double *DX = DZ + NN;       // 3 tiles N*T
   double *DRED = DX + 3 * NT; // T+1
 
-  const double *geo = a.geo + 11 * (int64_t)cell;
-  const R Ji00 = (R)geo[6], Ji01 = (R)geo[7], Ji10 = (R)geo[8], Ji11 = (R)geo[9];
-  const R det = (R)geo[10];
-  const int64_t zo = a.off[cell], qo = 2 * zo;
-  const double zref = MIX ? a.zeta_ref : 0.0;
-  const R g = (R)a.g, cu4 = (R)a.cu4;
-  const R zbe_flat = (R)zref;  // zb + zeta_ref where no bathymetry is given
-  const int s = a.stage;
-  const StageDyn dy = *a.dyn;
-
-  // ---- 1. stage input DoFs ---------------------------------------------------
-  if (member && t < N) {
-#pragma unroll
-    for (int ix = 0; ix < N; ++ix) {
-      const int d = t * N + ix;
-      U[d] = load_r<R>(a.rz, zo + d, a.r_is_float, zref);
-      U[NN + d] = load_r<R>(a.rq, qo + d, a.r_is_float, 0.0);
-      U[2 * NN + d] = load_r<R>(a.rq, qo + NN + d, a.r_is_float, 0.0);
+  // ---- 0. prologue: cells, stage input, face records, partial rhs ------------
+  if (lane < CPWMAX) {
+    const int j = lane;
+    const int gi = nvalid > 0 ? gi0 + (j < nvalid ? j : 0) : 0;  // idle warps read cell 0
+    const int c = a.group_cells ? a.group_cells[gi] : a.group_first + gi;
+    w_cell[j] = c;
+    w_off[j] = a.off[c];
+    w_flag[j] = 0;
+  }
+  __syncwarp();
+  const int cell = w_cell[team];
+  const int64_t zo = w_off[team], qo = 2 * zo;
+  for (int e = lane; e < nvalid * 16; e += 32) {  // face records (invalid teams: empty)
+    const int j = e >> 4, k = e & 15;
+    w_rec[j * 16 + k] = a.cfrec[16 * (int64_t)w_cell[j] + k];
+  }
+  for (int e = lane; e < (CPWMAX - nvalid) * 16; e += 32) {
+    const int j = nvalid + (e >> 4);
+    w_rec[j * 16 + (e & 15)] = (e & 1) ? 0 : -1;
+  }
+  if (a.cfsdo)
+    for (int e = lane; e < nvalid * 8; e += 32)
+      w_sdo[e] = a.cfsdo[8 * (int64_t)w_cell[e >> 3] + (e & 7)];
+#pragma unroll 4
+  for (int e = lane; e < nvalid * NN; e += 32) {
+    const int j = e / NN, d = e - j * NN;
+    const int64_t oz = w_off[j] + d, oq = 2 * (int64_t)w_off[j] + d;
+    R *Uj = Rreg(j);
+    Uj[d] = load_in<RIN, R>(a.rz, oz, zref);
+    Uj[NN + d] = load_in<RIN, R>(a.rq, oq, 0.0);
+    Uj[2 * NN + d] = load_in<RIN, R>(a.rq, oq + NN, 0.0);
+    if (!a.apply_mode) {
+      R bprev = 0;  // sum_{j<s} f_j kz_j in the reference's order
+      for (int jj = 0; jj < s; ++jj)
+        bprev = jj == 0 ? fR[0] * (R) static_cast<const KT *>(a.kz[1])[oz]
+                        : bprev + fR[jj] * (R) static_cast<const KT *>(a.kz[jj + 1])[oz];
+      Uj[8 * NN + d] = bprev;
+      if constexpr (fast) {
+        Uj[9 * NN + d] = s == 0 ? Uj[d] : (R)a.un_zf[oz];
+      } else if constexpr (MIX) {
+        Uj[9 * NN + d] = (R)(a.un_z[oz] - zref);
+      }
     }
   }
   __syncwarp();
 
-  // ---- 2. cell integrals: local_apply_cell_height (OceanDG.h:669-693),
+  const double *geo = a.geo + 11 * (int64_t)cell;
+  R gR[11];  // geometry in the compute type (FP32 copy in the mixed form)
+#pragma unroll
+  for (int k = 0; k < 11; ++k) {
+    if constexpr (MIX) gR[k] = (R)a.geof[11 * (int64_t)cell + k];
+    else gR[k] = (R)geo[k];
+  }
+  const R Ji00 = gR[6], Ji01 = gR[7], Ji10 = gR[8], Ji11 = gR[9];
+  const R det = gR[10];
+
+  // ---- 1. cell integrals: local_apply_cell_height (OceanDG.h:669-693),
   //         local_apply_cell_discharge / _nonstiff / _stiff (:695-826) ---------
   if (member && t < N) {  // x-pass on rows iy = t
     R z[N], q0[N], q1[N];
@@ -490,9 +653,9 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
         const R h = depth<R>(z, zb);
         const R dz0 = Ji00 * zx + Ji10 * zy, dz1 = Ji01 * zx + Ji11 * zy;
         R fr0 = 0, fr1 = 0;
-        if (a.friction) friction<R>(a.friction, g, v0, v1, cf, h, fr0, fr1);
-        const R s0 = -g * h * dz0 - (split ? R(0) : fr0) + w0 + fc * q1;
-        const R s1 = -g * h * dz1 - (split ? R(0) : fr1) + w1 - fc * q0;
+        if (a.friction && !split) friction<R>(a.friction, g, v0, v1, cf, h, fr0, fr1);
+        const R s0 = -g * h * dz0 - fr0 + w0 + fc * q1;
+        const R s1 = -g * h * dz1 - fr1 + w1 - fc * q0;
         const R F00 = q0 * v0, F01 = q0 * v1, F10 = q1 * v0, F11 = q1 * v1;
         const R g00 = (Ji00 * F00 + Ji01 * F01) * w, g01 = (Ji10 * F00 + Ji11 * F01) * w;
         const R g10 = (Ji00 * F10 + Ji01 * F11) * w, g11 = (Ji10 * F10 + Ji11 * F11) * w;
@@ -539,230 +702,203 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
       }
     }
     __syncwarp();
-    if (split) {  // warp-uniform: stiff (friction) residual, a second pass over the points
-      if (member && t < N) {  // x-pass of the stage input again (X was overwritten)
-        R z[N], q0[N], q1[N];
+  }
+  if (split) {  // warp-uniform: stiff (friction) residual, a second pass over the points
+    if (member && t < N) {
+      R z[N], q0[N], q1[N];
+#pragma unroll
+      for (int ix = 0; ix < N; ++ix) {
+        z[ix] = U[t * N + ix];
+        q0[ix] = U[NN + t * N + ix];
+        q1[ix] = U[2 * NN + t * N + ix];
+      }
+#pragma unroll
+      for (int qx = 0; qx < Q; ++qx) {
+        R b0 = 0, a0 = 0, a1 = 0;
 #pragma unroll
         for (int ix = 0; ix < N; ++ix) {
-          z[ix] = U[t * N + ix];
-          q0[ix] = U[NN + t * N + ix];
-          q1[ix] = U[2 * NN + t * N + ix];
+          b0 += tb.BQ[qx][ix] * z[ix];
+          a0 += tb.BQ[qx][ix] * q0[ix];
+          a1 += tb.BQ[qx][ix] * q1[ix];
         }
-#pragma unroll
-        for (int qx = 0; qx < Q; ++qx) {
-          R b0 = 0, a0 = 0, a1 = 0;
-#pragma unroll
-          for (int ix = 0; ix < N; ++ix) {
-            b0 += tb.BQ[qx][ix] * z[ix];
-            a0 += tb.BQ[qx][ix] * q0[ix];
-            a1 += tb.BQ[qx][ix] * q1[ix];
-          }
-          X[2 * NT + t * T + qx] = b0;
-          X[3 * NT + t * T + qx] = a0;
-          X[4 * NT + t * T + qx] = a1;
-        }
+        X[2 * NT + t * T + qx] = b0;
+        X[3 * NT + t * T + qx] = a0;
+        X[4 * NT + t * T + qx] = a1;
       }
-      __syncwarp();
-      R S0[N], S1[N];
+    }
+    __syncwarp();
+    R S0[N], S1[N];
 #pragma unroll
-      for (int i = 0; i < N; ++i) S0[i] = S1[i] = 0;
-      if (member && t < Q) {
-        const double *sd0 = a.sd0 ? a.sd0 + a.sdo0[cell] : nullptr;
-        const float *sd0e = a.sd0e ? a.sd0e + a.sdo0[cell] : nullptr;
+    for (int i = 0; i < N; ++i) S0[i] = S1[i] = 0;
+    if (member && t < Q) {
+      const double *sd0 = a.sd0 ? a.sd0 + a.sdo0[cell] : nullptr;
+      const float *sd0e = a.sd0e ? a.sd0e + a.sdo0[cell] : nullptr;
 #pragma unroll
-        for (int qy = 0; qy < Q; ++qy) {
-          R z = 0, q0 = 0, q1 = 0;
-#pragma unroll
-          for (int iy = 0; iy < N; ++iy) {
-            z += tb.BQ[qy][iy] * X[2 * NT + iy * T + t];
-            q0 += tb.BQ[qy][iy] * X[3 * NT + iy * T + t];
-            q1 += tb.BQ[qy][iy] * X[4 * NT + iy * T + t];
-          }
-          const int k = qy * Q + t;
-          R zb = MIX ? zbe_flat : R(0), cf = 0;
-          if (MIX && sd0e) { zb = (R)sd0e[5 * k]; cf = (R)sd0e[5 * k + 1]; }
-          else if (!MIX && sd0) { zb = (R)sd0[5 * k]; cf = (R)sd0[5 * k + 1]; }
-          R v0, v1, fr0 = 0, fr1 = 0;
-          velocity<R>(z, q0, q1, zb, cu4, v0, v1);
-          if (a.friction) friction<R>(a.friction, g, v0, v1, cf, depth<R>(z, zb), fr0, fr1);
-          const R w = tb.wQ[t] * tb.wQ[qy] * det;
-          const R st0 = -fr0 * w, st1 = -fr1 * w;
-#pragma unroll
-          for (int iy = 0; iy < N; ++iy) {
-            S0[iy] += tb.BQ[qy][iy] * st0;
-            S1[iy] += tb.BQ[qy][iy] * st1;
-          }
-        }
-      }
-      __syncwarp();
-      if (member && t < Q) {
+      for (int qy = 0; qy < Q; ++qy) {
+        R z = 0, q0 = 0, q1 = 0;
 #pragma unroll
         for (int iy = 0; iy < N; ++iy) {
-          X[0 * NT + iy * T + t] = S0[iy];
-          X[1 * NT + iy * T + t] = S1[iy];
+          z += tb.BQ[qy][iy] * X[2 * NT + iy * T + t];
+          q0 += tb.BQ[qy][iy] * X[3 * NT + iy * T + t];
+          q1 += tb.BQ[qy][iy] * X[4 * NT + iy * T + t];
+        }
+        const int k = qy * Q + t;
+        R zb = MIX ? zbe_flat : R(0), cf = 0;
+        if (MIX && sd0e) { zb = (R)sd0e[5 * k]; cf = (R)sd0e[5 * k + 1]; }
+        else if (!MIX && sd0) { zb = (R)sd0[5 * k]; cf = (R)sd0[5 * k + 1]; }
+        R v0, v1, fr0 = 0, fr1 = 0;
+        velocity<R>(z, q0, q1, zb, cu4, v0, v1);
+        if (a.friction) friction<R>(a.friction, g, v0, v1, cf, depth<R>(z, zb), fr0, fr1);
+        const R w = tb.wQ[t] * tb.wQ[qy] * det;
+        const R st0 = -fr0 * w, st1 = -fr1 * w;
+#pragma unroll
+        for (int iy = 0; iy < N; ++iy) {
+          S0[iy] += tb.BQ[qy][iy] * st0;
+          S1[iy] += tb.BQ[qy][iy] * st1;
         }
       }
-      __syncwarp();
-      if (member && t < N) {
-#pragma unroll
-        for (int ix = 0; ix < N; ++ix) {
-          R r0 = 0, r1 = 0;
-#pragma unroll
-          for (int qx = 0; qx < Q; ++qx) {
-            r0 += tb.BQ[qx][ix] * X[0 * NT + t * T + qx];
-            r1 += tb.BQ[qx][ix] * X[1 * NT + t * T + qx];
-          }
-          RST[t * N + ix] = r0;
-          RST[NN + t * N + ix] = r1;
-        }
-      }
-      __syncwarp();
     }
+    __syncwarp();
+    if (member && t < Q) {
+#pragma unroll
+      for (int iy = 0; iy < N; ++iy) {
+        X[0 * NT + iy * T + t] = S0[iy];
+        X[1 * NT + iy * T + t] = S1[iy];
+      }
+    }
+    __syncwarp();
+    if (member && t < N) {
+#pragma unroll
+      for (int ix = 0; ix < N; ++ix) {
+        R r0 = 0, r1 = 0;
+#pragma unroll
+        for (int qx = 0; qx < Q; ++qx) {
+          r0 += tb.BQ[qx][ix] * X[0 * NT + t * T + qx];
+          r1 += tb.BQ[qx][ix] * X[1 * NT + t * T + qx];
+        }
+        RST[t * N + ix] = r0;
+        RST[NN + t * N + ix] = r1;
+      }
+    }
+    __syncwarp();
   }
 
-  // ---- 3. faces: local_apply_face_* (OceanDG.h:936-1050) and
+  // ---- 2. faces: local_apply_face_* (OceanDG.h:936-1050) and
   //         local_apply_boundary_face_* (:1105-1339) ----------------------------
-  const int *slots = a.slots + 8 * (int64_t)cell;
+  const FaceRec *recs = reinterpret_cast<const FaceRec *>(w_rec + 16 * team);
+  // 2a. neighbour traces of every inner slot into X: [slot][var][node]
+  R *NB = X;
+  if (member) {
+    for (int e = t; e < 8 * OC_MAXN; e += T) {
+      const int sl = e / OC_MAXN, i = e - sl * OC_MAXN;
+      const FaceRec r = recs[sl];
+      const int Nn = r.nb_deg() + 1;
+      if (r.kind() == 1 && i < Nn) {
+        const int d = face_dof(Nn, r.nb_face(), i);
+        const int64_t oz = r.other, oq = 2 * (int64_t)r.other;
+        NB[(sl * 3 + 0) * OC_MAXN + i] = load_in<RIN, R>(a.rz, oz + d, zref);
+        NB[(sl * 3 + 1) * OC_MAXN + i] = load_in<RIN, R>(a.rq, oq + d, 0.0);
+        NB[(sl * 3 + 2) * OC_MAXN + i] = load_in<RIN, R>(a.rq, oq + Nn * Nn + d, 0.0);
+      }
+    }
+  }
+  __syncwarp();
+  // own outward normals and face lengths of the affine cell
+  const R J00 = gR[2], J01 = gR[3], J10 = gR[4], J11 = gR[5];
 #pragma unroll 1
   for (int sl = 0; sl < 8; ++sl) {
-    const int ref = member ? slots[sl] : -1;
-    int nfo = 0, fo = 0, tsel = 0;  // own point count, own face number, own table
-    if (ref >= 0) {
-      const int f = ref >> 1, side = ref & 1;
-      const int pk = a.fpack[f];
-      const int fm = pk & 15, fp = (pk >> 4) & 15, sub = ((pk >> 8) & 15) - 1,
-                orient = (pk >> 12) & 15, nf = (pk >> 16) & 15;
-      const int cm = a.fcm[f], cp = a.fcp[f];
-      const int pm = a.deg[cm], pp = a.deg[cp];
-      const int Nm = pm + 1, Np = pp + 1;
-      const DegTables<R> &tm = tab<R>(pm);
-      const DegTables<R> &tp = tab<R>(pp);
-      const int64_t zom = a.off[cm], zop = a.off[cp];
-      const int64_t nm = (int64_t)Nm * Nm, np = (int64_t)Np * Np;
-      const R n0 = (R)a.fnrm[2 * f], n1 = (R)a.fnrm[2 * f + 1];
-      const R len = (R)a.flen[f];
-      const int sdo = a.fsd[f];
-      nfo = nf;
-      fo = side ? fp : fm;
-      tsel = side ? sub + 1 : 0;
-      for (int k = t; k < nf; k += T) {
-        const int kp = orient ? nf - 1 - k : k;
-        R zm = 0, qm0 = 0, qm1 = 0, zp = 0, qp0 = 0, qp1 = 0;
-        for (int i = 0; i < Nm; ++i) {
-          const int d = face_dof(Nm, fm, i);
-          const R l = tm.F[0][nf][k][i];
-          zm += l * load_r<R>(a.rz, zom + d, a.r_is_float, zref);
-          qm0 += l * load_r<R>(a.rq, 2 * zom + d, a.r_is_float, 0.0);
-          qm1 += l * load_r<R>(a.rq, 2 * zom + nm + d, a.r_is_float, 0.0);
-        }
-        for (int i = 0; i < Np; ++i) {
-          const int d = face_dof(Np, fp, i);
-          const R l = tp.F[sub + 1][nf][kp][i];
-          zp += l * load_r<R>(a.rz, zop + d, a.r_is_float, zref);
-          qp0 += l * load_r<R>(a.rq, 2 * zop + d, a.r_is_float, 0.0);
-          qp1 += l * load_r<R>(a.rq, 2 * zop + np + d, a.r_is_float, 0.0);
-        }
-        R zbm = MIX ? zbe_flat : R(0), zbp = zbm;
-        if (MIX && a.sdfe) {
-          zbm = (R)a.sdfe[sdo + 2 * k]; zbp = (R)a.sdfe[sdo + 2 * k + 1];
-        } else if (!MIX && a.sdf) {
-          zbm = (R)a.sdf[sdo + 2 * k]; zbp = (R)a.sdf[sdo + 2 * k + 1];
-        }
-        R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
-        face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1, Pm0,
-                     Pm1, Pp0, Pp1);
-        const R jxw = tb.wF[nf][k] * len;
-        const int ko = side ? kp : k;
-        if (side == 0) {
-          FV[ko] = -F * jxw;
-          FV[FVS + ko] = (-Fa0 - Pm0) * jxw;
-          FV[2 * FVS + ko] = (-Fa1 - Pm1) * jxw;
-        } else {
-          FV[ko] = F * jxw;
-          FV[FVS + ko] = (Fa0 + Pp0) * jxw;
-          FV[2 * FVS + ko] = (Fa1 + Pp1) * jxw;
-        }
-      }
-    } else if (ref < -1) {  // boundary face
-      const int b = -ref - 2;
-      const int f = a.n_inner + b;
-      const int fm = a.fpack[f] & 15;
-      const R n0 = (R)a.fnrm[2 * f], n1 = (R)a.fnrm[2 * f + 1];
-      const R len = (R)a.flen[f];
-      const int bid = a.bbid[b];
-      const int kind = (bid >= 0 && bid < OC_MAXBID) ? a.bc_kind[bid] : 0;
-      if (kind == 0 && t == 0) atomicOr(a.err, ERR_UNKNOWN_BID);
-      const int sdo = a.fsd[f];
-      nfo = Q;
-      fo = fm;
-      tsel = -1;
-      if (t < Q) {
-        const int k = t;
-        R zm = 0, qm0 = 0, qm1 = 0;
+    const FaceRec r = recs[sl];
+    const int kind = member ? r.kind() : 0;
+    const int fo = r.own_face();
+    int nfo = 0, tsel = 0;
+    if (kind != 0) {
+      // outward normal of the own face: J^-T n_ref / |.|; tangent length |J t_ref|
+      const R nr0 = fo == 0 ? R(-1) : fo == 1 ? R(1) : R(0);
+      const R nr1 = fo == 2 ? R(-1) : fo == 3 ? R(1) : R(0);
+      R on0 = Ji00 * nr0 + Ji10 * nr1, on1 = Ji01 * nr0 + Ji11 * nr1;
+      const R inv = R(1) / m_sqrt(on0 * on0 + on1 * on1);
+      on0 *= inv; on1 *= inv;
+      const R tx = fo < 2 ? J01 : J00, ty = fo < 2 ? J11 : J10;
+      R len = m_sqrt(tx * tx + ty * ty);
+      if (kind == 1) {
+        const int side = r.side(), sub = r.sub(), orient = r.orient(), nf = r.nf();
+        const int pn = r.nb_deg(), Nn = pn + 1;
+        const DegTables<R> &tn = tab<R>(pn);
+        if (side == 1 && sub >= 0) len *= R(0.5);  // coarse side: the fine half-face
+        const R n0 = side ? -on0 : on0, n1 = side ? -on1 : on1;  // minus normal
+        const int sdo = a.cfsdo ? w_sdo[8 * team + sl] : 0;
+        nfo = nf;
+        tsel = side ? sub + 1 : 0;
+        for (int k = t; k < nf; k += T) {
+          const int kp = orient ? nf - 1 - k : k;  // point index on the plus side
+          const int ko = side ? kp : k, kn = side ? k : kp;
+          R zo_ = 0, qo0 = 0, qo1 = 0, zn = 0, qn0 = 0, qn1 = 0;
 #pragma unroll
-        for (int i = 0; i < N; ++i) {
-          const int d = face_dof(N, fm, i);
-          const R l = tb.BQ[k][i];
-          zm += l * U[d];
-          qm0 += l * U[NN + d];
-          qm1 += l * U[2 * NN + d];
+          for (int i = 0; i < N; ++i) {  // own trace
+            const int d = face_dof(N, fo, i);
+            const R l = tb.F[tsel][nf][ko][i];
+            zo_ += l * U[d];
+            qo0 += l * U[NN + d];
+            qo1 += l * U[2 * NN + d];
+          }
+          const int nsel = side ? 0 : sub + 1;
+          for (int i = 0; i < Nn; ++i) {  // neighbour trace
+            const R l = tn.F[nsel][nf][kn][i];
+            zn += l * NB[(sl * 3 + 0) * OC_MAXN + i];
+            qn0 += l * NB[(sl * 3 + 1) * OC_MAXN + i];
+            qn1 += l * NB[(sl * 3 + 2) * OC_MAXN + i];
+          }
+          const R zm = side ? zn : zo_, qm0 = side ? qn0 : qo0, qm1 = side ? qn1 : qo1;
+          const R zp = side ? zo_ : zn, qp0 = side ? qo0 : qn0, qp1 = side ? qo1 : qn1;
+          R zbm = MIX ? zbe_flat : R(0), zbp = zbm;
+          if (MIX && a.sdfe) {
+            zbm = (R)a.sdfe[sdo + 2 * k]; zbp = (R)a.sdfe[sdo + 2 * k + 1];
+          } else if (!MIX && a.sdf) {
+            zbm = (R)a.sdf[sdo + 2 * k]; zbp = (R)a.sdf[sdo + 2 * k + 1];
+          }
+          R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
+          face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1, Pm0,
+                       Pm1, Pp0, Pp1);
+          const R jxw = tb.wF[nf][k] * len;
+          if (side == 0) {
+            FV[ko] = -F * jxw;
+            FV[FVS + ko] = (-Fa0 - Pm0) * jxw;
+            FV[2 * FVS + ko] = (-Fa1 - Pm1) * jxw;
+          } else {
+            FV[ko] = F * jxw;
+            FV[FVS + ko] = (Fa0 + Pp0) * jxw;
+            FV[2 * FVS + ko] = (Fa1 + Pp1) * jxw;
+          }
         }
-        R zbm = MIX ? zbe_flat : R(0);
-        double zb_abs = 0.;
-        if (a.sdb) zb_abs = a.sdb[sdo + k];
-        if (MIX && a.sdbe) zbm = (R)a.sdbe[sdo + k];
-        else if (!MIX && a.sdb) zbm = (R)zb_abs;
-        const double sx = tab<double>(P).xQ[k];
-        const double e0 = fm == 0 ? 0. : fm == 1 ? 1. : sx;
-        const double e1 = fm < 2 ? sx : fm == 2 ? 0. : 1.;
-        const double px = geo[0] + geo[2] * e0 + geo[3] * e1;
-        const double py = geo[1] + geo[4] * e0 + geo[5] * e1;
-        const R un = qm0 * n0 + qm1 * n1;
-        R zp = zm, qp0 = qm0, qp1 = qm1;
-        bool at_outflow = false;
-        if (kind == 1) {  // wall
-          qp0 = qm0 - R(2.) * un * n0;
-          qp1 = qm1 - R(2.) * un * n1;
-        } else if (kind == 2) {  // supercritical inflow
-          const double zd = bc_value(a, bid, px, py, 0);
-          zp = (R)(zd - zref);
-          const R hh = depth<R>(zp, zbm);
-          qp0 = (R)bc_value(a, bid, px, py, 1) * hh;
-          qp1 = (R)bc_value(a, bid, px, py, 2) * hh;
-        } else if (kind == 3) {  // supercritical outflow
-          at_outflow = true;
-        } else if (kind == 4) {  // height inflow
-          zp = (R)(bc_value(a, bid, px, py, 0) - zref);
-        } else if (kind == 5) {  // discharge inflow
-          const R qn = (R)bc_value(a, bid, px, py, 1);
-          qp0 = qn * -n0;
-          qp1 = qn * -n1;
-        } else if (kind == 6) {  // absorbing outflow (Riemann invariants)
-          const R zf = (R)(bc_value(a, bid, px, py, 0) - zref);
-          const R hf = depth<R>(zf, zbm);
-          const R qf0 = (R)bc_value(a, bid, px, py, 1) * hf;
-          const R qf1 = (R)bc_value(a, bid, px, py, 2) * hf;
-          R v0, v1, u0, u1;
-          velocity<R>(zm, qm0, qm1, zbm, cu4, v0, v1);
-          const R rp = v0 * n0 + v1 * n1 + R(2.) * sqrt(g * depth<R>(zm, zbm));
-          velocity<R>(zf, qf0, qf1, zbm, cu4, u0, u1);
-          const R rm = u0 * n0 + u1 * n1 - R(2.) * sqrt(g * depth<R>(zf, zbm));
-          const R cb = R(0.25) * (rp - rm), hb = cb * cb / g, ub = R(0.5) * (rp + rm);
-          zp = hb - zbm;
-          const R hd = depth<R>(zp, zbm);
-          qp0 = ub * hd * n0;
-          qp1 = ub * hd * n1;
+      } else {  // boundary face
+        const int b = r.other;
+        const int bid = r.bid();
+        const int bkind = a.bc_kind[bid];
+        if (bkind == 0 && t == 0) atomicOr(a.err, ERR_UNKNOWN_BID);
+        const int sdo = a.cfsdo ? w_sdo[8 * team + sl] : 0;
+        const R n0 = on0, n1 = on1;
+        nfo = Q;
+        tsel = -1;
+        (void)b;
+        if (t < Q) {
+          const int k = t;
+          R zm = 0, qm0 = 0, qm1 = 0;
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            const int d = face_dof(N, fo, i);
+            const R l = tb.BQ[k][i];
+            zm += l * U[d];
+            qm0 += l * U[NN + d];
+            qm1 += l * U[2 * NN + d];
+          }
+          R F, Fa0, Fa1;
+          boundary_flux<R, MIX>(a, bid, bkind, fo, tab<double>(P).xQ[k], geo, zref, sdo + k, g, cu4,
+                                zm, qm0, qm1, n0, n1, F, Fa0, Fa1);
+          const R jxw = tb.wQ[k] * len;
+          FV[k] = -F * jxw;
+          FV[FVS + k] = -Fa0 * jxw;
+          FV[2 * FVS + k] = -Fa1 * jxw;
         }
-        R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
-        face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbm, F, Fa0, Fa1, Pm0,
-                     Pm1, Pp0, Pp1);
-        Fa0 += Pm0;
-        Fa1 += Pm1;
-        if (at_outflow && un < R(-1e-12)) Fa0 = Fa1 = 0;
-        const R jxw = tb.wQ[k] * len;
-        FV[k] = -F * jxw;
-        FV[FVS + k] = -Fa0 * jxw;
-        FV[2 * FVS + k] = -Fa1 * jxw;
       }
     }
     __syncwarp();
@@ -832,56 +968,43 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
     return;
   }
 
-  // ---- 4. zeta: pre-lambda + local_apply_cell_mass_height (OceanDG.h:1830-1849)
+  // ---- 3. zeta: pre-lambda + local_apply_cell_mass_height (OceanDG.h:1830-1849)
   //         and local_apply_inverse_mass_matrix_height (:1373-1507) ------------
-  KT *kz_out = static_cast<KT *>(a.kz[s + 1]);
-  if (valid && t < N) {
+  // b = sum_{j<s} f_j kz_j (prologue) + f_s L_h zeta, in the reference's order
+  if (member && t < N) {
 #pragma unroll
     for (int ix = 0; ix < N; ++ix) {
       const int d = t * N + ix;
-      const R res = RES[d];
-      kz_out[zo + d] = (KT)res;
-      R bsum = (R)dy.f[0] * (s == 0 ? res : (R) static_cast<const KT *>(a.kz[1])[zo + d]);
-      for (int j = 1; j < s + 1; ++j)
-        bsum += (R)dy.f[j] * (j == s ? res : (R) static_cast<const KT *>(a.kz[j + 1])[zo + d]);
-      BZ[d] = bsum;
+      BZ[d] = s == 0 ? fR[0] * RES[d] : BZ[d] + fR[s] * RES[d];
     }
   }
   __syncwarp();
-  double znext[N];  // FP64 result rows of thread t < N
   bool need_fp64 = !MIX;
   if (MIX) {
+    const R wet_thr = (R)a.wet_threshold;
     // wet check of u^n at the Gauss-Lobatto points (FP32 estimate)
     bool wet = true;
-    if (member && t < N) {
-#pragma unroll
-      for (int ix = 0; ix < N; ++ix) X[t * N + ix] = (R)(a.un_z[zo + t * N + ix] - zref);
-    }
-    __syncwarp();
     if (member && t < N) {
 #pragma unroll
       for (int gx = 0; gx < G; ++gx) {
         R v = 0;
 #pragma unroll
-        for (int ix = 0; ix < N; ++ix) v += tb.BG[gx][ix] * X[t * N + ix];
+        for (int ix = 0; ix < N; ++ix) v += tb.BG[gx][ix] * ZN[t * N + ix];
         X[NT + t * T + gx] = v;
       }
     }
     __syncwarp();
+    const float *zb1e = a.sd1e ? a.sd1e + a.sdo1[cell] : nullptr;
     if (member && t < G) {
-      const float *zb1e = a.sd1e ? a.sd1e + a.sdo1[cell] : nullptr;
 #pragma unroll
       for (int gy = 0; gy < G; ++gy) {
         R v = 0;
 #pragma unroll
         for (int iy = 0; iy < N; ++iy) v += tb.BG[gy][iy] * X[NT + iy * T + t];
         const R zb = zb1e ? (R)zb1e[gy * G + t] : zbe_flat;
-        wet = wet && (v + zb > (R)a.wet_threshold);
+        wet = wet && (v + zb > wet_thr);
       }
     }
-    // team AND through the FP64 reduction slots
-    const double dryc = team_sum<T>(DRED, t, member, wet ? 0. : 1.);
-    const bool team_wet = dryc == 0.;
     // closed form of max_iter sweeps on fully wet cells: delta = A_K b
     if (member && t < N) {
 #pragma unroll
@@ -907,47 +1030,45 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
         R v = 0;
 #pragma unroll
         for (int aa = 0; aa < N; ++aa) v += tb.W2[iy][aa] * c[aa];
-        X[NT + iy * T + t] = v;
+        X[2 * NT + iy * T + t] = v;
       }
     }
     __syncwarp();
-    if (member && t < N) {
+    if (member && t < N) {  // delta rows into tile 3, zeta' of the result into tile 4
 #pragma unroll
       for (int ix = 0; ix < N; ++ix) {
         R dl = 0;
 #pragma unroll
-        for (int ap = 0; ap < N; ++ap) dl += tb.W2[ix][ap] * X[NT + t * T + ap];
-        znext[ix] = a.un_z[zo + t * N + ix] + (double)dl;
-        X[2 * NT + t * N + ix] = X[t * N + ix] + dl;  // zeta' of the result (wet check)
+        for (int ap = 0; ap < N; ++ap) dl += tb.W2[ix][ap] * X[2 * NT + t * T + ap];
+        X[3 * NT + t * N + ix] = dl;
+        X[4 * NT + t * N + ix] = ZN[t * N + ix] + dl;
       }
     }
     __syncwarp();
     // the closed form is the literal iteration only while every point stays wet:
     // check the result too, else redo the cell with the FP64 literal iteration
-    bool wet2 = true;
     if (member && t < N) {
 #pragma unroll
       for (int gx = 0; gx < G; ++gx) {
         R v = 0;
 #pragma unroll
-        for (int ix = 0; ix < N; ++ix) v += tb.BG[gx][ix] * X[2 * NT + t * N + ix];
-        X[3 * NT + t * T + gx] = v;
+        for (int ix = 0; ix < N; ++ix) v += tb.BG[gx][ix] * X[4 * NT + t * N + ix];
+        X[5 * NT + t * T + gx] = v;
       }
     }
     __syncwarp();
     if (member && t < G) {
-      const float *zb1e = a.sd1e ? a.sd1e + a.sdo1[cell] : nullptr;
 #pragma unroll
       for (int gy = 0; gy < G; ++gy) {
         R v = 0;
 #pragma unroll
-        for (int iy = 0; iy < N; ++iy) v += tb.BG[gy][iy] * X[3 * NT + iy * T + t];
+        for (int iy = 0; iy < N; ++iy) v += tb.BG[gy][iy] * X[5 * NT + iy * T + t];
         const R zb = zb1e ? (R)zb1e[gy * G + t] : zbe_flat;
-        wet2 = wet2 && (v + zb > (R)a.wet_threshold);
+        wet = wet && (v + zb > wet_thr);
       }
     }
-    const double dry2 = team_sum<T>(DRED, t, member, wet2 ? 0. : 1.);
-    need_fp64 = !(team_wet && dry2 == 0.);
+    const unsigned drym = __ballot_sync(OC_FULL, member && !wet);  // team OR of "not wet"
+    need_fp64 = ((drym >> (team * T)) & ((1u << T) - 1u)) != 0u;
   }
   if (__any_sync(OC_FULL, valid && need_fp64)) {
     // literal FP64 iteration (all lanes; teams with work = valid && need_fp64)
@@ -976,25 +1097,18 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
         for (int ix = 0; ix < N; ++ix) rhs[ix] = (double)BZ[t * N + ix] + rhs[ix];
     }
     zeta_iteration_fp64<P>(a, cell, DZ, DX, DRED, warp_norm, team, cpw, t, member, work, rhs);
-    if (work && t < N)
-#pragma unroll
-      for (int ix = 0; ix < N; ++ix) znext[ix] = DZ[t * N + ix];
-    __syncwarp();
+    if (work && t == 0) w_flag[team] = 1;
   }
-  if (valid && t < N) {
+  if (MIX && member && t < N && !need_fp64) {  // wet: keep delta (FP32) in BZ
 #pragma unroll
-    for (int ix = 0; ix < N; ++ix) {
-      const int d = t * N + ix;
-      if (a.out_z) a.out_z[zo + d] = znext[ix];
-      if (MIX && a.out_rz) a.out_rz[zo + d] = (float)(znext[ix] - zref);
-    }
+    for (int ix = 0; ix < N; ++ix) BZ[t * N + ix] = X[3 * NT + t * N + ix];
   }
+  __syncwarp();
 
-  // ---- 5. discharge: local_apply_inverse_mass_matrix_discharge (OceanDG.h:1532-1571)
-  //         + post-lambda (:1878-1909); ARK: :2052-2116 ----------------------------
-  // b = sum of weighted residual registers (ARK), or the ERK residual itself
+  // ---- 4. discharge: local_apply_inverse_mass_matrix_discharge (OceanDG.h:1532-1571);
+  //         ARK: cell_mass_discharge + inverse_modified_mass (:1573-1645, :2086-2116) ----
   if (split) {
-    // rhs of the modified mass: b = sum_j (f_j kex_j + ft_j kim_j)
+    // b = sum_j (f_j kex_j + ft_j kim_j); stores kex_s, kim_s
     if (member && t < N) {
 #pragma unroll
       for (int e = 0; e < 2; ++e)
@@ -1043,12 +1157,8 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
   // coefficient of the diagonal (JxW)^-1 at Gauss p+1; ARK internal: modified mass
   // (OceanDG.h:1573-1645): (JxW (1 + fm J_fric(r)))^-1
   R coef[N];  // column qx = t: coef[qy]
-  R corr[2][N];  // mixed ARK: S^T diag(JxW fm J) S q^n, rows of t < N (y-integrated per column)
 #pragma unroll
-  for (int i = 0; i < N; ++i) {
-    coef[i] = 0;
-    corr[0][i] = corr[1][i] = 0;
-  }
+  for (int i = 0; i < N; ++i) coef[i] = 0;
   if (member && t < N) {
 #pragma unroll
     for (int qy = 0; qy < N; ++qy) coef[qy] = R(1) / (tb.wM[t] * tb.wM[qy] * det);
@@ -1141,7 +1251,7 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
     }
     __syncwarp();
   }
-  // S^-1 diag(coef) S^-T applied to the two discharge components of RES
+  // S^-1 diag(coef) S^-T applied to the two discharge components of RES (in place)
   if (member && t < N) {  // x-pass: A[iy][qx] = sum_ix Sinv[ix][qx] in[iy][ix]
 #pragma unroll
     for (int e = 0; e < 2; ++e)
@@ -1175,7 +1285,7 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
     }
   }
   __syncwarp();
-  if (valid && t < N) {  // x back-transform, registers, RK update in FP64
+  if (member && t < N) {  // x back-transform into RES_q
 #pragma unroll
     for (int e = 0; e < 2; ++e)
 #pragma unroll
@@ -1183,27 +1293,119 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
         R v = 0;
 #pragma unroll
         for (int qx = 0; qx < N; ++qx) v += tb.Sinv[ix][qx] * X[(2 + e) * NT + t * T + qx];
-        const int64_t gidx = qo + e * NN + t * N + ix;
-        double nxt;
-        if (!a.ark) {
-          // ERK: k_q[s+1] = M^-1 L_h q; next = q^n + sum_j f_j k_q[j+1]
-          if (!a.last || a.write_kq_last) static_cast<KT *>(a.kq[s + 1])[gidx] = (KT)v;
-          const double kc = (double)(KT)v;
-          double acc = a.un_q[gidx] + dy.f[0] * (s == 0 ? kc : (double)static_cast<const KT *>(a.kq[1])[gidx]);
-          for (int j = 1; j < s + 1; ++j)
-            acc += dy.f[j] * (j == s ? kc : (double)static_cast<const KT *>(a.kq[j + 1])[gidx]);
-          nxt = acc;
-          if (a.out_q) a.out_q[gidx] = nxt;
-        } else if (!a.last) {
-          nxt = MIX ? a.un_q[gidx] + (double)v : (double)v;
-          if (a.out_q) a.out_q[gidx] = nxt;
-        } else {
-          if (a.aux_q) a.aux_q[gidx] = (double)v;
-          nxt = a.un_q[gidx] + (double)v;
-          a.out_q[gidx] = nxt;
-        }
-        if (MIX && a.out_rq) a.out_rq[gidx] = (float)nxt;
+        RES[(1 + e) * NN + t * N + ix] = v;
       }
+  }
+  __syncwarp();
+
+  // ---- 5. epilogue: warp-cooperative RK update and stores ------------------------
+  // FP64 form and the reference-ABI stage: next = u^n + sum_j f_j k_j in FP64.
+  // Mixed time step (fast): delta = sum_j f_j k_j in FP32; internal stages store
+  // u^n_f32 + delta (FP32), the last stage accumulates u^n + delta in FP64.
+  KT *kz_out = static_cast<KT *>(a.kz[s + 1]);
+  if constexpr (fast) {
+    // FP32 stage input u^n_f32 + delta; FP64 result only at the last stage (its
+    // own loop, so that no FP64 work is issued at the internal stages)
+    const bool anyflag = __any_sync(OC_FULL, lane < CPWMAX && lane < nvalid && w_flag[lane]);
+#pragma unroll 2
+    for (int e = lane; e < nvalid * NN; e += 32) {
+      const int j = e / NN, d = e - j * NN;
+      const int64_t gz = w_off[j] + d;
+      const R *Rj = Rreg(j);
+      kz_out[gz] = (KT)Rj[3 * NN + d];
+      if (s == 0 && a.out_unzf) a.out_unzf[gz] = (float)Rj[9 * NN + d];
+      if (a.out_rz) a.out_rz[gz] = (float)(Rj[9 * NN + d] + Rj[8 * NN + d]);
+    }
+    if (a.out_z) {
+#pragma unroll 2
+      for (int e = lane; e < nvalid * NN; e += 32) {
+        const int j = e / NN, d = e - j * NN;
+        const int64_t gz = w_off[j] + d;
+        a.out_z[gz] = a.un_z[gz] + (double)Rreg(j)[8 * NN + d];
+      }
+    }
+    if (anyflag) {  // cells that took the FP64 literal iteration (rare)
+      for (int e = lane; e < nvalid * NN; e += 32) {
+        const int j = e / NN, d = e - j * NN;
+        if (!w_flag[j]) continue;
+        const int64_t gz = w_off[j] + d;
+        const double *DZj = reinterpret_cast<const double *>(
+            wbase + D::template d_offset<R>() + j * D::bytes_d());
+        if (a.out_z) a.out_z[gz] = DZj[d];
+        if (a.out_rz) a.out_rz[gz] = (float)(DZj[d] - zref);
+      }
+    }
+  } else {
+#pragma unroll 2
+    for (int e = lane; e < nvalid * NN; e += 32) {  // zeta
+      const int j = e / NN, d = e - j * NN;
+      const int64_t gz = w_off[j] + d;
+      const R *Rj = Rreg(j);
+      kz_out[gz] = (KT)Rj[3 * NN + d];
+      double zn;
+      if (w_flag[j]) {
+        const double *DZj = reinterpret_cast<const double *>(
+            wbase + D::template d_offset<R>() + j * D::bytes_d());
+        zn = DZj[d];
+      } else {
+        zn = a.un_z[gz] + (double)Rj[8 * NN + d];
+      }
+      if (a.out_z) a.out_z[gz] = zn;
+      if (MIX && a.out_rz) a.out_rz[gz] = (float)(zn - zref);
+    }
+  }
+  const bool wkq = !a.ark && (!a.last || a.write_kq_last);
+  if (fast && !a.ark) {
+    // delta = sum_j f_j k_q[j+1] in FP32 (kept in smem for the FP64 loop)
+#pragma unroll 2
+    for (int e = lane; e < nvalid * 2 * NN; e += 32) {
+      const int j = e / (2 * NN), d = e - j * 2 * NN;
+      const int64_t gq = 2 * (int64_t)w_off[j] + d;
+      R *Rj = Rreg(j);
+      const R v = Rj[4 * NN + d];
+      if (wkq) static_cast<KT *>(a.kq[s + 1])[gq] = (KT)v;
+      R dl = fR[0] * (s == 0 ? v : (R) static_cast<const KT *>(a.kq[1])[gq]);
+      for (int jj = 1; jj < s + 1; ++jj)
+        dl += fR[jj] * (jj == s ? v : (R) static_cast<const KT *>(a.kq[jj + 1])[gq]);
+      if (s == 0 && a.out_unqf) a.out_unqf[gq] = (float)Rj[NN + d];
+      if (a.out_rq) {
+        const R qn = s == 0 ? Rj[NN + d] : (R)a.un_qf[gq];
+        a.out_rq[gq] = (float)(qn + dl);
+      }
+      Rj[4 * NN + d] = dl;
+    }
+    if (a.out_q) {
+#pragma unroll 2
+      for (int e = lane; e < nvalid * 2 * NN; e += 32) {
+        const int j = e / (2 * NN), d = e - j * 2 * NN;
+        const int64_t gq = 2 * (int64_t)w_off[j] + d;
+        a.out_q[gq] = a.un_q[gq] + (double)Rreg(j)[4 * NN + d];
+      }
+    }
+    return;
+  }
+#pragma unroll 2
+  for (int e = lane; e < nvalid * 2 * NN; e += 32) {  // discharge
+    const int j = e / (2 * NN), d = e - j * 2 * NN;
+    const int64_t gq = 2 * (int64_t)w_off[j] + d;
+    const R v = Rreg(j)[4 * NN + d];  // RES[NN + d] of team j
+    double nxt;
+    if (!a.ark) {
+      // ERK: k_q[s+1] = M^-1 L_h q; next = q^n + sum_j f_j k_q[j+1]
+      const double kc = (double)(KT)v;
+      if (wkq) static_cast<KT *>(a.kq[s + 1])[gq] = (KT)v;
+      double acc = a.un_q[gq] + dy.f[0] * (s == 0 ? kc : (double)static_cast<const KT *>(a.kq[1])[gq]);
+      for (int jj = 1; jj < s + 1; ++jj)
+        acc += dy.f[jj] * (jj == s ? kc : (double)static_cast<const KT *>(a.kq[jj + 1])[gq]);
+      nxt = acc;
+    } else if (!a.last) {
+      nxt = MIX ? a.un_q[gq] + (double)v : (double)v;
+    } else {
+      if (a.aux_q) a.aux_q[gq] = (double)v;
+      nxt = a.un_q[gq] + (double)v;
+    }
+    if (a.out_q) a.out_q[gq] = nxt;
+    if (MIX && a.out_rq) a.out_rq[gq] = (float)nxt;
   }
 }
 

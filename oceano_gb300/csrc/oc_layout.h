@@ -46,7 +46,9 @@ struct StageArgs {
   const int *deg;              // [n_cells]
   const int *off;              // [n_cells] zeta offset (discharge: 2*off)
   const double *geo;           // [n_cells*11]: x0,y0,J00,J01,J10,J11,Ji00,Ji01,Ji10,Ji11,det
-  const int *slots;            // [n_cells*8]: 2 refs per face number
+  const int *slots;            // [n_cells*8]: 2 refs per face number (host bookkeeping)
+  const int *cfrec;            // [n_cells*16]: 8 face records (other, packed word)
+  const int *cfsdo;            // [n_cells*8]: static face-data offsets, NULL without data
   const int *fcm, *fcp;        // [n_inner+n_bnd], [n_inner]
   const int *fpack;            // fm | fp<<4 | (sub+1)<<8 | orient<<12 | nf<<16
   const double *fnrm;          // [n_faces*2] minus normal
@@ -66,6 +68,14 @@ struct StageArgs {
   void *kq[2 * OC_MAXSTAGES];
   double *out_z, *out_q;       // next_ri or solution (FP64)
   float *out_rz, *out_rq;      // mixed: FP32 stage input of the next stage (may be NULL)
+  // mixed time-step path: FP32 copies of u^n (zeta - zeta_ref, q), written at
+  // stage 0 (out_un*) and read by the later stages (un_*f); internal stage
+  // inputs are then formed as u^n_f32 + delta in FP32 and only the last stage
+  // accumulates in FP64
+  const float *un_zf, *un_qf;
+  float *out_unzf, *out_unqf;
+  int fast_mixed;
+  const float *geof;           // [n_cells*11] FP32 copy of geo (mixed form)
   double *aux_q;               // ARK last stage: next_ri_discharge receives M^-1 rhs
   const struct StageDyn *dyn;  // device copy of the per-call coefficients
   int stage, n_stages, ark, last, write_kq_last, apply_mode;

@@ -13,38 +13,42 @@ namespace oc {
 
 static const int kMaxWarpsPerBlock = 4;
 
-template <typename R, typename KT, bool MIX>
+template <typename R, typename KT, bool MIX, typename RIN>
 static cudaError_t configure_one() {
   constexpr int P = OC_DEGREE;
   const int smem = kMaxWarpsPerBlock * Dims<P>::template warp_bytes<R>();
-  return cudaFuncSetAttribute(stage_kernel<P, R, KT, MIX>,
+  return cudaFuncSetAttribute(stage_kernel<P, R, KT, MIX, RIN>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
-template <typename R, typename KT, bool MIX>
+template <typename R, typename KT, bool MIX, typename RIN>
 static cudaError_t launch_one(const StageArgs &a, int grid, int wpb, cudaStream_t st) {
   constexpr int P = OC_DEGREE;
   if (wpb > kMaxWarpsPerBlock) return cudaErrorInvalidValue;
   const int smem = wpb * Dims<P>::template warp_bytes<R>();
-  stage_kernel<P, R, KT, MIX><<<grid, wpb * 32, smem, st>>>(a);
+  stage_kernel<P, R, KT, MIX, RIN><<<grid, wpb * 32, smem, st>>>(a);
   return cudaGetLastError();
 }
 
 // dynamic shared-memory opt-in, done once at set-up (outside any stream capture)
 cudaError_t OC_CAT(configure_stage_p, OC_DEGREE)() {
-  cudaError_t e = configure_one<double, double, false>();
-  if (e == cudaSuccess) e = configure_one<float, float, true>();
-  if (e == cudaSuccess) e = configure_one<float, double, true>();
+  cudaError_t e = configure_one<double, double, false, double>();
+  if (e == cudaSuccess) e = configure_one<float, float, true, float>();
+  if (e == cudaSuccess) e = configure_one<float, float, true, double>();
+  if (e == cudaSuccess) e = configure_one<float, double, true, double>();
   return e;
 }
 
-// variant 0: FP64; 1: mixed with FP32 registers; 2: mixed with FP64 registers
+// variant 0: FP64; 1: mixed time step with FP32 registers (FP64 stage input at
+// stage 0, FP32 afterwards); 2: mixed reference-ABI stage (FP64 registers and vectors)
 cudaError_t OC_CAT(launch_stage_p, OC_DEGREE)(const StageArgs &a, int variant, int grid, int wpb,
                                                cudaStream_t st) {
   switch (variant) {
-    case 0: return launch_one<double, double, false>(a, grid, wpb, st);
-    case 1: return launch_one<float, float, true>(a, grid, wpb, st);
-    case 2: return launch_one<float, double, true>(a, grid, wpb, st);
+    case 0: return launch_one<double, double, false, double>(a, grid, wpb, st);
+    case 1:
+      return a.r_is_float ? launch_one<float, float, true, float>(a, grid, wpb, st)
+                          : launch_one<float, float, true, double>(a, grid, wpb, st);
+    case 2: return launch_one<float, double, true, double>(a, grid, wpb, st);
     default: return cudaErrorInvalidValue;
   }
 }
