@@ -214,6 +214,21 @@ oc_status oc_vorticity_indicator(oc_op *op, const double *velocity, int32_t n_q_
 oc_status oc_project_vortex(oc_op *op, double time, double *height, double *discharge,
                             int32_t memory);
 
+/*
+ * Transport-speed maximum without any device allocation.  No counterpart in
+ * the reference: it serves callers that cannot call cudaMalloc when they need
+ * dt (code running during CUDA-graph stream capture, hosts whose device memory
+ * belongs to a pool or arena, allocation-free real-time loops).  height and
+ * discharge are device vectors, speed is one device double written on the
+ * handle's stream (NaN if the state holds a non-finite value); the call does
+ * not synchronise.  Scratch is a fixed device array inside the library: at most
+ * 524,288 cells (else OC_ERR_UNSUPPORTED); calls that overlap on the GPU share
+ * it and race; the first call on a device sets it up and must come before any
+ * stream capture.
+ */
+oc_status oc_transport_speed_noalloc(oc_op *op, const double *height, const double *discharge,
+                                     double *speed);
+
 /* device synchronisation and the stream the handle launches on */
 oc_status oc_synchronize(oc_op *op);
 void *oc_stream(oc_op *op);

@@ -69,6 +69,7 @@ EXPORTS = {
     "oc_vorticity_indicator": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
                                          C.c_int32]),
     "oc_project_vortex": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_int32]),
+    "oc_transport_speed_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "oc_synchronize": (C.c_int, [C.c_void_p]),
     "oc_stream": (C.c_void_p, [C.c_void_p]),
     "oc_launch_count": (C.c_int64, [C.c_void_p]),

@@ -38,6 +38,7 @@ def _sources():
                       [f"-DOC_DEGREE={p}", "-ftz=true", "-prec-div=false", "-prec-sqrt=false"]))
     units.append((os.path.join(CSRC, "oc_aux.cu"), "oc_aux.o", []))
     units.append((os.path.join(CSRC, "oc_api.cu"), "oc_api.o", []))
+    units.append((os.path.join(CSRC, "oc_noalloc.cu"), "oc_noalloc.o", []))
     return units
 
 

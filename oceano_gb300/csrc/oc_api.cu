@@ -945,3 +945,13 @@ extern "C" oc_status oc_project_vortex(oc_op *op, double time, double *z, double
   }
   return read_error(op);
 }
+
+// Handle data for oc_transport_speed_noalloc (oc_noalloc.cu): reads the handle only.
+namespace oc {
+bool noalloc_aux_args(const oc_op *op, AuxArgs *a, cudaStream_t *stream) {
+  if (!op || !op->d_geo) return false;
+  *a = aux_args(const_cast<oc_op *>(op));
+  *stream = op->stream;
+  return true;
+}
+}  // namespace oc
