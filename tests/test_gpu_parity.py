@@ -242,3 +242,14 @@ def test_unknown_boundary_id(gpu_lib):
         op.compute_cell_transport_speed(z, q)  # no boundary needed: fine
         op.perform_time_step("ssp33", 0.0, 1e-3, z, q)
     assert e.value.status == 2
+
+
+@pytest.mark.parametrize("name", ["mixed_degree", "hanging_p3_bathy", "open_bcs_p2"])
+def test_static_data_point_order(gpu_lib, name):
+    """The library lays static data out at the same points as the oracle."""
+    mesh, orc, op = setup(name)
+    for which in range(5):
+        a = op.quadrature_points(which)
+        b = orc.points(which)
+        assert a.shape == b.shape
+        assert np.abs(a - b).max() < 1e-13

@@ -1,0 +1,173 @@
+"""Known-answer tests of the FP64 oracle (CPU only).
+
+The reference ships no test suite and cannot be built here, so the oracle is
+pinned by properties the reference's scheme must have: free-stream
+preservation (also across hanging faces and degree jumps), the lake at rest to
+machine precision (well-balancing of OceanDG.h's hydrostatic reconstruction),
+global mass conservation of a stage, consistency of the explicit and additive
+stage drivers, and convergence to the analytic travelling vortex.
+"""
+import numpy as np
+import pytest
+
+from cases import VORTEX, hanging_mesh, mixed_degree
+from oceano_gb300 import QuadForest, uniform_mesh, vortex_mesh
+from oceano_gb300.icbc import vortex as vortex_np
+from oracle import oracle as O
+
+
+def uniform_state(mesh, z=1.0, q=(1.0, 0.0)):
+    off = mesh.offsets()
+    n = int(off[-1])
+    zz = np.full(n, z)
+    qq = np.zeros(2 * n)
+    for c in range(mesh.n_cells):
+        nd = off[c + 1] - off[c]
+        qq[2 * off[c]:2 * off[c] + nd] = q[0]
+        qq[2 * off[c] + nd:2 * off[c] + 2 * nd] = q[1]
+    return zz, qq
+
+
+def residuals(orc, z, q, t=0.0):
+    n = orc.n
+    kz = [np.zeros(n) for _ in range(4)]
+    kq = [np.zeros(2 * n) for _ in range(4)]
+    nz, nq = np.zeros(n), np.zeros(2 * n)
+    orc.stage_erk(0, 3, t, np.array([1e-3]), z, q, kz, kq, z.copy(), q.copy(), nz, nq)
+    return kz[1], kq[0], nz, nq
+
+
+@pytest.mark.parametrize("mesh_f", [lambda: vortex_mesh(0, 1), lambda: vortex_mesh(0, 4),
+                                    lambda: hanging_mesh(3), lambda: mixed_degree(hanging_mesh(2))])
+def test_free_stream_preserved(mesh_f):
+    mesh = mesh_f()
+    orc = O.Oracle(mesh, bcs={0: ("wall",)})
+    z, q = uniform_state(mesh)
+    rz, rq, nz, nq = residuals(orc, z, q)
+    assert np.abs(rz).max() < 1e-13 and np.abs(rq).max() < 1e-12
+    assert np.abs(nz - z).max() < 1e-13 and np.abs(nq - q).max() < 1e-12
+
+
+def bump(x, y):
+    zb = 1.0 - 0.4 * np.exp(-8 * ((x - 1.0) ** 2 + (y - 0.5) ** 2))
+    return np.stack([zb, 0.03 + 0 * x, 0 * x, 0 * x, 0 * x])
+
+
+@pytest.mark.parametrize("degree", [1, 3])
+def test_lake_at_rest(degree):
+    from cases import static_arrays
+    mesh = uniform_mesh(8, 4, (0.0, 2.0, 0.0, 1.0), False, degree)
+    orc = O.Oracle(mesh, friction=2, bcs={b: ("wall",) for b in (0, 1, 2)})
+    orc.set_static(*static_arrays(orc, bump))
+    z, q = uniform_state(mesh, z=0.25, q=(0.0, 0.0))
+    rz, rq, nz, nq = residuals(orc, z, q)
+    assert np.abs(rz).max() < 1e-15 and np.abs(rq).max() < 1e-14
+    assert np.abs(nz - z).max() < 1e-15 and np.abs(nq).max() < 1e-14
+
+
+def cell_integrals(mesh, z):
+    """int zeta over the domain (nodal GL quadrature is exact for degree 2p-1 >= p)."""
+    from oceano_gb300.basis import lobatto
+    off = mesh.offsets()
+    tot = 0.0
+    for c in range(mesh.n_cells):
+        p = int(mesh.degree[c])
+        _, w = lobatto(p + 1)
+        v = mesh.vertices[c]
+        det = (v[2] - v[0]) * (v[5] - v[1]) - (v[4] - v[0]) * (v[3] - v[1])
+        tot += det * np.kron(w, w) @ z[off[c]:off[c + 1]]
+    return tot
+
+
+@pytest.mark.parametrize("mesh_f", [lambda: vortex_mesh(0, 2), lambda: hanging_mesh(2)])
+def test_mass_conserved(mesh_f):
+    mesh = mesh_f()
+    orc = O.Oracle(mesh, bcs={0: ("wall",)}, vortex=VORTEX + [0, 0])
+    z, q = orc.project_vortex(0.0)
+    m0 = cell_integrals(mesh, z)
+    tb = O.TABLEAUX["ssp33"]
+    dt = 0.075 / orc.transport_speed(z, q)
+    for it in range(3):
+        O.erk_step(orc, tb["a"], tb["b"], tb["c"], it * dt, dt, z, q)
+    assert abs(cell_integrals(mesh, z) - m0) < 1e-13 * abs(m0)
+
+
+def test_erk_ark_same_height_residual():
+    mesh = vortex_mesh(0, 2)
+    orc = O.Oracle(mesh, bcs={0: ("wall",)}, vortex=VORTEX + [0, 0])
+    z, q = orc.project_vortex(0.0)
+    n = orc.n
+    a = [np.zeros(n) for _ in range(4)]
+    b = [np.zeros(2 * n) for _ in range(4)]
+    orc.stage_erk(0, 3, 0.0, np.array([1e-3]), z, q, a, b, z.copy(), q.copy(), np.zeros(n),
+                  np.zeros(2 * n))
+    c = [np.zeros(n) for _ in range(4)]
+    d = [np.zeros(2 * n) for _ in range(6)]
+    orc.stage_ark(0, 3, 0.0, np.array([1e-3]), np.array([1e-3]), 1e-3, z, q, c, d, z.copy(),
+                  q.copy(), np.zeros(n), np.zeros(2 * n))
+    assert np.array_equal(a[1], c[1])
+
+
+def test_tableaux_order_conditions():
+    for name, order in (("ssp33", 3), ("ssp22", 2), ("rk4", 4), ("giraldo32", 2)):
+        t = O.TABLEAUX[name]
+        b, c = np.array(t["b"]), np.array(t["c"])
+        assert abs(b.sum() - 1) < 1e-15
+        assert abs(b @ c - 0.5) < 1e-15
+        if order >= 3:
+            assert abs(b @ c ** 2 - 1 / 3) < 1e-15
+        for i, row in enumerate(t["a"]):  # row i gives the input of stage i+1
+            assert abs(sum(row) - c[i + 1]) < 1e-15
+
+
+def vortex_error(refine, degree, steps=20):
+    """L2 error of zeta at nodes after `steps` SSP-RK3 steps of the periodic vortex."""
+    from oceano_gb300.icbc import nodal_points, vortex_params
+    mesh = vortex_mesh(refine, degree)
+    vx = vortex_params(uoo=1.0, peak=0.1, r0=0.2)
+    orc = O.Oracle(mesh, bcs={0: ("wall",)}, vortex=vx + [0, 0])
+    z, q = orc.project_vortex(0.0)
+    dt = 0.05 * 0.1 / 4.2 * (0.5 ** refine)  # Courant 0.05 of the coarse mesh, halved per level
+    tb = O.TABLEAUX["ssp33"]
+    for it in range(steps):
+        O.erk_step(orc, tb["a"], tb["b"], tb["c"], it * dt, dt, z, q)
+    t = steps * dt
+    pts = nodal_points(mesh)
+    h, _, _ = vortex_np(pts[:, 0], pts[:, 1], t, *[vx[0], vx[1], vx[2], vx[3], vx[4], vx[5]])
+    return np.sqrt(np.mean((z - h) ** 2)), t
+
+
+def test_vortex_converges():
+    """Error at a fixed final time drops at least like h^2 under refinement (p=2)."""
+    e0, t0 = vortex_error(0, 2, steps=10)
+    e1, t1 = vortex_error(1, 2, steps=20)
+    assert abs(t0 - t1) < 1e-14
+    assert e1 < e0 / 4
+
+
+def test_projection_matches_nodal_interpolation():
+    from oceano_gb300.icbc import nodal_points, vortex_params
+    mesh = vortex_mesh(1, 3)
+    vx = vortex_params()
+    orc = O.Oracle(mesh, vortex=vx + [0, 0])
+    z, q = orc.project_vortex(0.0)
+    pts = nodal_points(mesh)
+    h, u, v = vortex_np(pts[:, 0], pts[:, 1], 0.0, *vx)
+    assert np.abs(z - h).max() < 1e-4
+
+
+def test_unknown_boundary_id_raises():
+    mesh = uniform_mesh(4, 2, (0, 2, 0, 1), False, 1)
+    orc = O.Oracle(mesh, bcs={0: ("wall",)})
+    z, q = uniform_state(mesh)
+    with pytest.raises(RuntimeError):
+        residuals(orc, z, q)
+
+
+def test_transport_speed_uniform():
+    mesh = uniform_mesh(20, 10, (0, 2, 0, 1), True, 1)
+    orc = O.Oracle(mesh, bcs={0: ("wall",)})
+    z, q = uniform_state(mesh)
+    h = 0.1
+    expect = np.sqrt(9.81) / h + 1.0 / h  # sigma_max(J^-1) c + |J^-1 u|
+    assert abs(orc.transport_speed(z, q) - expect) < 1e-12 * expect
