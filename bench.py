@@ -16,6 +16,14 @@ roofline : dominant kernel = the fused stage kernel; algorithmic bytes per
            DoF-stage as documented in DESIGN.md; peak from MEASURED_PEAKS.json.
 cpu_baseline / --impl reference: the FP64 C oracle (CPU restatement; the
            reference itself needs deal.II + MPI) with OpenMP on all host cores.
+
+Secondary workloads (--workload; same JSON keys, not the headline line):
+  hp        the vortex on the seeded random hp mesh (about 60k cells, degrees
+            1-4, hanging faces), SSP-RK3, launch shape autotuned;
+  channel   250x10 cells, p = 2, bump bathymetry, implicit Manning friction
+            (ARK Giraldo / TR-BDF2);
+  ensemble  64 vortices with seeded centres, radii and strengths on refined-disk
+            meshes of 5k-40k cells each (p = 1, 2), one operator over their union.
 """
 from __future__ import annotations
 
@@ -44,6 +52,75 @@ def workload():
     return mesh, vortex_params()
 
 
+class Workload:
+    """Operators (mixed, FP64), initial state, dt and scheme of one workload,
+    and a factory of the matching FP64 oracle for the CPU baseline."""
+
+    def __init__(self, name):
+        from oceano_gb300 import workloads as W
+        self.name = name
+        self.scheme = "ssp33"
+        if name == "vortex":
+            mesh, vx = workload()
+            self.op_m, self.op_d = make_op(mesh, vx, "mixed"), make_op(mesh, vx, "fp64")
+            n = self.op_d.n_dofs
+            self.z0, self.q0 = np.zeros(n), np.zeros(2 * n)
+            self.op_d.project_vortex(0.0, self.z0, self.q0)
+            self.desc = "vortex p=3, 320x160 cells (51200), 2457600 DoFs, SSP-RK3 step"
+            self.oracle_kw = dict(bcs={0: ("wall",)}, vortex=list(vx) + [0, 0])
+        elif name == "hp":
+            self.op_m, self.z0, self.q0 = W.hp_vortex("mixed")
+            self.op_d, _, _ = W.hp_vortex("fp64")
+            self.desc = (f"vortex on the seeded random hp mesh ({self.op_d.mesh.n_cells} cells, "
+                         f"p=1..4, hanging faces), SSP-RK3 step")
+            self.oracle_kw = dict(bcs={0: ("wall",)}, vortex=list(W.vortex_params()) + [0, 0])
+        elif name == "channel":
+            self.op_m, self.z0, self.q0 = W.channel("mixed")
+            self.op_d, _, _ = W.channel("fp64")
+            self.scheme = "ark_stage3_order2"
+            self.desc = ("channel 250x10 cells p=2, bump, implicit Manning n=0.03, "
+                         "ARK stage_3_order_2 step")
+            self.oracle_kw = dict(friction=2, bcs=W.CHANNEL_BCS)
+        elif name == "ensemble":
+            self.op_m, self.z0, self.q0, members, meshes = W.ensemble(64, "mixed")
+            from oceano_gb300.operator import OceanoOperator
+            self.op_d = OceanoOperator(self.op_m.mesh, precision="fp64")
+            self.op_d.set_wall_boundary(0)
+            self.desc = (f"64-member vortex ensemble, {self.op_d.mesh.n_cells} cells "
+                         f"(5k-40k per member, p=1,2), one operator, SSP-RK3 step")
+            self.oracle_kw = dict(bcs={0: ("wall",)})
+        else:
+            raise ValueError(name)
+        self.mesh = self.op_d.mesh
+        self.n = self.op_d.n_dofs
+        self.dt = CFL / self.op_d.compute_cell_transport_speed(self.z0, self.q0)
+
+    def oracle(self):
+        from oracle import oracle as O
+        orc = O.Oracle(self.mesh, **self.oracle_kw)
+        if self.name == "channel":
+            from oceano_gb300.icbc import channel_problem_data
+            from oceano_gb300 import workloads as W
+            arrs = []
+            for which in range(5):
+                xy = orc.points(which)
+                d = np.asarray(channel_problem_data(W.CHANNEL_MANNING)(xy[:, 0], xy[:, 1]))
+                arrs.append(np.ascontiguousarray(d.T).ravel() if which == 0 else
+                            np.ascontiguousarray(d[:2].T).ravel() if which == 2 else
+                            np.ascontiguousarray(d[0]))
+            orc.set_static(*arrs)
+        return orc
+
+    def oracle_step(self, orc, t, z, q):
+        from oracle import oracle as O
+        if self.scheme == "ssp33":
+            tb = O.TABLEAUX["ssp33"]
+            O.erk_step(orc, tb["a"], tb["b"], tb["c"], t, self.dt, z, q)
+        else:
+            g, tr = O.TABLEAUX["giraldo32"], O.TABLEAUX["trbdf2"]
+            O.ark_step(orc, g["a"], g["b"], g["c"], tr["a"], tr["d"], t, self.dt, z, q)
+
+
 def make_op(mesh, vx, precision):
     from oceano_gb300.operator import OceanoOperator
     op = OceanoOperator(mesh, precision=precision, zeta_reference=1.0 if precision == "mixed" else 0.0)
@@ -52,16 +129,17 @@ def make_op(mesh, vx, precision):
     return op
 
 
-def algorithmic_bytes(n_dofs_var, n_cells, mixed):
-    """Bytes one SSP-RK3 step must move: per stage the stage input r_i, u^n and
+def algorithmic_bytes(n_dofs_var, n_cells, mixed, static_bytes=0):
+    """Bytes one 3-stage step must move: per stage the stage input r_i, u^n and
     the stage output at their stored precision (stage 0: r_0 = u^n, counted
-    once), plus the affine geometry (J^-1 and det, 5 doubles per cell)."""
+    once), the affine geometry (J^-1 and det, 5 doubles per cell) and the static
+    data a stage reads (bathymetry, friction coefficient; FP32 in the mixed form)."""
     n = 3 * n_dofs_var  # scalar DoFs of zeta, hu, hv
     if mixed:
         per_dof = (8 + 4) + (4 + 8 + 4) + (4 + 8 + 8)
     else:
         per_dof = (8 + 8) + (8 + 8 + 8) + (8 + 8 + 8)
-    return n * per_dof + 3 * n_cells * 5 * 8
+    return n * per_dof + 3 * n_cells * 5 * 8 + 3 * static_bytes
 
 
 def measured_traffic():
@@ -134,7 +212,7 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def time_device(op, mesh, z0, q0, steps, warmup, dt, flush):
+def time_device(op, mesh, z0, q0, steps, warmup, dt, flush, scheme="ssp33"):
     """Per-step CUDA-event times (ms) of oc_perform_time_step on device vectors."""
     import torch
     stream = torch.cuda.ExternalStream(op.stream)
@@ -143,7 +221,7 @@ def time_device(op, mesh, z0, q0, steps, warmup, dt, flush):
     torch.cuda.synchronize()
     with torch.cuda.stream(stream):
         for i in range(warmup):
-            op.perform_time_step("ssp33", i * dt, dt, z, q)
+            op.perform_time_step(scheme, i * dt, dt, z, q)
         op.synchronize()
         times = []
         launches0 = op.launch_count
@@ -152,7 +230,7 @@ def time_device(op, mesh, z0, q0, steps, warmup, dt, flush):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            op.perform_time_step("ssp33", (warmup + i) * dt, dt, z, q)
+            op.perform_time_step(scheme, (warmup + i) * dt, dt, z, q)
             e1.record(stream)
             times.append((e0, e1))
         op.synchronize()
@@ -162,44 +240,43 @@ def time_device(op, mesh, z0, q0, steps, warmup, dt, flush):
     return ms, z.cpu().numpy(), q.cpu().numpy(), launches
 
 
-def time_e2e(op, z0, q0, steps, warmup, dt):
+def time_e2e(op, z0, q0, steps, warmup, dt, scheme="ssp33"):
     """Same steps through the C ABI with pinned host buffers (copies timed)."""
     import torch
     zh = torch.from_numpy(z0.copy()).pin_memory()
     qh = torch.from_numpy(q0.copy()).pin_memory()
     stream = torch.cuda.ExternalStream(op.stream)
     for i in range(warmup):
-        _host_step(op, i * dt, dt, zh, qh)
+        _host_step(op, i * dt, dt, zh, qh, scheme)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for i in range(steps):
-        _host_step(op, (warmup + i) * dt, dt, zh, qh)
+        _host_step(op, (warmup + i) * dt, dt, zh, qh, scheme)
     e1.record(stream)
     e1.synchronize()
     return e0.elapsed_time(e1) / steps, (zh.numel() + qh.numel()) * 8
 
 
-def _host_step(op, t, dt, zh, qh):
+def _host_step(op, t, dt, zh, qh, scheme="ssp33"):
     """oc_perform_time_step with OC_MEM_HOST on pinned tensors (host pointers)."""
     import ctypes as C
     from oceano_gb300 import _lib
-    _lib.check(_lib.lib().oc_perform_time_step(op.h, _lib.SCHEME["ssp33"], t, dt,
+    _lib.check(_lib.lib().oc_perform_time_step(op.h, _lib.SCHEME[scheme], t, dt,
                                                C.c_void_p(zh.data_ptr()),
                                                C.c_void_p(qh.data_ptr()), _lib.OC_MEM_HOST),
                op.h)
 
 
-def cpu_baseline(mesh, vx, z0, q0, dt, steps):
+def cpu_baseline(wl, steps):
     """FP64 C oracle (OpenMP, all host cores) on `steps` full RK steps."""
     from oracle import oracle as O
-    orc = O.Oracle(mesh, bcs={0: ("wall",)}, vortex=list(vx) + [0, 0])
-    tb = O.TABLEAUX["ssp33"]
-    z, q = z0.copy(), q0.copy()
+    orc = wl.oracle()
+    z, q = wl.z0.copy(), wl.q0.copy()
     t0 = time.perf_counter()
     for i in range(steps):
-        O.erk_step(orc, tb["a"], tb["b"], tb["c"], i * dt, dt, z, q)
+        wl.oracle_step(orc, i * wl.dt, z, q)
     el = time.perf_counter() - t0
     ndof = 3 * orc.n
     return ndof * 3 * steps / el, O.num_threads(), el
@@ -245,19 +322,16 @@ def run_reference(args, rank, world):
     """CPU restatement timed on the host cores (rank 0 only)."""
     if rank != 0:
         return
-    mesh, vx = workload()
-    from oracle import oracle as O
-    orc = O.Oracle(mesh, bcs={0: ("wall",)}, vortex=list(vx) + [0, 0])
-    z0, q0 = orc.project_vortex(0.0)
-    dt = CFL / orc.transport_speed(z0, q0)
-    tb = O.TABLEAUX["ssp33"]
-    z, q = z0.copy(), q0.copy()
+    wl = Workload(args.workload)
+    orc = wl.oracle()
+    z, q = wl.z0.copy(), wl.q0.copy()
     for i in range(args.warmup):
-        O.erk_step(orc, tb["a"], tb["b"], tb["c"], i * dt, dt, z, q)
+        wl.oracle_step(orc, i * wl.dt, z, q)
     t0 = time.perf_counter()
     for i in range(args.steps):
-        O.erk_step(orc, tb["a"], tb["b"], tb["c"], i * dt, dt, z, q)
+        wl.oracle_step(orc, (args.warmup + i) * wl.dt, z, q)
     el = time.perf_counter() - t0
+    from oracle import oracle as O
     ndof = 3 * orc.n
     v = ndof * 3 * args.steps / el
     cores = O.num_threads()
@@ -266,10 +340,9 @@ def run_reference(args, rank, world):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "vortex p=3, 320x160 cells (51200), 2457600 DoFs, SSP-RK3",
-                   "degree": DEGREE, "cells": mesh.n_cells, "dofs": ndof},
+        "config": {"workload": wl.desc, "cells": wl.mesh.n_cells, "dofs": ndof},
         "cpu_baseline": {"value": v, "unit": "DoF-stage/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} full SSP-RK3 steps of the workload"},
+                         "sample": f"{args.steps} full time steps of the workload"},
         "e2e": {"value": v, "unit": "DoF-stage/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "note": "FP64 C restatement of the reference operator (OpenMP); the reference "
@@ -282,6 +355,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="vortex", choices=["vortex", "hp", "channel", "ensemble"])
     ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -293,31 +367,32 @@ def main():
     import torch
     import __graft_entry__ as ge
     ge.build()
-    mesh, vx = workload()
-    op_m = make_op(mesh, vx, "mixed")
-    op_d = make_op(mesh, vx, "fp64")
-    n = op_m.n_dofs
-    z0, q0 = np.zeros(n), np.zeros(2 * n)
-    op_d.project_vortex(0.0, z0, q0)
-    dt = CFL / op_d.compute_cell_transport_speed(z0, q0)
+    wl = Workload(args.workload)
+    mesh, n, dt, z0, q0 = wl.mesh, wl.n, wl.dt, wl.z0, wl.q0
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     barrier(world)
     with Clocks() as clk:  # samples over both timed loops (the mixed one alone is ~30 ms)
-        ms_m, zm, qm, launches = time_device(op_m, mesh, z0, q0, args.steps, args.warmup, dt, flush)
-        ms_d, zd, qd, _ = time_device(op_d, mesh, z0, q0, args.steps, args.warmup, dt, flush)
+        ms_m, zm, qm, launches = time_device(wl.op_m, mesh, z0, q0, args.steps, args.warmup, dt,
+                                             flush, wl.scheme)
+        ms_d, zd, qd, _ = time_device(wl.op_d, mesh, z0, q0, args.steps, args.warmup, dt, flush,
+                                      wl.scheme)
     t_m = max_over_ranks(sum(ms_m) / 1e3, world)
     t_d = max_over_ranks(sum(ms_d) / 1e3, world)
     ndof = 3 * n
-    units = ndof * 3 * args.steps * world  # every rank advances its own replica
+    stages = 3
+    units = ndof * stages * args.steps * world  # every rank advances its own replica
     value = units / t_m
     value_d = units / t_d
-    e2e_ms, io_bytes = time_e2e(op_m, z0, q0, max(2, args.steps // 4), 2, dt)
+    e2e_ms, io_bytes = time_e2e(wl.op_m, z0, q0, max(2, args.steps // 4), 2, dt, wl.scheme)
     e2e_ms = max_over_ranks(e2e_ms, world)
-    e2e_value = ndof * 3 * world / (e2e_ms / 1e3)
+    e2e_value = ndof * stages * world / (e2e_ms / 1e3)
     peak, peak_kind = peaks()
-    bytes_step = algorithmic_bytes(n, mesh.n_cells, True)
+    static_bytes = 4 * sum(wl.op_m.static_data_size(k) for k in range(5)) \
+        if wl.name == "channel" else 0
+    bytes_step = algorithmic_bytes(n, mesh.n_cells, True, static_bytes)
     step_s = statistics.mean(ms_m) / 1e3
-    achieved = bytes_step / 3 / (step_s / 3) / 1e9  # per launch: step = 3 launches
+    per_step_launches = launches / args.steps
+    achieved = bytes_step / per_step_launches / (step_s / per_step_launches) / 1e9
     clocks = clk.summary()
     err_z, err_q = rel(zm, zd), rel(qm, qd)
     out = {
@@ -325,17 +400,19 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_m / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": "vortex p=3, 320x160 cells (51200), 2457600 DoFs, SSP-RK3 step",
-                   "degree": DEGREE, "cells": mesh.n_cells, "dofs": ndof,
+        "config": {"workload": wl.desc, "cells": mesh.n_cells, "dofs": ndof,
+                   "degrees": sorted(int(p) for p in np.unique(mesh.degree)),
                    "l2": "flushed between steps (512 MB write)",
-                   "replicas": world},
-        "fp64": {"value": value_d, "ms_per_step": 1e3 * t_d / args.steps},
+                   "replicas": world, "launch": wl.op_m.launch_config},
+        "fp64": {"value": value_d, "ms_per_step": 1e3 * t_d / args.steps,
+                 "launch": wl.op_d.launch_config},
         "speedup_vs_fp64": value / value_d,
         "l2_error_vs_fp64": {"zeta": err_z, "hu_hv": err_q, "after_steps": args.warmup + args.steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": measured_traffic(),
+                     "frac": achieved / peak,
+                     "traffic": measured_traffic() if args.workload == "vortex" else None,
                      "peak_source": peak_kind,
-                     "kernel": "oc::stage_kernel<3,float,float,true>",
+                     "kernel": "oc::stage_kernel (mixed, FP32 stage input)",
                      "algorithmic_bytes_per_step": bytes_step},
         "e2e": {"value": e2e_value, "unit": "DoF-stage/s", "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes},
@@ -343,9 +420,9 @@ def main():
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu:
-        v, cores, el = cpu_baseline(mesh, vx, z0, q0, dt, args.cpu_steps)
+        v, cores, el = cpu_baseline(wl, args.cpu_steps)
         out["cpu_baseline"] = {"value": v, "unit": "DoF-stage/s", "cores": cores, "kind": "port",
-                               "sample": f"{args.cpu_steps} full SSP-RK3 step(s) of the workload "
+                               "sample": f"{args.cpu_steps} full time step(s) of the workload "
                                          f"({el:.1f} s)"}
     if rank == 0:
         print(json.dumps(out))

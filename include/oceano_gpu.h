@@ -229,6 +229,21 @@ oc_status oc_project_vortex(oc_op *op, double time, double *height, double *disc
 oc_status oc_transport_speed_noalloc(oc_op *op, const double *height, const double *discharge,
                                      double *speed);
 
+/* Launch configuration of the stage kernels (no reference counterpart: deal.II's
+ * MatrixFree loops have no launch shape).  OC_LAUNCH_AUTO (default) times, at the
+ * first oc_perform_time_step, one launch per degree group with 1, 2 or 4 warps
+ * per block against one launch over all groups (hp meshes) with 2 or 4, on a
+ * scratch copy of the solution, and keeps the fastest.  The other modes fix the
+ * launch shape and tune only the block size.  Setting a mode drops the tuned
+ * configuration and the captured step graph. */
+#define OC_LAUNCH_AUTO 0
+#define OC_LAUNCH_PER_GROUP 1
+#define OC_LAUNCH_ONE 2
+oc_status oc_set_launch_mode(oc_op *op, int32_t mode);
+/* out[0] one launch for all groups (0/1), out[1] its warps per block,
+ * out[2..5] warps per block of the degree 1..4 groups, out[6] tuned (0/1) */
+oc_status oc_launch_config(const oc_op *op, int32_t *out);
+
 /* device synchronisation and the stream the handle launches on */
 oc_status oc_synchronize(oc_op *op);
 void *oc_stream(oc_op *op);

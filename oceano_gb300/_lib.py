@@ -18,6 +18,7 @@ OC_MEM_HOST, OC_MEM_DEVICE = 0, 1
 OC_PREC_FP64, OC_PREC_MIXED = 0, 1
 BC_KIND = {"none": 0, "wall": 1, "supercritical_inflow": 2, "supercritical_outflow": 3,
            "height_inflow": 4, "discharge_inflow": 5, "absorbing_outflow": 6}
+LAUNCH_MODE = {"auto": 0, "per_group": 1, "one": 2}
 SCHEME = {"forward_euler": 0, "ssp22": 1, "ssp33": 2, "rk4": 3, "stage3_order2": 4,
           "ark_stage3_order2": 5}
 
@@ -70,6 +71,8 @@ EXPORTS = {
                                          C.c_int32]),
     "oc_project_vortex": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_int32]),
     "oc_transport_speed_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "oc_set_launch_mode": (C.c_int, [C.c_void_p, C.c_int32]),
+    "oc_launch_config": (C.c_int, [C.c_void_p, C.c_void_p]),
     "oc_synchronize": (C.c_int, [C.c_void_p]),
     "oc_stream": (C.c_void_p, [C.c_void_p]),
     "oc_launch_count": (C.c_int64, [C.c_void_p]),

@@ -36,6 +36,10 @@ def _sources():
         # square root (affects single precision only; the FP64 form is IEEE)
         units.append((os.path.join(CSRC, "oc_stage_inst.cu"), f"oc_stage_p{p}.o",
                       [f"-DOC_DEGREE={p}", "-ftz=true", "-prec-div=false", "-prec-sqrt=false"]))
+    for v in (0, 1, 2):
+        units.append((os.path.join(CSRC, "oc_stage_hp.cu"), f"oc_stage_hp_v{v}.o",
+                      [f"-DOC_HP_VARIANT={v}", "-ftz=true", "-prec-div=false",
+                       "-prec-sqrt=false"]))
     units.append((os.path.join(CSRC, "oc_aux.cu"), "oc_aux.o", []))
     units.append((os.path.join(CSRC, "oc_api.cu"), "oc_api.o", []))
     units.append((os.path.join(CSRC, "oc_noalloc.cu"), "oc_noalloc.o", []))
@@ -63,7 +67,7 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         return cmd, r
 
-    with cf.ThreadPoolExecutor(max_workers=min(6, os.cpu_count() or 2)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(10, os.cpu_count() or 2)) as ex:
         for cmd, r in ex.map(run, jobs):
             if verbose or r.returncode:
                 print(" ".join(cmd))

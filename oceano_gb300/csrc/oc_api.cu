@@ -31,6 +31,16 @@ cudaError_t upload_tables_p2(const DegTables<double> *, const DegTables<float> *
 cudaError_t upload_tables_p3(const DegTables<double> *, const DegTables<float> *);
 cudaError_t upload_tables_p4(const DegTables<double> *, const DegTables<float> *);
 
+cudaError_t configure_stage_hp_v0();
+cudaError_t configure_stage_hp_v1();
+cudaError_t configure_stage_hp_v2();
+cudaError_t launch_stage_hp_v0(const StageArgs &, int, int, cudaStream_t);
+cudaError_t launch_stage_hp_v1(const StageArgs &, int, int, cudaStream_t);
+cudaError_t launch_stage_hp_v2(const StageArgs &, int, int, cudaStream_t);
+cudaError_t upload_tables_hp_v0(const DegTables<double> *, const DegTables<float> *);
+cudaError_t upload_tables_hp_v1(const DegTables<double> *, const DegTables<float> *);
+cudaError_t upload_tables_hp_v2(const DegTables<double> *, const DegTables<float> *);
+
 cudaError_t aux_upload_tables(const DegTables<double> *, const DegTables<float> *);
 cudaError_t launch_transport_speed(const AuxArgs &, const double *, const double *,
                                    unsigned long long *, cudaStream_t);
@@ -103,6 +113,7 @@ struct oc_op {
   int *d_cfrec = nullptr, *d_cfsdo = nullptr;
   double *d_geo = nullptr, *d_fnrm = nullptr, *d_flen = nullptr;
   float *d_geof = nullptr;
+  double *d_dscratch = nullptr;  // mixed form: FP64 zeta work area per (warp, team) slot
   double *d_sd[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   float *d_sde[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   // degree groups
@@ -128,7 +139,15 @@ struct oc_op {
   double *ts_z = nullptr, *ts_q = nullptr;  // solution when the caller passes host memory
   double *ts_aux = nullptr;
   float *ts_unzf = nullptr, *ts_unqf = nullptr;  // FP32 copies of u^n (mixed time step)
+  // launch configuration: OC_LAUNCH_AUTO tunes it at the first time step
+  int launch_mode = OC_LAUNCH_AUTO;
+  int tuned = 0;
+  int use_hp = 0;                           // one launch for all degree groups
+  int hp_wpb = 4;                           // warps per block of that launch
+  int wpb[OC_MAXDEG + 1] = {4, 4, 4, 4, 4}; // warps per block per degree group
+  float tune_ms[2] = {0.f, 0.f};            // measured stage time: per-group, one launch
   // graph cache of oc_perform_time_step
+  int64_t graph_launches = 0;
   cudaGraphExec_t graph = nullptr;
   int graph_scheme = -1;
   const void *graph_z = nullptr, *graph_q = nullptr;
@@ -163,6 +182,12 @@ static cudaError_t alloc(oc_op *op, void **dst, size_t bytes) {
   return e;
 }
 
+static int n_groups(const oc_op *op) {
+  int k = 0;
+  for (int p = 1; p <= OC_MAXDEG; ++p) k += op->group_n[p] > 0;
+  return k;
+}
+
 static int cells_per_warp(int p) {
   switch (p) {
     case 1: return stage_cells_per_warp_p1();
@@ -172,12 +197,21 @@ static int cells_per_warp(int p) {
   }
 }
 
-static cudaError_t launch_stage(int p, const StageArgs &a, int variant, int grid, cudaStream_t s) {
+static cudaError_t launch_stage(int p, const StageArgs &a, int variant, int grid, int wpb,
+                                cudaStream_t s) {
   switch (p) {
-    case 1: return launch_stage_p1(a, variant, grid, kWarpsPerBlock, s);
-    case 2: return launch_stage_p2(a, variant, grid, kWarpsPerBlock, s);
-    case 3: return launch_stage_p3(a, variant, grid, kWarpsPerBlock, s);
-    default: return launch_stage_p4(a, variant, grid, kWarpsPerBlock, s);
+    case 1: return launch_stage_p1(a, variant, grid, wpb, s);
+    case 2: return launch_stage_p2(a, variant, grid, wpb, s);
+    case 3: return launch_stage_p3(a, variant, grid, wpb, s);
+    default: return launch_stage_p4(a, variant, grid, wpb, s);
+  }
+}
+
+static cudaError_t launch_stage_hp(int hv, const StageArgs &a, int grid, int wpb, cudaStream_t s) {
+  switch (hv) {
+    case 0: return launch_stage_hp_v0(a, grid, wpb, s);
+    case 1: return launch_stage_hp_v1(a, grid, wpb, s);
+    default: return launch_stage_hp_v2(a, grid, wpb, s);
   }
 }
 
@@ -187,6 +221,25 @@ const char *oc_last_error(const oc_op *op) { return op ? op->err.c_str() : "null
 int64_t oc_n_dofs(const oc_op *op) { return op ? op->n_dofs : -1; }
 int64_t oc_launch_count(const oc_op *op) { return op ? op->launches : -1; }
 void *oc_stream(oc_op *op) { return op ? (void *)op->stream : nullptr; }
+
+oc_status oc_set_launch_mode(oc_op *op, int32_t mode) {
+  if (!op) return OC_ERR_INVALID_ARG;
+  if (mode < OC_LAUNCH_AUTO || mode > OC_LAUNCH_ONE)
+    return fail(op, OC_ERR_INVALID_ARG, "unknown launch mode");
+  op->launch_mode = mode;
+  op->tuned = 0;
+  op->use_hp = mode == OC_LAUNCH_ONE && n_groups(op) > 1;
+  if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
+  return OC_OK;
+}
+
+oc_status oc_launch_config(const oc_op *op, int32_t *out) {
+  if (!op || !out) return OC_ERR_INVALID_ARG;
+  out[0] = op->use_hp; out[1] = op->hp_wpb;
+  for (int p = 1; p <= OC_MAXDEG; ++p) out[1 + p] = op->wpb[p];
+  out[6] = op->tuned;
+  return OC_OK;
+}
 
 oc_status oc_synchronize(oc_op *op) {
   if (!op) return OC_ERR_INVALID_ARG;
@@ -371,6 +424,20 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
     op->group_n[p] = (int)g.size();
     if (!uniform && !g.empty()) OC_TRY(upload(op, &op->d_group[p], g.data(), g.size()));
   }
+  if (op->prm.precision == OC_PREC_MIXED) {
+    // FP64 zeta work area of the mixed kernels: one slot per (warp, team) of the
+    // largest degree-group launch
+    // (the one-launch hp grid is the longest: every group's warps, each group
+    // rounded up to whole blocks of at most kWarpsPerBlock warps)
+    size_t warps = 0;
+    for (int p = 1; p <= OC_MAXDEG; ++p) {
+      const int cpw = (cells_per_warp(p) / op->prm.batch_width) * op->prm.batch_width;
+      if (op->group_n[p] == 0 || cpw == 0) continue;
+      warps += (op->group_n[p] + cpw - 1) / cpw + kWarpsPerBlock;
+    }
+    const size_t slots = warps * OC_MAXCPW;
+    OC_TRY(alloc(op, (void **)&op->d_dscratch, std::max<size_t>(slots, 1) * OC_DSTRIDE * 8));
+  }
   // tables
   std::vector<DegTables<double>> td(OC_MAXDEG);
   std::vector<DegTables<float>> tf(OC_MAXDEG);
@@ -382,6 +449,9 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   OC_TRY(upload_tables_p2(td.data(), tf.data()));
   OC_TRY(upload_tables_p3(td.data(), tf.data()));
   OC_TRY(upload_tables_p4(td.data(), tf.data()));
+  OC_TRY(upload_tables_hp_v0(td.data(), tf.data()));
+  OC_TRY(upload_tables_hp_v1(td.data(), tf.data()));
+  OC_TRY(upload_tables_hp_v2(td.data(), tf.data()));
   OC_TRY(aux_upload_tables(td.data(), tf.data()));
   OC_TRY(alloc(op, (void **)&op->d_err, sizeof(int)));
   OC_TRY(alloc(op, (void **)&op->d_speed, sizeof(unsigned long long)));
@@ -391,6 +461,9 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   OC_TRY(configure_stage_p2());
   OC_TRY(configure_stage_p3());
   OC_TRY(configure_stage_p4());
+  OC_TRY(configure_stage_hp_v0());
+  OC_TRY(configure_stage_hp_v1());
+  OC_TRY(configure_stage_hp_v2());
   OC_TRY(cudaMemset(op->d_err, 0, sizeof(int)));
   OC_TRY(cudaDeviceSynchronize());
   *out = op;
@@ -514,6 +587,7 @@ static void fill_common(oc_op *op, StageArgs &a) {
   a.sdo0 = op->d_sdo[0]; a.sdo1 = op->d_sdo[1]; a.sdo2 = op->d_sdo[2];
   a.cfrec = op->d_cfrec;
   a.geof = op->prm.precision == OC_PREC_MIXED ? op->d_geof : nullptr;
+  a.dscratch = op->d_dscratch;
   a.cfsdo = (op->d_sd[3] || op->d_sd[4]) ? op->d_cfsdo : nullptr;
   const double cu = op->prm.threshold_wetdry;
   a.g = op->prm.g; a.cu4 = cu * cu * cu * cu; a.nu = op->prm.horizontal_viscosity;
@@ -538,19 +612,41 @@ static oc_status check_boundaries(oc_op *op) {
   return OC_OK;
 }
 
-// launch the fused kernel over every degree group
+// launch the fused kernel over every degree group: one launch per group, or
+// (hp meshes, use_hp) one launch whose grid concatenates the groups, highest
+// degree first; variant 2 (the mixed reference-ABI stage) always per group
 static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
   const int batch = op->prm.batch_width;
+  for (int p = 1; p <= OC_MAXDEG; ++p)
+    if (op->group_n[p] && (cells_per_warp(p) / batch) * batch == 0)
+      return fail(op, OC_ERR_UNSUPPORTED, "batch_width larger than the cells of a warp");
+  if (op->use_hp && variant != 2 && n_groups(op) > 1) {
+    const int wpb = op->hp_wpb;
+    int b0 = 0;
+    for (int p = OC_MAXDEG; p >= 1; --p) {
+      const int n = op->group_n[p];
+      const int cpw = (cells_per_warp(p) / batch) * batch;
+      a.hp_first_block[p] = b0;
+      a.hp_n[p] = n;
+      a.hp_cells[p] = op->d_group[p];
+      a.hp_blocks[p] = n ? (n + wpb * cpw - 1) / (wpb * cpw) : 0;
+      b0 += a.hp_blocks[p];
+    }
+    const int hv = variant == 0 ? 0 : (a.r_is_float ? 1 : 2);
+    OC_TRY(launch_stage_hp(hv, a, b0, wpb, op->stream));
+    op->launches++;
+    return OC_OK;
+  }
   for (int p = 1; p <= OC_MAXDEG; ++p) {
     const int n = op->group_n[p];
     if (n == 0) continue;
     const int cpw = (cells_per_warp(p) / batch) * batch;
-    if (cpw == 0) return fail(op, OC_ERR_UNSUPPORTED, "batch_width larger than the cells of a warp");
+    const int wpb = op->wpb[p];
     a.n_group = n;
     a.group_cells = op->uniform_deg ? nullptr : op->d_group[p];
     a.group_first = 0;
-    const int grid = (n + kWarpsPerBlock * cpw - 1) / (kWarpsPerBlock * cpw);
-    OC_TRY(launch_stage(p, a, variant, grid, op->stream));
+    const int grid = (n + wpb * cpw - 1) / (wpb * cpw);
+    OC_TRY(launch_stage(p, a, variant, grid, wpb, op->stream));
     op->launches++;
   }
   return OC_OK;
@@ -697,12 +793,12 @@ static oc_status ensure_ts(oc_op *op, const Scheme &sc) {
   return OC_OK;
 }
 
-// enqueue the stages of one time step on op->stream (capturable)
-static oc_status enqueue_step(oc_op *op, const Scheme &sc, double *z, double *q) {
+// arguments of stage st of a time step on the solution (z, q)
+static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, double *q,
+                            StageArgs &a) {
   const bool mixed = op->prm.precision == OC_PREC_MIXED;
-  StageArgs a;
   fill_common(op, a);
-  for (int st = 0; st < sc.s; ++st) {
+  {
     const bool last = st == sc.s - 1;
     a.dyn = op->d_dyn + st;
     a.stage = st; a.n_stages = sc.s; a.ark = sc.ark; a.last = last; a.write_kq_last = 0;
@@ -731,10 +827,112 @@ static oc_status enqueue_step(oc_op *op, const Scheme &sc, double *z, double *q)
       a.out_z = (double *)op->ts_rz[st & 1]; a.out_q = (double *)op->ts_rq[st & 1];
       a.out_rz = nullptr; a.out_rq = nullptr; a.aux_q = nullptr;
     }
+  }
+}
+
+// enqueue the stages of one time step on op->stream (capturable)
+static oc_status enqueue_step(oc_op *op, const Scheme &sc, double *z, double *q) {
+  const bool mixed = op->prm.precision == OC_PREC_MIXED;
+  for (int st = 0; st < sc.s; ++st) {
+    StageArgs a;
+    step_stage_args(op, sc, st, z, q, a);
     oc_status s = launch_groups(op, a, mixed ? 1 : 0);
     if (s != OC_OK) return s;
   }
   return OC_OK;
+}
+
+// mean time (ms) of `reps` launches of stage 1 of a time step (stage 0 first,
+// to fill its inputs); the stage reads (z, q) and writes only time-step registers
+static oc_status time_stage(oc_op *op, const Scheme &sc, double *z, double *q, int reps,
+                            float *ms) {
+  const bool mixed = op->prm.precision == OC_PREC_MIXED;
+  StageArgs a0, a1;
+  step_stage_args(op, sc, 0, z, q, a0);
+  step_stage_args(op, sc, sc.s > 2 ? 1 : 0, z, q, a1);
+  oc_status s = launch_groups(op, a0, mixed ? 1 : 0);
+  if (s != OC_OK) return s;
+  cudaEvent_t e0, e1;
+  OC_TRY(cudaEventCreate(&e0));
+  OC_TRY(cudaEventCreate(&e1));
+  for (int r = 0; r < 2 && s == OC_OK; ++r) s = launch_groups(op, a1, mixed ? 1 : 0);  // warm-up
+  cudaEventRecord(e0, op->stream);
+  for (int r = 0; r < reps && s == OC_OK; ++r) s = launch_groups(op, a1, mixed ? 1 : 0);
+  cudaEventRecord(e1, op->stream);
+  cudaError_t ce = cudaEventSynchronize(e1);
+  float t = 0.f;
+  if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (s != OC_OK) return s;
+  if (ce != cudaSuccess) return fail(op, OC_ERR_CUDA, cudaGetErrorString(ce));
+  *ms = t / reps;
+  return OC_OK;
+}
+
+// Launch autotuner (first time step, before the graph is captured): warps per
+// block {1, 2, 4} per degree group for per-group launches and {2, 4} for the
+// one-launch hp stage, each timed on a scratch copy of the solution; keeps the
+// fastest configuration.  OC_LAUNCH_PER_GROUP / OC_LAUNCH_ONE fix the mode and
+// tune only its block size.
+static oc_status autotune(oc_op *op, const Scheme &sc, const double *z, const double *q) {
+  const size_t nz = op->n_dofs, nq = 2 * nz;
+  double *tz = nullptr, *tq = nullptr;
+  OC_TRY(cudaMalloc((void **)&tz, nz * 8));
+  OC_TRY(cudaMalloc((void **)&tq, nq * 8));
+  oc_status st = OC_OK;
+  cudaError_t ce = cudaMemcpyAsync(tz, z, nz * 8, cudaMemcpyDeviceToDevice, op->stream);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(tq, q, nq * 8, cudaMemcpyDeviceToDevice, op->stream);
+  if (ce != cudaSuccess) st = fail(op, OC_ERR_CUDA, cudaGetErrorString(ce));
+  const int64_t launches = op->launches;
+  const int reps = 5;
+  const int cand[3] = {1, 2, 4};
+  // per-group launches: each group alone, best block size per degree
+  float per_group = 0.f;
+  if (st == OC_OK && op->launch_mode != OC_LAUNCH_ONE) {
+    op->use_hp = 0;
+    int saved[OC_MAXDEG + 1];
+    for (int p = 0; p <= OC_MAXDEG; ++p) saved[p] = op->group_n[p];
+    for (int p = 1; p <= OC_MAXDEG && st == OC_OK; ++p) {
+      if (!saved[p]) continue;
+      for (int k = 0; k <= OC_MAXDEG; ++k) op->group_n[k] = k == p ? saved[k] : 0;
+      float best = 3.4e38f;
+      int bw = 4;
+      for (int c = 0; c < 3 && st == OC_OK; ++c) {
+        op->wpb[p] = cand[c];
+        float t = 0.f;
+        st = time_stage(op, sc, tz, tq, reps, &t);
+        if (st == OC_OK && t < best) { best = t; bw = cand[c]; }
+      }
+      op->wpb[p] = bw;
+      per_group += best;
+    }
+    for (int p = 0; p <= OC_MAXDEG; ++p) op->group_n[p] = saved[p];
+  }
+  op->tune_ms[0] = per_group;
+  float one = 3.4e38f;
+  if (st == OC_OK && op->launch_mode != OC_LAUNCH_PER_GROUP && n_groups(op) > 1) {
+    op->use_hp = 1;
+    int bw = 4;
+    for (int c = 1; c < 3 && st == OC_OK; ++c) {
+      op->hp_wpb = cand[c];
+      float t = 0.f;
+      st = time_stage(op, sc, tz, tq, reps, &t);
+      if (st == OC_OK && t < one) { one = t; bw = cand[c]; }
+    }
+    op->hp_wpb = bw;
+    op->tune_ms[1] = one;
+  }
+  op->use_hp = op->launch_mode == OC_LAUNCH_ONE ? (n_groups(op) > 1)
+               : op->launch_mode == OC_LAUNCH_PER_GROUP ? 0
+               : (n_groups(op) > 1 && one < per_group);
+  op->launches = launches;
+  cudaStreamSynchronize(op->stream);
+  cudaFree(tz);
+  cudaFree(tq);
+  if (st != OC_OK) return st;
+  op->tuned = 1;
+  return read_error(op);
 }
 
 extern "C" oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time, double dt,
@@ -768,6 +966,10 @@ extern "C" oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time
   }
   OC_TRY(cudaMemcpyAsync(op->d_dyn, op->h_dyn, sizeof(StageDyn) * sc.s, cudaMemcpyHostToDevice,
                          op->stream));
+  if (!op->tuned) {
+    st = autotune(op, sc, dz, dq);
+    if (st != OC_OK) return st;
+  }
   if (!op->graph || op->graph_scheme != scheme || op->graph_z != dz || op->graph_q != dq) {
     if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
     cudaGraph_t g;
@@ -775,6 +977,7 @@ extern "C" oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time
     const int64_t before = op->launches;
     st = enqueue_step(op, sc, dz, dq);
     cudaError_t ce = cudaStreamEndCapture(op->stream, &g);
+    op->graph_launches = op->launches - before;
     op->launches = before;
     if (st != OC_OK) return st;
     if (ce != cudaSuccess) return fail(op, OC_ERR_CUDA, cudaGetErrorString(ce));
@@ -783,7 +986,7 @@ extern "C" oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time
     op->graph_scheme = scheme; op->graph_z = dz; op->graph_q = dq;
   }
   OC_TRY(cudaGraphLaunch(op->graph, op->stream));
-  for (int p = 1; p <= OC_MAXDEG; ++p) op->launches += op->group_n[p] ? sc.s : 0;
+  op->launches += op->graph_launches;
   if (memory == OC_MEM_HOST) {
     OC_TRY(cudaMemcpyAsync(z, op->ts_z, nz * 8, cudaMemcpyDeviceToHost, op->stream));
     OC_TRY(cudaMemcpyAsync(q, op->ts_q, nq * 8, cudaMemcpyDeviceToHost, op->stream));

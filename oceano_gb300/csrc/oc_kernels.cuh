@@ -216,11 +216,16 @@ struct Dims {
     return (((SZR + 31) / 32) * 32 + (sizeof(R) == 4 ? pad_f : pad_d)) * (int)sizeof(R);
   }
   static constexpr int bytes_d() { return (((SZD + 31) / 32) * 32 + pad_d) * 8; }
+  static_assert(SZD <= OC_DSTRIDE, "FP64 zeta work area exceeds its global stride");
+  // the FP64 team region lives in shared memory in the FP64 form only; the mixed
+  // form (FP32 compute type) keeps it in the per-cell global work area
+  template <typename R>
+  static constexpr int bytes_d_smem() { return sizeof(R) == 4 ? 0 : bytes_d(); }
   // per warp: CPW compute regions, CPW FP64 regions, CPW batch-norm slots, int area
   template <typename R>
   static constexpr int d_offset() { return ((CPW * bytes_r<R>() + 15) / 16) * 16; }
   template <typename R>
-  static constexpr int norm_offset() { return d_offset<R>() + CPW * bytes_d(); }
+  static constexpr int norm_offset() { return d_offset<R>() + CPW * bytes_d_smem<R>(); }
   template <typename R>
   static constexpr int int_offset() { return norm_offset<R>() + CPW * 8; }
   static constexpr int INTS = 2 + 16 + 8 + 1;  // cell, offset, 8 slot records, 8 sdo, flag
@@ -485,12 +490,21 @@ struct FaceRec {
 // stores).  Global accesses of the prologue/epilogue are lane-contiguous over
 // the warp's cells.
 // ---------------------------------------------------------------------------
+// resident 4-warp blocks per SM the mixed kernels are compiled for (register cap)
+#ifndef OC_MIXED_MIN_BLOCKS
+#define OC_MIXED_MIN_BLOCKS 5
+#endif
+// One block of the stage: `blk` is the block index within the degree group of
+// n_group cells (listed by group_cells, or group_first + i when NULL); the FP64
+// work-area slots of the mixed form are indexed by the launch-wide block index.
 template <int P, typename R, typename KT, bool MIX, typename RIN>
-__global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
+__device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *smem_raw,
+                                           const int blk, const int n_group,
+                                           const int *group_cells, const int group_first) {
   using D = Dims<P>;
   constexpr int N = D::N, Q = D::Q, G = D::G, T = D::T, NN = D::NN, NT = D::NT;
   constexpr int CPWMAX = D::CPW;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  static_assert(CPWMAX <= OC_MAXCPW, "cells per warp above the work-area slot stride");
   const DegTables<R> &tb = tab<R>(P);
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -500,8 +514,8 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
   const int W = a.batch;
   const int cpw = (CPWMAX / W) * W;
   const int wpb = blockDim.x >> 5;
-  const int gi0 = (blockIdx.x * wpb + warp) * cpw;
-  const int nvalid = max(0, min(cpw, a.n_group - gi0));  // cells of this warp
+  const int gi0 = (blk * wpb + warp) * cpw;
+  const int nvalid = max(0, min(cpw, n_group - gi0));  // cells of this warp
   const bool valid = member && team < nvalid;
   const int s = a.stage;
   const StageDyn dy = *a.dyn;
@@ -527,16 +541,18 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
   R *ZN = BZ + NN;            // NN mixed form: zeta^n - zeta_ref
   R *X = ZN + NN;             // scratch tiles / neighbour traces
   R *FV = X + D::XS;          // 3*FVS face point values
-  double *dm = reinterpret_cast<double *>(wbase + D::template d_offset<R>() + team * D::bytes_d());
-  double *DZ = dm;            // NN FP64 iterate
-  double *DX = DZ + NN;       // 3 tiles N*T
-  double *DRED = DX + 3 * NT; // T+1
+  auto Dreg = [&](int j) {  // FP64 team region of team j: shared (FP64 form) or global slot
+    if constexpr (MIX)
+      return a.dscratch + ((int64_t)(blockIdx.x * wpb + warp) * OC_MAXCPW + j) * OC_DSTRIDE;
+    else
+      return reinterpret_cast<double *>(wbase + D::template d_offset<R>() + j * D::bytes_d());
+  };
 
   // ---- 0. prologue: cells, stage input, face records, partial rhs ------------
   if (lane < CPWMAX) {
     const int j = lane;
     const int gi = nvalid > 0 ? gi0 + (j < nvalid ? j : 0) : 0;  // idle warps read cell 0
-    const int c = a.group_cells ? a.group_cells[gi] : a.group_first + gi;
+    const int c = group_cells ? group_cells[gi] : group_first + gi;
     w_cell[j] = c;
     w_off[j] = a.off[c];
     w_flag[j] = 0;
@@ -544,6 +560,9 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
   __syncwarp();
   const int cell = w_cell[team];
   const int64_t zo = w_off[team], qo = 2 * zo;
+  double *DZ = Dreg(team);        // NN FP64 iterate
+  double *DX = DZ + NN;           // 3 tiles N*T
+  double *DRED = DX + 3 * NT;     // T+1
   for (int e = lane; e < nvalid * 16; e += 32) {  // face records (invalid teams: empty)
     const int j = e >> 4, k = e & 15;
     w_rec[j * 16 + k] = a.cfrec[16 * (int64_t)w_cell[j] + k];
@@ -1329,8 +1348,7 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
         const int j = e / NN, d = e - j * NN;
         if (!w_flag[j]) continue;
         const int64_t gz = w_off[j] + d;
-        const double *DZj = reinterpret_cast<const double *>(
-            wbase + D::template d_offset<R>() + j * D::bytes_d());
+        const double *DZj = Dreg(j);
         if (a.out_z) a.out_z[gz] = DZj[d];
         if (a.out_rz) a.out_rz[gz] = (float)(DZj[d] - zref);
       }
@@ -1344,8 +1362,7 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
       kz_out[gz] = (KT)Rj[3 * NN + d];
       double zn;
       if (w_flag[j]) {
-        const double *DZj = reinterpret_cast<const double *>(
-            wbase + D::template d_offset<R>() + j * D::bytes_d());
+        const double *DZj = Dreg(j);
         zn = DZj[d];
       } else {
         zn = a.un_z[gz] + (double)Rj[8 * NN + d];
@@ -1407,6 +1424,36 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs a) {
     if (a.out_q) a.out_q[gq] = nxt;
     if (MIX && a.out_rq) a.out_rq[gq] = (float)nxt;
   }
+}
+
+// One degree group per launch.
+template <int P, typename R, typename KT, bool MIX, typename RIN>
+__global__ void __launch_bounds__(128, MIX ? OC_MIXED_MIN_BLOCKS : 1) stage_kernel(const StageArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  stage_body<P, R, KT, MIX, RIN>(a, smem_raw, blockIdx.x, a.n_group, a.group_cells, a.group_first);
+}
+
+// Every degree group of an hp mesh in one launch: the grid is the concatenation
+// of the groups' block ranges, most expensive degree first (a.hp_first_block[p],
+// a.hp_blocks[p]); each block runs the body of its degree.
+#ifndef OC_HP_MIN_BLOCKS
+#define OC_HP_MIN_BLOCKS 4
+#endif
+template <typename R, typename KT, bool MIX, typename RIN>
+__global__ void __launch_bounds__(128, MIX ? OC_HP_MIN_BLOCKS : 1) stage_kernel_hp(const StageArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int b = blockIdx.x;
+#define OC_HP_CASE(P)                                                                          \
+  if (b >= a.hp_first_block[P] && b < a.hp_first_block[P] + a.hp_blocks[P]) {                 \
+    stage_body<P, R, KT, MIX, RIN>(a, smem_raw, b - a.hp_first_block[P], a.hp_n[P],           \
+                                   a.hp_cells[P], 0);                                          \
+    return;                                                                                    \
+  }
+  OC_HP_CASE(4)
+  OC_HP_CASE(3)
+  OC_HP_CASE(2)
+  OC_HP_CASE(1)
+#undef OC_HP_CASE
 }
 
 }  // namespace oc

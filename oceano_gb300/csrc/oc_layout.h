@@ -9,6 +9,8 @@
 #define OC_MAXBID 16   // boundary ids
 #define OC_MAXSTAGES 4
 #define OC_MAXDEG 4
+#define OC_MAXCPW 10    // cells per warp at p = 1 (the most of any degree)
+#define OC_DSTRIDE 144  // doubles per cell of the FP64 zeta work area, >= N^2 + 3 N T + T + 2
 
 // Per-degree tables; matrices are [point][node] on [0,1].
 template <typename R>
@@ -76,7 +78,15 @@ struct StageArgs {
   float *out_unzf, *out_unqf;
   int fast_mixed;
   const float *geof;           // [n_cells*11] FP32 copy of geo (mixed form)
-  double *aux_q;               // ARK last stage: next_ri_discharge receives M^-1 rhs
+  // mixed form: FP64 work area of the literal zeta iteration, OC_DSTRIDE doubles
+  // per (launch-wide warp, team) slot, OC_MAXCPW slots per warp (only cells that
+  // are not fully wet touch it)
+  double *dscratch;
+  // one-launch hp stage (stage_kernel_hp): per degree p the first block, the
+  // number of blocks, the cells and the cell list of the group
+  int hp_first_block[OC_MAXDEG + 1], hp_blocks[OC_MAXDEG + 1], hp_n[OC_MAXDEG + 1];
+  const int *hp_cells[OC_MAXDEG + 1];
+  double *aux_q;              // ARK last stage: next_ri_discharge receives M^-1 rhs
   const struct StageDyn *dyn;  // device copy of the per-call coefficients
   int stage, n_stages, ark, last, write_kq_last, apply_mode;
   // model

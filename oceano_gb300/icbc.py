@@ -76,13 +76,17 @@ def channel_problem_data(manning=0.03):
 def nodal_points(mesh: Mesh):
     """Physical coordinates of every DoF (Gauss-Lobatto nodes, lexicographic)."""
     from .basis import lobatto
-    pts = []
-    for c in range(mesh.n_cells):
-        p = int(mesh.degree[c])
-        xn, _ = lobatto(p + 1)
-        v = mesh.vertices[c]
+    off = mesh.offsets()
+    out = np.zeros((int(off[-1]), 2))
+    for p in np.unique(mesh.degree):
+        cells = np.nonzero(mesh.degree == p)[0]
+        xn, _ = lobatto(int(p) + 1)
         ex, ey = np.meshgrid(xn, xn)  # ey varies along rows (iy), ex along columns (ix)
-        X = v[0] + (v[2] - v[0]) * ex + (v[4] - v[0]) * ey
-        Y = v[1] + (v[3] - v[1]) * ex + (v[5] - v[1]) * ey
-        pts.append(np.stack([X.ravel(), Y.ravel()], 1))
-    return np.concatenate(pts)
+        ex, ey = ex.ravel()[None, :], ey.ravel()[None, :]
+        v = mesh.vertices[cells]
+        X = v[:, 0:1] + (v[:, 2:3] - v[:, 0:1]) * ex + (v[:, 4:5] - v[:, 0:1]) * ey
+        Y = v[:, 1:2] + (v[:, 3:4] - v[:, 1:2]) * ex + (v[:, 5:6] - v[:, 1:2]) * ey
+        idx = off[cells][:, None] + np.arange(ex.shape[1])[None, :]
+        out[idx, 0] = X
+        out[idx, 1] = Y
+    return out

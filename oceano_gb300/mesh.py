@@ -269,3 +269,67 @@ def vortex_mesh(refine: int, degree: int) -> Mesh:
 def channel_mesh(degree: int = 2, nx: int = 250, ny: int = 10, length=25.0) -> Mesh:
     """[0,length]x[0,1] channel: inflow id 1 (left), outflow id 2 (right), walls 0."""
     return uniform_mesh(nx, ny, (0.0, length, 0.0, 1.0), periodic_x=False, degree=degree)
+
+
+def concatenate_meshes(meshes) -> Mesh:
+    """Disjoint union of meshes (an ensemble run as one operator): cells in
+    order, then every mesh's inner faces, then every mesh's boundary faces
+    (the operator's inner-first face convention)."""
+    off = np.cumsum([0] + [m.n_cells for m in meshes])
+    inner_m, inner_p, fm, fp, sub, ori = [], [], [], [], [], []
+    bnd_m, bnd_f, bid = [], [], []
+    for k, m in enumerate(meshes):
+        ni = m.n_inner
+        inner_m.append(m.cell_m[:ni] + off[k]); inner_p.append(m.cell_p + off[k])
+        fm.append(m.face_m[:ni]); fp.append(m.face_p); sub.append(m.subface); ori.append(m.orient)
+        bnd_m.append(m.cell_m[ni:] + off[k]); bnd_f.append(m.face_m[ni:]); bid.append(m.bid)
+    return Mesh(
+        degree=np.concatenate([m.degree for m in meshes]).astype(np.int32),
+        vertices=np.concatenate([m.vertices for m in meshes]),
+        cell_m=np.concatenate(inner_m + bnd_m).astype(np.int32),
+        cell_p=np.concatenate(inner_p).astype(np.int32),
+        face_m=np.concatenate(fm + bnd_f).astype(np.int8),
+        face_p=np.concatenate(fp).astype(np.int8),
+        subface=np.concatenate(sub).astype(np.int8),
+        orient=np.concatenate(ori).astype(np.int8),
+        bid=np.concatenate(bid).astype(np.int32),
+        level=np.concatenate([m.level for m in meshes]).astype(np.int32),
+        domain=meshes[0].domain,
+    )
+
+
+def disk_refined_mesh(center, scale, coarse=(20, 10), domain=(0.0, 2.0, 0.0, 1.0),
+                      global_refine=2, extra=3, periodic_x=True, radii=(2.0, 1.4, 1.0),
+                      degree_radius=None):
+    """Nested disks of refinement around `center` (AMR-like meshes of an
+    ensemble member): after `global_refine` levels, level k of `extra` splits
+    the leaves whose centre lies within radii[k] * scale of `center` (periodic
+    distance in x), then 2:1 balance.  Degree 2 inside `degree_radius`, 1
+    elsewhere (degree 1 everywhere when None)."""
+    x0, x1, y0, y1 = domain
+    f = QuadForest(coarse[0], coarse[1], domain, periodic_x)
+    f.refine_global(global_refine)
+    lx = x1 - x0
+    for k in range(extra):
+        l = global_refine + k
+        r = radii[k] * scale
+        hx, hy = lx / (coarse[0] << l), (y1 - y0) / (coarse[1] << l)
+        for leaf in [lf for lf in f.leaves if lf[0] == l]:
+            _, i, j = leaf
+            dx = x0 + (i + 0.5) * hx - center[0]
+            if periodic_x:
+                dx -= lx * np.round(dx / lx)
+            dy = y0 + (j + 0.5) * hy - center[1]
+            if dx * dx + dy * dy < r * r:
+                f.refine(leaf)
+    f.balance()
+    mesh = f.build(1)
+    if degree_radius is not None:
+        v = mesh.vertices
+        cx = 0.5 * (v[:, 0] + v[:, 6]) - center[0]
+        if periodic_x:
+            cx -= lx * np.round(cx / lx)
+        cy = 0.5 * (v[:, 1] + v[:, 7]) - center[1]
+        deg = np.where(cx * cx + cy * cy < degree_radius ** 2, 2, 1).astype(np.int32)
+        mesh = mesh.with_degree(deg)
+    return mesh

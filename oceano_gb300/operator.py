@@ -203,6 +203,18 @@ class OceanoOperator:
         mem = _memory(height, discharge)
         check(lib().oc_project_vortex(self.h, time, _ptr(height), _ptr(discharge), mem), self.h)
 
+    # ---- launch configuration (GB300-specific; no reference counterpart) -------------
+    def set_launch_mode(self, mode: str):
+        """"auto" (tuned at the first time step), "per_group" or "one" (hp meshes)."""
+        check(lib().oc_set_launch_mode(self.h, _lib.LAUNCH_MODE[mode]), self.h)
+
+    @property
+    def launch_config(self) -> dict:
+        out = np.zeros(7, np.int32)
+        check(lib().oc_launch_config(self.h, _ptr(out)), self.h)
+        return {"one_launch": bool(out[0]), "one_launch_warps": int(out[1]),
+                "group_warps": {p: int(out[1 + p]) for p in range(1, 5)}, "tuned": bool(out[6])}
+
     def synchronize(self):
         check(lib().oc_synchronize(self.h), self.h)
 

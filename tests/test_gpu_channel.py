@@ -1,0 +1,80 @@
+"""IMEX channel over a bump with implicit Manning friction (250x10 cells, p = 2),
+and the lake at rest on the same bathymetry.
+
+* Lake at rest (walls everywhere, zeta = 0, q = 0): the state stays exactly at
+  rest in both forms (well-balanced hydrostatic reconstruction).
+* Channel (discharge 4.42 in, zeta = 0 out): the first ARK steps match the
+  FP64 oracle to 1e-12; the FP64 form reaches the steady state with
+  ||(U^{n+1} - U^n)/dt||_rms < 1e-10; the mixed form settles at its FP32
+  evaluation floor (bound written below) on the same steady state.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+GIR, TRB = O.TABLEAUX["giraldo32"], O.TABLEAUX["trbdf2"]
+CFL = 0.075
+
+
+def device_run(op, z0, q0, dt, steps, every):
+    """ARK steps on device vectors; returns the rms residual every `every` steps."""
+    import torch
+    st = torch.cuda.ExternalStream(op.stream)
+    z = torch.from_numpy(z0).cuda()
+    q = torch.from_numpy(q0).cuda()
+    res = []
+    torch.cuda.synchronize()
+    with torch.cuda.stream(st):
+        for it in range(steps):
+            chk = (it + 1) % every == 0
+            if chk:
+                zp, qp = z.clone(), q.clone()
+            op.perform_time_step("ark_stage3_order2", it * dt, dt, z, q)
+            if chk:
+                d = (torch.sum((z - zp) ** 2) + torch.sum((q - qp) ** 2)) / (3 * op.n_dofs)
+                res.append(float(torch.sqrt(d)) / dt)
+    torch.cuda.synchronize()
+    return z.cpu().numpy(), q.cpu().numpy(), res
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_lake_at_rest_stays_at_rest(gpu_lib, precision):
+    from oceano_gb300 import workloads as W
+    op, z0, q0 = W.channel(precision, lake=True)
+    z, q, res = device_run(op, z0, q0, 1e-3, 2000, 500)
+    assert np.abs(z).max() == 0.0 and np.abs(q).max() == 0.0
+    assert max(res) == 0.0
+
+
+def test_channel_first_steps_match_oracle(gpu_lib):
+    from cases import static_arrays
+    from oceano_gb300 import workloads as W
+    from oceano_gb300.icbc import channel_problem_data
+    op, z0, q0 = W.channel("fp64")
+    orc = O.Oracle(op.mesh, friction=2, bcs=W.CHANNEL_BCS)
+    orc.set_static(*static_arrays(orc, channel_problem_data(W.CHANNEL_MANNING)))
+    dt = CFL / orc.transport_speed(z0, q0)
+    zo, qo, zg, qg = z0.copy(), q0.copy(), z0.copy(), q0.copy()
+    for it in range(5):
+        O.ark_step(orc, GIR["a"], GIR["b"], GIR["c"], TRB["a"], TRB["d"], it * dt, dt, zo, qo)
+        op.perform_time_step("ark_stage3_order2", it * dt, dt, zg, qg)
+    assert np.linalg.norm(zg - zo) <= 1e-12 * np.linalg.norm(zo)
+    assert np.linalg.norm(qg - qo) <= 1e-12 * np.linalg.norm(qo)
+
+
+def test_channel_steady_state(gpu_lib):
+    """FP64: residual below 1e-10 within 260k steps (about 290 s of flow);
+    mixed: same flow, residual floor below 5e-4 (FP32 evaluation of fluxes of
+    magnitude ~20 per cell), steady states within 1e-5 of each other."""
+    from oceano_gb300 import workloads as W
+    op, z0, q0 = W.channel("fp64")
+    dt = CFL / op.compute_cell_transport_speed(z0, q0)
+    z64, q64, res64 = device_run(op, z0, q0, dt, 260000, 20000)
+    assert res64[-1] < 1e-10, res64
+    opm, _, _ = W.channel("mixed")
+    zm, qm, resm = device_run(opm, z0, q0, dt, 160000, 20000)
+    assert resm[-1] < 5e-4, resm
+    assert np.abs(zm - z64).max() < 1e-5 and np.abs(qm - q64).max() < 1e-5 * 4.42
