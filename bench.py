@@ -42,6 +42,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 DEGREE, REFINE, CFL = 3, 4, 0.075  # CFL of the reference's degree-3 case (channelFlow.prm)
+CFL_HP = 0.05  # random hp mesh (degrees up to 4)
 METRIC = "DG DoF-stage updates/s, mixed vs FP64 on same GPU at stated L2 error; % HBM roofline"
 
 
@@ -93,7 +94,10 @@ class Workload:
             raise ValueError(name)
         self.mesh = self.op_d.mesh
         self.n = self.op_d.n_dofs
-        self.dt = CFL / self.op_d.compute_cell_transport_speed(self.z0, self.q0)
+        # degree-4 cells at the finest level of the hp mesh need a smaller Courant
+        # number (CFL 0.075 diverges there within 20 steps, in the oracle as well)
+        self.cfl = CFL_HP if name == "hp" else CFL
+        self.dt = self.cfl / self.op_d.compute_cell_transport_speed(self.z0, self.q0)
 
     def oracle(self):
         from oracle import oracle as O

@@ -244,6 +244,53 @@ oc_status oc_set_launch_mode(oc_op *op, int32_t mode);
  * out[2..5] warps per block of the degree 1..4 groups, out[6] tuned (0/1) */
 oc_status oc_launch_config(const oc_op *op, int32_t *out);
 
+/* ---- learned refinement indicator (no reference counterpart) -------------------
+ * The reference refines where the vorticity indicator (hpTuner.h:247-305) exceeds
+ * a fraction of its maximum (main.cc:749-765).  The functions below compute
+ * per-cell features of the state on the GPU and train / evaluate a small BF16
+ * multilayer perceptron that predicts those flags some steps ahead.
+ *
+ * oc_indicator_features: per cell c, from (zeta, q) and
+ *   cell_info[6c + 0..3] = neighbour cell across faces 0..3 (-1 on the boundary;
+ *                          on a coarse face with two fine neighbours, either),
+ *   cell_info[6c + 4]    = refinement level, cell_info[6c + 5] = member index
+ *                          (< n_members; the vorticity maximum is taken per member),
+ * writes features[12c + 0..11] = cell means of zeta, hu, hv; vorticity w/max;
+ *   d/dx, d/dy of w/max from the face neighbours; the four neighbours' w/max;
+ *   level; degree.  The vorticity is the reference indicator (max over QGauss(p_max)
+ *   points of |dv/dx - du/dy|).  flags (may be NULL): 1 where w/max > threshold.
+ *   vorticity (may be NULL): w/max per cell. */
+oc_status oc_indicator_features(oc_op *op, const double *zeta, const double *q,
+                                const int32_t *cell_info, int32_t n_members, float threshold,
+                                float *features, float *flags, float *vorticity, int32_t memory);
+
+#define OC_MLP_FEATURES 12
+#define OC_MLP_HIDDEN 64
+#define OC_MLP_PARAMS (64 * 12 + 64 + 64 * 64 + 64 + 64 + 1)
+typedef struct oc_mlp oc_mlp;
+/* seeded He-uniform initialisation; all array arguments of the oc_mlp_* calls
+ * below are device pointers unless named host */
+oc_status oc_mlp_create(uint64_t seed, oc_mlp **out);
+void oc_mlp_destroy(oc_mlp *m);
+const char *oc_mlp_last_error(const oc_mlp *m);
+void *oc_mlp_stream(oc_mlp *m);
+oc_status oc_mlp_synchronize(oc_mlp *m);
+/* FP32 master parameters, host arrays of OC_MLP_PARAMS floats */
+oc_status oc_mlp_get_params(oc_mlp *m, float *host_params);
+oc_status oc_mlp_set_params(oc_mlp *m, const float *host_params);
+/* input normalisation (mean[12], 1/std[12]), host arrays; fit from n feature rows */
+oc_status oc_mlp_get_normalization(oc_mlp *m, float *host_mean_inv_std);
+oc_status oc_mlp_set_normalization(oc_mlp *m, const float *host_mean_inv_std);
+oc_status oc_mlp_fit_normalization(oc_mlp *m, const float *features, int64_t n);
+/* logits of n feature rows */
+oc_status oc_mlp_forward(oc_mlp *m, const float *features, int64_t n, float *logits);
+/* mean weighted BCE-with-logits loss (host) and its gradient, kept in the handle
+ * and copied to host_grad when not NULL */
+oc_status oc_mlp_gradient(oc_mlp *m, const float *features, const float *labels, int64_t n,
+                          float pos_weight, float *host_grad, double *host_loss);
+/* one Adam step (beta 0.9, 0.999, eps 1e-8) with the handle's gradient */
+oc_status oc_mlp_adam_step(oc_mlp *m, float lr);
+
 /* device synchronisation and the stream the handle launches on */
 oc_status oc_synchronize(oc_op *op);
 void *oc_stream(oc_op *op);

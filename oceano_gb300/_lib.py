@@ -71,6 +71,23 @@ EXPORTS = {
                                          C.c_int32]),
     "oc_project_vortex": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_int32]),
     "oc_transport_speed_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "oc_indicator_features": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_int32, C.c_float, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_int32]),
+    "oc_mlp_create": (C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
+    "oc_mlp_destroy": (None, [C.c_void_p]),
+    "oc_mlp_last_error": (C.c_char_p, [C.c_void_p]),
+    "oc_mlp_stream": (C.c_void_p, [C.c_void_p]),
+    "oc_mlp_synchronize": (C.c_int, [C.c_void_p]),
+    "oc_mlp_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "oc_mlp_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "oc_mlp_get_normalization": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "oc_mlp_set_normalization": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "oc_mlp_fit_normalization": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "oc_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "oc_mlp_gradient": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float,
+                                  C.c_void_p, C.POINTER(C.c_double)]),
+    "oc_mlp_adam_step": (C.c_int, [C.c_void_p, C.c_float]),
     "oc_set_launch_mode": (C.c_int, [C.c_void_p, C.c_int32]),
     "oc_launch_config": (C.c_int, [C.c_void_p, C.c_void_p]),
     "oc_synchronize": (C.c_int, [C.c_void_p]),

@@ -43,6 +43,7 @@ def _sources():
     units.append((os.path.join(CSRC, "oc_aux.cu"), "oc_aux.o", []))
     units.append((os.path.join(CSRC, "oc_api.cu"), "oc_api.o", []))
     units.append((os.path.join(CSRC, "oc_noalloc.cu"), "oc_noalloc.o", []))
+    units.append((os.path.join(CSRC, "oc_mlp.cu"), "oc_mlp.o", []))
     return units
 
 

@@ -49,6 +49,9 @@ cudaError_t launch_velocity_field(const AuxArgs &, const double *, const double 
 cudaError_t launch_vorticity(const AuxArgs &, const double *, int, const double *,
                              const double *, float *, cudaStream_t);
 cudaError_t launch_project_vortex(const AuxArgs &, double, double *, double *, cudaStream_t);
+cudaError_t launch_features(const AuxArgs &, const double *, const double *, const float *,
+                            const int *, int, unsigned *, float, float *, float *, float *,
+                            cudaStream_t);
 }  // namespace oc
 
 using namespace oc;
@@ -146,6 +149,13 @@ struct oc_op {
   int hp_wpb = 4;                           // warps per block of that launch
   int wpb[OC_MAXDEG + 1] = {4, 4, 4, 4, 4}; // warps per block per degree group
   float tune_ms[2] = {0.f, 0.f};            // measured stage time: per-group, one launch
+  // vorticity: basis values / derivatives at QGauss(nq) per degree (cached per nq)
+  double *d_vtab[9] = {nullptr};
+  // indicator features: velocity and vorticity scratch, per-member maxima
+  double *d_ivel = nullptr;
+  float *d_ivort = nullptr;
+  unsigned *d_imax = nullptr;
+  int imax_n = 0;
   // graph cache of oc_perform_time_step
   int64_t graph_launches = 0;
   cudaGraphExec_t graph = nullptr;
@@ -1090,27 +1100,37 @@ extern "C" oc_status oc_velocity_field(oc_op *op, const double *z, const double 
   return read_error(op);
 }
 
+// basis values and derivatives at QGauss(nq1d) for every degree, built once per nq1d:
+// [B | D], each OC_MAXDEG * 8 * OC_MAXN doubles
+static oc_status vorticity_tables(oc_op *op, int nq1d, const double **dB, const double **dD) {
+  const size_t sz = OC_MAXDEG * 8 * OC_MAXN;
+  if (!op->d_vtab[nq1d]) {
+    std::vector<double> t(2 * sz, 0.0);
+    double xq[16], wq[16], xn[16], wn[16];
+    gauss_rule(nq1d, xq, wq);
+    for (int p = 1; p <= OC_MAXDEG; ++p) {
+      lobatto_rule(p + 1, xn, wn);
+      for (int k = 0; k < nq1d; ++k)
+        for (int i = 0; i <= p; ++i) {
+          t[((p - 1) * 8 + k) * OC_MAXN + i] = lag(p + 1, xn, i, xq[k]);
+          t[sz + ((p - 1) * 8 + k) * OC_MAXN + i] = lag_d(p + 1, xn, i, xq[k]);
+        }
+    }
+    OC_TRY(alloc(op, (void **)&op->d_vtab[nq1d], 2 * sz * 8));
+    OC_TRY(cudaMemcpy(op->d_vtab[nq1d], t.data(), 2 * sz * 8, cudaMemcpyHostToDevice));
+  }
+  *dB = op->d_vtab[nq1d];
+  *dD = op->d_vtab[nq1d] + sz;
+  return OC_OK;
+}
+
 extern "C" oc_status oc_vorticity_indicator(oc_op *op, const double *u, int32_t nq1d,
                                             float *ind, int32_t memory) {
   if (!op || !u || !ind || nq1d < 1 || nq1d > 8) return OC_ERR_INVALID_ARG;
   const size_t nq = 2 * op->n_dofs;
-  // basis values/derivatives at QGauss(nq1d) for every degree
-  std::vector<double> B(OC_MAXDEG * 8 * OC_MAXN, 0.0), Dm(OC_MAXDEG * 8 * OC_MAXN, 0.0);
-  double xq[16], wq[16], xn[16], wn[16];
-  gauss_rule(nq1d, xq, wq);
-  for (int p = 1; p <= OC_MAXDEG; ++p) {
-    lobatto_rule(p + 1, xn, wn);
-    for (int k = 0; k < nq1d; ++k)
-      for (int i = 0; i <= p; ++i) {
-        B[((p - 1) * 8 + k) * OC_MAXN + i] = lag(p + 1, xn, i, xq[k]);
-        Dm[((p - 1) * 8 + k) * OC_MAXN + i] = lag_d(p + 1, xn, i, xq[k]);
-      }
-  }
-  double *dB = nullptr, *dD = nullptr;
-  OC_TRY(cudaMalloc((void **)&dB, B.size() * 8));
-  OC_TRY(cudaMalloc((void **)&dD, Dm.size() * 8));
-  OC_TRY(cudaMemcpyAsync(dB, B.data(), B.size() * 8, cudaMemcpyHostToDevice, op->stream));
-  OC_TRY(cudaMemcpyAsync(dD, Dm.data(), Dm.size() * 8, cudaMemcpyHostToDevice, op->stream));
+  const double *dB = nullptr, *dD = nullptr;
+  oc_status vs = vorticity_tables(op, nq1d, &dB, &dD);
+  if (vs != OC_OK) return vs;
   const double *du = u;
   float *dind = ind;
   float *tmp = nullptr;
@@ -1126,8 +1146,59 @@ extern "C" oc_status oc_vorticity_indicator(oc_op *op, const double *u, int32_t 
   if (memory == OC_MEM_HOST)
     OC_TRY(cudaMemcpyAsync(ind, tmp, op->n_cells * sizeof(float), cudaMemcpyDeviceToHost, op->stream));
   oc_status st = read_error(op);
-  cudaFree(dB); cudaFree(dD);
   if (tmp) cudaFree(tmp);
+  return st;
+}
+
+extern "C" oc_status oc_indicator_features(oc_op *op, const double *z, const double *q,
+                                           const int32_t *info, int32_t n_members, float thr,
+                                           float *feat, float *flags, float *vort,
+                                           int32_t memory) {
+  if (!op || !z || !q || !info || !feat || n_members < 1) return OC_ERR_INVALID_ARG;
+  const size_t nz = op->n_dofs, nq = 2 * nz, nc = op->n_cells;
+  int pmax = 1;
+  for (int p = 1; p <= OC_MAXDEG; ++p)
+    if (op->group_n[p]) pmax = p;
+  const double *dB = nullptr, *dD = nullptr;
+  oc_status vs = vorticity_tables(op, pmax, &dB, &dD);  // QGauss(max degree), hpTuner.h:261
+  if (vs != OC_OK) return vs;
+  if (ensure(op, &op->d_ivel, nq)) return OC_ERR_CUDA;
+  if (!op->d_ivort) OC_TRY(alloc(op, (void **)&op->d_ivort, nc * sizeof(float)));
+  if (op->imax_n < n_members) {
+    OC_TRY(alloc(op, (void **)&op->d_imax, n_members * sizeof(unsigned)));
+    op->imax_n = n_members;
+  }
+  const double *dz = z, *dq = q;
+  const int *dinfo = info;
+  float *dfeat = feat, *dflags = flags, *dvort = vort;
+  std::vector<void *> tmp;
+  if (memory == OC_MEM_HOST) {
+    void *p[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    const size_t sz[6] = {nz * 8, nq * 8, nc * 6 * 4, nc * 12 * 4, nc * 4, nc * 4};
+    for (int k = 0; k < 6; ++k) {
+      if ((k == 4 && !flags) || (k == 5 && !vort)) continue;
+      OC_TRY(cudaMalloc(&p[k], sz[k]));
+      tmp.push_back(p[k]);
+    }
+    OC_TRY(cudaMemcpyAsync(p[0], z, sz[0], cudaMemcpyHostToDevice, op->stream));
+    OC_TRY(cudaMemcpyAsync(p[1], q, sz[1], cudaMemcpyHostToDevice, op->stream));
+    OC_TRY(cudaMemcpyAsync(p[2], info, sz[2], cudaMemcpyHostToDevice, op->stream));
+    dz = (double *)p[0]; dq = (double *)p[1]; dinfo = (int *)p[2];
+    dfeat = (float *)p[3]; dflags = (float *)p[4]; dvort = (float *)p[5];
+  }
+  const AuxArgs a = aux_args(op);
+  OC_TRY(launch_velocity_field(a, dz, dq, op->d_ivel, op->stream));
+  OC_TRY(launch_vorticity(a, op->d_ivel, pmax, dB, dD, op->d_ivort, op->stream));
+  OC_TRY(launch_features(a, dz, dq, op->d_ivort, dinfo, n_members, op->d_imax, thr, dfeat,
+                         dflags, dvort, op->stream));
+  op->launches += 4;
+  if (memory == OC_MEM_HOST) {
+    OC_TRY(cudaMemcpyAsync(feat, dfeat, nc * 12 * 4, cudaMemcpyDeviceToHost, op->stream));
+    if (flags) OC_TRY(cudaMemcpyAsync(flags, dflags, nc * 4, cudaMemcpyDeviceToHost, op->stream));
+    if (vort) OC_TRY(cudaMemcpyAsync(vort, dvort, nc * 4, cudaMemcpyDeviceToHost, op->stream));
+  }
+  oc_status st = read_error(op);
+  for (void *p : tmp) cudaFree(p);
   return st;
 }
 

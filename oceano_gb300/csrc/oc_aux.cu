@@ -213,6 +213,70 @@ cudaError_t launch_velocity_field(const AuxArgs &a, const double *z, const doubl
   return cudaGetLastError();
 }
 
+// Largest vorticity of each member (non-negative floats order like their bits).
+__global__ void member_max_kernel(int n, const float *w, const int *info, int n_members,
+                                  unsigned *vmax) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const int m = info[6 * (int64_t)c + 5];
+  if (m >= 0 && m < n_members) atomicMax(&vmax[m], __float_as_uint(fmaxf(w[c], 0.f)));
+}
+
+// Indicator features of one cell (see oc_indicator_features in oceano_gpu.h).
+__global__ void features_kernel(const AuxArgs a, const double *z, const double *q, const float *w,
+                                const int *info, int n_members, const unsigned *vmax, float thr,
+                                float *feat, float *flags, float *wn) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.n_cells) return;
+  const int p = a.deg[c], N = p + 1, n = N * N;
+  const DegTables<double> &tb = tab<double>(p);
+  // integral weights of the nodal basis on [0,1] (Gauss p+1 is exact for them)
+  double mw[OC_MAXN];
+  for (int i = 0; i < N; ++i) {
+    double s = 0;
+    for (int k = 0; k < N; ++k) s += tb.wM[k] * tb.BM[k][i];
+    mw[i] = s;
+  }
+  const int64_t zo = a.off[c];
+  double zm = 0, q0 = 0, q1 = 0;
+  for (int iy = 0; iy < N; ++iy)
+    for (int ix = 0; ix < N; ++ix) {
+      const double wt = mw[ix] * mw[iy];
+      zm += wt * z[zo + iy * N + ix];
+      q0 += wt * q[2 * zo + iy * N + ix];
+      q1 += wt * q[2 * zo + n + iy * N + ix];
+    }
+  const int *inf = info + 6 * (int64_t)c;
+  const int m = inf[5];
+  const float mx = (m >= 0 && m < n_members) ? __uint_as_float(vmax[m]) : 0.f;
+  const float inv = mx > 0.f ? 1.f / mx : 0.f;
+  const float w0 = w[c] * inv;
+  float nb[4];
+  for (int f = 0; f < 4; ++f) nb[f] = inf[f] >= 0 ? w[inf[f]] * inv : w0;
+  const double *J = a.geo + 11 * (int64_t)c;
+  const float hx = (float)sqrt(J[2] * J[2] + J[4] * J[4]);
+  const float hy = (float)sqrt(J[3] * J[3] + J[5] * J[5]);
+  float *o = feat + 12 * (int64_t)c;
+  o[0] = (float)zm; o[1] = (float)q0; o[2] = (float)q1; o[3] = w0;
+  o[4] = (nb[1] - nb[0]) / (2.f * hx);
+  o[5] = (nb[3] - nb[2]) / (2.f * hy);
+  o[6] = nb[0]; o[7] = nb[1]; o[8] = nb[2]; o[9] = nb[3];
+  o[10] = (float)inf[4]; o[11] = (float)p;
+  if (flags) flags[c] = w0 > thr ? 1.f : 0.f;
+  if (wn) wn[c] = w0;
+}
+
+cudaError_t launch_features(const AuxArgs &a, const double *z, const double *q, const float *w,
+                            const int *info, int n_members, unsigned *vmax, float thr,
+                            float *feat, float *flags, float *wn, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(vmax, 0, sizeof(unsigned) * n_members, st);
+  if (e != cudaSuccess) return e;
+  const int nb = (a.n_cells + 127) / 128;
+  member_max_kernel<<<nb, 128, 0, st>>>(a.n_cells, w, info, n_members, vmax);
+  features_kernel<<<nb, 128, 0, st>>>(a, z, q, w, info, n_members, vmax, thr, feat, flags, wn);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_vorticity(const AuxArgs &a, const double *u, int nq, const double *B,
                              const double *D, float *out, cudaStream_t st) {
   vorticity_kernel<<<(a.n_cells + 127) / 128, 128, 0, st>>>(a, u, nq, B, D, out);

@@ -1,0 +1,443 @@
+// Learned refinement indicator: a 12-64-64-1 multilayer perceptron with BF16
+// weights and activations (FP32 accumulation, FP32 master weights), evaluated
+// and trained on the GPU.  It predicts, from per-cell features of the state,
+// whether the vorticity indicator (hpTuner.h:247-305 with the relative
+// thresholds of main.cc:749-765) will flag the cell some steps ahead.
+//
+// Parameter vector (FP32, OC_MLP_PARAMS floats):
+//   W1 [64][12] | b1 [64] | W2 [64][64] | b2 [64] | w3 [64] | b3
+// Forward, per sample x (12 features):
+//   xh = bf16((x - mean) * inv_std)
+//   h1 = bf16(relu(b1 + W1 xh)),  h2 = bf16(relu(b2 + W2 h1)),  z = b3 + w3 . h2
+// with W1, W2, w3 rounded to BF16.  Loss: mean over samples of the weighted
+// binary cross-entropy with logits, weight pos_weight on positive labels.
+// The gradient treats the BF16 roundings as identities (straight-through).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "oceano_gpu.h"
+
+namespace {
+
+constexpr int NF = OC_MLP_FEATURES, NH = OC_MLP_HIDDEN, NP = OC_MLP_PARAMS;
+constexpr int OW1 = 0, OB1 = OW1 + NH * NF, OW2 = OB1 + NH, OB2 = OW2 + NH * NH, OW3 = OB2 + NH,
+              OB3 = OW3 + NH;
+static_assert(OB3 + 1 == NP, "parameter layout");
+
+constexpr int kThreads = 128;      // samples per tile = threads per block
+constexpr int kGradBlocks = 304;   // persistent gradient grid (2 per SM)
+
+__device__ __forceinline__ float bf(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+// Weights as FP32 values of their BF16 roundings, biases FP32, normalisation.
+struct SmemWeights {
+  float w1[NH * NF], b1[NH], w2[NH * NH], b2[NH], w3[NH], b3, mean[NF], istd[NF];
+};
+
+__device__ void load_weights(SmemWeights &s, const float *w, const float *norm) {
+  for (int i = threadIdx.x; i < NH * NF; i += blockDim.x) s.w1[i] = bf(w[OW1 + i]);
+  for (int i = threadIdx.x; i < NH * NH; i += blockDim.x) s.w2[i] = bf(w[OW2 + i]);
+  for (int i = threadIdx.x; i < NH; i += blockDim.x) {
+    s.b1[i] = w[OB1 + i];
+    s.b2[i] = w[OB2 + i];
+    s.w3[i] = bf(w[OW3 + i]);
+  }
+  for (int i = threadIdx.x; i < NF; i += blockDim.x) {
+    s.mean[i] = norm[i];
+    s.istd[i] = norm[NF + i];
+  }
+  if (threadIdx.x == 0) s.b3 = w[OB3];
+}
+
+// normalised, BF16-rounded input and first hidden layer of one sample
+__device__ __forceinline__ void layer1(const SmemWeights &s, const float *x, float *xh, float *h1) {
+#pragma unroll
+  for (int i = 0; i < NF; ++i) xh[i] = bf((x[i] - s.mean[i]) * s.istd[i]);
+#pragma unroll
+  for (int k = 0; k < NH; ++k) {
+    float a = s.b1[k];
+#pragma unroll
+    for (int i = 0; i < NF; ++i) a = fmaf(s.w1[k * NF + i], xh[i], a);
+    h1[k] = bf(fmaxf(a, 0.f));
+  }
+}
+
+__device__ __forceinline__ float layer2_row(const SmemWeights &s, const float *h1, int j) {
+  float a = s.b2[j];
+#pragma unroll
+  for (int k = 0; k < NH; ++k) a = fmaf(s.w2[j * NH + k], h1[k], a);
+  return bf(fmaxf(a, 0.f));
+}
+
+__global__ void __launch_bounds__(kThreads) mlp_forward_kernel(const float *w, const float *norm,
+                                                               const float *feat, int64_t n,
+                                                               float *logit) {
+  __shared__ SmemWeights s;
+  load_weights(s, w, norm);
+  __syncthreads();
+  // block-uniform tile loop; the barrier keeps the shared weight reads inside it
+  const int64_t tiles = (n + kThreads - 1) / kThreads;
+  for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int64_t c = tile * kThreads + threadIdx.x;
+    if (c < n) {
+      float x[NF], xh[NF], h1[NH];
+#pragma unroll
+      for (int i = 0; i < NF; ++i) x[i] = feat[c * NF + i];
+      layer1(s, x, xh, h1);
+      float z = s.b3;
+#pragma unroll 1
+      for (int j = 0; j < NH; ++j) z = fmaf(s.w3[j], layer2_row(s, h1, j), z);
+      logit[c] = z;
+    }
+    __syncthreads();
+  }
+}
+
+// Per-tile activations of the gradient kernel (one row per sample).
+struct SmemTile {
+  float xh[kThreads][NF + 1];
+  float h1[kThreads][NH + 1];
+  float h2[kThreads][NH + 1];
+  float d2[kThreads][NH + 1];  // dL/da2
+  float d1[kThreads][NH + 1];  // dL/da1
+  float dz[kThreads];
+};
+
+// Persistent gradient kernel: each block walks tiles of kThreads samples;
+// thread t owns parameter entries e = t + kThreads * r and accumulates their
+// sums over the tiles in registers; the block's partial gradient and loss go
+// to part[block][NP + 1] (summed in a fixed order by mlp_reduce_kernel).
+constexpr int kOwn = (NP + kThreads - 1) / kThreads;
+
+__global__ void __launch_bounds__(kThreads, 1) mlp_grad_kernel(const float *w, const float *norm,
+                                                                const float *feat,
+                                                                const float *label, int64_t n,
+                                                                float pos_weight, float inv_n,
+                                                                float *part) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SmemWeights &s = *reinterpret_cast<SmemWeights *>(smem_raw);
+  SmemTile &T = *reinterpret_cast<SmemTile *>(smem_raw + ((sizeof(SmemWeights) + 15) / 16) * 16);
+  load_weights(s, w, norm);
+  const int t = threadIdx.x;
+  float acc[kOwn];
+#pragma unroll
+  for (int r = 0; r < kOwn; ++r) acc[r] = 0.f;
+  double loss = 0.0;
+  __syncthreads();
+  const int64_t tiles = (n + kThreads - 1) / kThreads;
+  for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int64_t c = tile * kThreads + t;
+    const bool ok = c < n;
+    // forward, keeping the activations of the tile
+    {
+      float x[NF], xh[NF], h1[NH];
+#pragma unroll
+      for (int i = 0; i < NF; ++i) x[i] = ok ? feat[c * NF + i] : 0.f;
+      layer1(s, x, xh, h1);
+#pragma unroll
+      for (int i = 0; i < NF; ++i) T.xh[t][i] = xh[i];
+#pragma unroll
+      for (int k = 0; k < NH; ++k) T.h1[t][k] = h1[k];
+      float z = s.b3;
+#pragma unroll 1
+      for (int j = 0; j < NH; ++j) {
+        const float h2 = layer2_row(s, h1, j);
+        T.h2[t][j] = h2;
+        z = fmaf(s.w3[j], h2, z);
+      }
+      // weighted BCE with logits: wt * (softplus(z) - y z); dL/dz = wt (sigmoid(z) - y) / n
+      const float y = ok ? label[c] : 0.f;
+      const float wt = ok ? (y > 0.5f ? pos_weight : 1.f) : 0.f;
+      const float sp = fmaxf(z, 0.f) + log1pf(expf(-fabsf(z)));
+      loss += (double)(wt * (sp - y * z));
+      const float sg = 1.f / (1.f + expf(-z));
+      const float dz = wt * (sg - y) * inv_n;
+      T.dz[t] = dz;
+#pragma unroll 1
+      for (int j = 0; j < NH; ++j) T.d2[t][j] = T.h2[t][j] > 0.f ? dz * s.w3[j] : 0.f;
+#pragma unroll
+      for (int k = 0; k < NH; ++k) {  // dL/da1 = [h1 > 0] W2^T dL/da2
+        float a = 0.f;
+#pragma unroll 1
+        for (int j = 0; j < NH; ++j) a = fmaf(s.w2[j * NH + k], T.d2[t][j], a);
+        T.d1[t][k] = h1[k] > 0.f ? a : 0.f;
+      }
+    }
+    __syncthreads();
+    // parameter sums over the tile's samples
+    const int64_t left = n - tile * kThreads;
+    const int cnt = left < kThreads ? (int)left : kThreads;  // samples in the tile
+#pragma unroll
+    for (int r = 0; r < kOwn; ++r) {
+      const int e = t + kThreads * r;
+      if (e >= NP) break;
+      float v = 0.f;
+      if (e < OB1) {
+        const int k = e / NF, i = e - k * NF;
+        for (int q = 0; q < cnt; ++q) v = fmaf(T.d1[q][k], T.xh[q][i], v);
+      } else if (e < OW2) {
+        const int k = e - OB1;
+        for (int q = 0; q < cnt; ++q) v += T.d1[q][k];
+      } else if (e < OB2) {
+        const int j = (e - OW2) / NH, k = (e - OW2) - j * NH;
+        for (int q = 0; q < cnt; ++q) v = fmaf(T.d2[q][j], T.h1[q][k], v);
+      } else if (e < OW3) {
+        const int j = e - OB2;
+        for (int q = 0; q < cnt; ++q) v += T.d2[q][j];
+      } else if (e < OB3) {
+        const int j = e - OW3;
+        for (int q = 0; q < cnt; ++q) v = fmaf(T.dz[q], T.h2[q][j], v);
+      } else {
+        for (int q = 0; q < cnt; ++q) v += T.dz[q];
+      }
+      acc[r] += v;
+    }
+    __syncthreads();
+  }
+  float *out = part + (int64_t)blockIdx.x * (NP + 1);
+#pragma unroll
+  for (int r = 0; r < kOwn; ++r) {
+    const int e = t + kThreads * r;
+    if (e < NP) out[e] = acc[r];
+  }
+  // block loss: the samples' terms summed over the threads
+  __shared__ double red[kThreads];
+  red[t] = loss;
+  __syncthreads();
+  for (int h = kThreads / 2; h > 0; h >>= 1) {
+    if (t < h) red[t] += red[t + h];
+    __syncthreads();
+  }
+  if (t == 0) out[NP] = (float)red[0];
+}
+
+__global__ void mlp_reduce_kernel(const float *part, int nb, float *grad, double *loss) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e > NP) return;
+  double v = 0.0;
+  for (int b = 0; b < nb; ++b) v += part[(int64_t)b * (NP + 1) + e];
+  if (e < NP) grad[e] = (float)v;
+  else *loss = v;
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master weights.
+__global__ void mlp_adam_kernel(float *w, float *m, float *v, const float *g, float lr, float b1,
+                                float b2, float eps, float c1, float c2) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= NP) return;
+  const float gi = g[e];
+  const float mi = b1 * m[e] + (1.f - b1) * gi;
+  const float vi = b2 * v[e] + (1.f - b2) * gi * gi;
+  m[e] = mi;
+  v[e] = vi;
+  w[e] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// per-feature sum and sum of squares (normalisation statistics)
+__global__ void mlp_stats_kernel(const float *feat, int64_t n, double *stats) {
+  __shared__ double s[2 * NF];
+  if (threadIdx.x < 2 * NF) s[threadIdx.x] = 0.0;
+  __syncthreads();
+  double a[NF], b[NF];
+  for (int i = 0; i < NF; ++i) a[i] = b[i] = 0.0;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x)
+    for (int i = 0; i < NF; ++i) {
+      const double x = feat[c * NF + i];
+      a[i] += x;
+      b[i] += x * x;
+    }
+  for (int i = 0; i < NF; ++i) {
+    atomicAdd(&s[i], a[i]);
+    atomicAdd(&s[NF + i], b[i]);
+  }
+  __syncthreads();
+  if (threadIdx.x < 2 * NF) atomicAdd(&stats[threadIdx.x], s[threadIdx.x]);
+}
+
+}  // namespace
+
+struct oc_mlp {
+  cudaStream_t stream = nullptr;
+  float *d_w = nullptr, *d_m = nullptr, *d_v = nullptr, *d_g = nullptr, *d_part = nullptr,
+        *d_norm = nullptr;
+  double *d_loss = nullptr, *d_stats = nullptr;
+  int64_t steps = 0;
+  std::string err;
+};
+
+#define MLP_TRY(call)                                                         \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) {                                                  \
+      m->err = std::string(#call) + ": " + cudaGetErrorString(e_);            \
+      return OC_ERR_CUDA;                                                     \
+    }                                                                         \
+  } while (0)
+
+static size_t grad_smem() {
+  return ((sizeof(SmemWeights) + 15) / 16) * 16 + sizeof(SmemTile);
+}
+
+// splitmix64 (Steele, Lea, Flood 2014) for the seeded initialisation
+static uint64_t splitmix64(uint64_t &x) {
+  uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+extern "C" {
+
+oc_status oc_mlp_create(uint64_t seed, oc_mlp **out) {
+  if (!out) return OC_ERR_INVALID_ARG;
+  oc_mlp *m = new oc_mlp();
+  *out = m;
+  MLP_TRY(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+  MLP_TRY(cudaMalloc((void **)&m->d_w, NP * 4));
+  MLP_TRY(cudaMalloc((void **)&m->d_m, NP * 4));
+  MLP_TRY(cudaMalloc((void **)&m->d_v, NP * 4));
+  MLP_TRY(cudaMalloc((void **)&m->d_g, NP * 4));
+  MLP_TRY(cudaMalloc((void **)&m->d_norm, 2 * NF * 4));
+  MLP_TRY(cudaMalloc((void **)&m->d_part, (size_t)kGradBlocks * (NP + 1) * 4));
+  MLP_TRY(cudaMalloc((void **)&m->d_loss, 8));
+  MLP_TRY(cudaMalloc((void **)&m->d_stats, 2 * NF * 8));
+  MLP_TRY(cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)grad_smem()));
+  // He-uniform weights U(-sqrt(6/fan_in), +sqrt(6/fan_in)), zero biases
+  std::vector<float> w(NP, 0.f);
+  uint64_t st = seed;
+  auto uni = [&](float lim) {
+    const double u = (splitmix64(st) >> 11) * (1.0 / 9007199254740992.0);
+    return (float)((2.0 * u - 1.0) * lim);
+  };
+  for (int i = 0; i < NH * NF; ++i) w[OW1 + i] = uni(std::sqrt(6.f / NF));
+  for (int i = 0; i < NH * NH; ++i) w[OW2 + i] = uni(std::sqrt(6.f / NH));
+  for (int i = 0; i < NH; ++i) w[OW3 + i] = uni(std::sqrt(6.f / NH));
+  std::vector<float> norm(2 * NF, 0.f);
+  for (int i = 0; i < NF; ++i) norm[NF + i] = 1.f;
+  MLP_TRY(cudaMemcpy(m->d_w, w.data(), NP * 4, cudaMemcpyHostToDevice));
+  MLP_TRY(cudaMemcpy(m->d_norm, norm.data(), 2 * NF * 4, cudaMemcpyHostToDevice));
+  MLP_TRY(cudaMemset(m->d_m, 0, NP * 4));
+  MLP_TRY(cudaMemset(m->d_v, 0, NP * 4));
+  MLP_TRY(cudaMemset(m->d_g, 0, NP * 4));
+  return OC_OK;
+}
+
+void oc_mlp_destroy(oc_mlp *m) {
+  if (!m) return;
+  if (m->stream) cudaStreamSynchronize(m->stream);
+  for (void *p : {(void *)m->d_w, (void *)m->d_m, (void *)m->d_v, (void *)m->d_g,
+                  (void *)m->d_part, (void *)m->d_norm, (void *)m->d_loss, (void *)m->d_stats})
+    if (p) cudaFree(p);
+  if (m->stream) cudaStreamDestroy(m->stream);
+  delete m;
+}
+
+const char *oc_mlp_last_error(const oc_mlp *m) { return m ? m->err.c_str() : "null handle"; }
+void *oc_mlp_stream(oc_mlp *m) { return m ? (void *)m->stream : nullptr; }
+
+oc_status oc_mlp_get_params(oc_mlp *m, float *params) {
+  if (!m || !params) return OC_ERR_INVALID_ARG;
+  MLP_TRY(cudaMemcpyAsync(params, m->d_w, NP * 4, cudaMemcpyDeviceToHost, m->stream));
+  MLP_TRY(cudaStreamSynchronize(m->stream));
+  return OC_OK;
+}
+
+oc_status oc_mlp_set_params(oc_mlp *m, const float *params) {
+  if (!m || !params) return OC_ERR_INVALID_ARG;
+  MLP_TRY(cudaMemcpyAsync(m->d_w, params, NP * 4, cudaMemcpyHostToDevice, m->stream));
+  MLP_TRY(cudaMemsetAsync(m->d_m, 0, NP * 4, m->stream));
+  MLP_TRY(cudaMemsetAsync(m->d_v, 0, NP * 4, m->stream));
+  MLP_TRY(cudaStreamSynchronize(m->stream));
+  m->steps = 0;
+  return OC_OK;
+}
+
+oc_status oc_mlp_get_normalization(oc_mlp *m, float *mean_inv_std) {
+  if (!m || !mean_inv_std) return OC_ERR_INVALID_ARG;
+  MLP_TRY(cudaMemcpyAsync(mean_inv_std, m->d_norm, 2 * NF * 4, cudaMemcpyDeviceToHost, m->stream));
+  MLP_TRY(cudaStreamSynchronize(m->stream));
+  return OC_OK;
+}
+
+oc_status oc_mlp_set_normalization(oc_mlp *m, const float *mean_inv_std) {
+  if (!m || !mean_inv_std) return OC_ERR_INVALID_ARG;
+  MLP_TRY(cudaMemcpyAsync(m->d_norm, mean_inv_std, 2 * NF * 4, cudaMemcpyHostToDevice, m->stream));
+  MLP_TRY(cudaStreamSynchronize(m->stream));
+  return OC_OK;
+}
+
+oc_status oc_mlp_fit_normalization(oc_mlp *m, const float *features, int64_t n) {
+  if (!m || !features || n <= 0) return OC_ERR_INVALID_ARG;
+  MLP_TRY(cudaMemsetAsync(m->d_stats, 0, 2 * NF * 8, m->stream));
+  const int grid = (int)std::min<int64_t>(1216, (n + 255) / 256);
+  mlp_stats_kernel<<<grid, 256, 0, m->stream>>>(features, n, m->d_stats);
+  MLP_TRY(cudaGetLastError());
+  double st[2 * NF];
+  MLP_TRY(cudaMemcpyAsync(st, m->d_stats, sizeof(st), cudaMemcpyDeviceToHost, m->stream));
+  MLP_TRY(cudaStreamSynchronize(m->stream));
+  float norm[2 * NF];
+  for (int i = 0; i < NF; ++i) {
+    const double mu = st[i] / n, var = std::max(st[NF + i] / n - mu * mu, 0.0);
+    norm[i] = (float)mu;
+    norm[NF + i] = var > 1e-20 ? (float)(1.0 / std::sqrt(var)) : 1.f;
+  }
+  return oc_mlp_set_normalization(m, norm);
+}
+
+oc_status oc_mlp_forward(oc_mlp *m, const float *features, int64_t n, float *logits) {
+  if (!m || !features || !logits || n < 0) return OC_ERR_INVALID_ARG;
+  if (n == 0) return OC_OK;
+  const int grid = (int)std::min<int64_t>(152 * 8, (n + kThreads - 1) / kThreads);
+  mlp_forward_kernel<<<grid, kThreads, 0, m->stream>>>(m->d_w, m->d_norm, features, n, logits);
+  MLP_TRY(cudaGetLastError());
+  return OC_OK;
+}
+
+oc_status oc_mlp_gradient(oc_mlp *m, const float *features, const float *labels, int64_t n,
+                          float pos_weight, float *grad, double *loss) {
+  if (!m || !features || !labels || n <= 0) return OC_ERR_INVALID_ARG;
+  const int64_t tiles = (n + kThreads - 1) / kThreads;
+  const int grid = (int)std::min<int64_t>(kGradBlocks, tiles);
+  mlp_grad_kernel<<<grid, kThreads, grad_smem(), m->stream>>>(
+      m->d_w, m->d_norm, features, labels, n, pos_weight, (float)(1.0 / (double)n), m->d_part);
+  MLP_TRY(cudaGetLastError());
+  mlp_reduce_kernel<<<(NP + 1 + 255) / 256, 256, 0, m->stream>>>(m->d_part, grid, m->d_g,
+                                                                  m->d_loss);
+  MLP_TRY(cudaGetLastError());
+  if (grad) MLP_TRY(cudaMemcpyAsync(grad, m->d_g, NP * 4, cudaMemcpyDeviceToHost, m->stream));
+  if (loss) {
+    double l = 0;
+    MLP_TRY(cudaMemcpyAsync(&l, m->d_loss, 8, cudaMemcpyDeviceToHost, m->stream));
+    MLP_TRY(cudaStreamSynchronize(m->stream));
+    *loss = l / (double)n;
+  } else if (grad) {
+    MLP_TRY(cudaStreamSynchronize(m->stream));
+  }
+  return OC_OK;
+}
+
+oc_status oc_mlp_adam_step(oc_mlp *m, float lr) {
+  if (!m || !(lr > 0.f)) return OC_ERR_INVALID_ARG;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  m->steps++;
+  const float c1 = 1.f - std::pow(b1, (float)m->steps), c2 = 1.f - std::pow(b2, (float)m->steps);
+  mlp_adam_kernel<<<(NP + 255) / 256, 256, 0, m->stream>>>(m->d_w, m->d_m, m->d_v, m->d_g, lr,
+                                                           b1, b2, eps, c1, c2);
+  MLP_TRY(cudaGetLastError());
+  return OC_OK;
+}
+
+oc_status oc_mlp_synchronize(oc_mlp *m) {
+  if (!m) return OC_ERR_INVALID_ARG;
+  MLP_TRY(cudaStreamSynchronize(m->stream));
+  return OC_OK;
+}
+
+}  // extern "C"

@@ -45,7 +45,7 @@ def compute(name):
     mesh, orc = oracle_for(name)
     n = orc.n
     z, q = perturbed_state(orc, 4, amp=1e-4)
-    out = {"n": n}
+    out = {"n": n, "in_z": z.copy(), "in_q": q.copy()}
     # ERK stage 1 of 3
     kz, kq = stage_inputs(n, 1)
     kz, kq = [k.copy() for k in kz], [k.copy() for k in kq[:4]]

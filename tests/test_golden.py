@@ -2,8 +2,8 @@
 
 CPU: the oracle still reproduces them (libm may differ in the last bit between
 x86 and Arm hosts, hence 1e-13 rather than bitwise).  GPU: the FP64 operator
-reproduces them through the C ABI within 1e-12, with inputs built by the GPU
-itself (no oracle call on that side).
+reproduces them through the C ABI within 1e-12 from the stored stage inputs
+(no oracle call on that side).
 """
 import os
 
@@ -37,14 +37,6 @@ def test_oracle_reproduces_golden(name):
         assert rel(np.asarray(out[k], np.float64), v) < 1e-13, k
 
 
-def gpu_inputs(op, n, seed=4, amp=1e-4):
-    """perturbed_state of tests/cases.py with the GPU's own projection."""
-    z, q = np.zeros(n), np.zeros(2 * n)
-    op.project_vortex(0.0, z, q)
-    rng = np.random.default_rng(seed)
-    return z + amp * rng.standard_normal(n), q + amp * rng.standard_normal(2 * n)
-
-
 def gpu_op(name):
     from oceano_gb300.operator import OceanoOperator
     from oceano_gb300.workloads import apply_bcs
@@ -68,7 +60,7 @@ def test_gpu_matches_golden(gpu_lib, name):
     op = gpu_op(name)
     n = int(ref["n"])
     assert op.n_dofs == n
-    z, q = gpu_inputs(op, n)
+    z, q = ref["in_z"], ref["in_q"]
     kz, kq = M.stage_inputs(n, 1)
     kz, kq = [k.copy() for k in kz], [k.copy() for k in kq[:4]]
     nz, nq = np.zeros(n), np.zeros(2 * n)

@@ -1,0 +1,130 @@
+"""Learned refinement indicator on the GPU against its CPU oracle.
+
+* features: the 12 per-cell features vs oracle/indicator_oracle.features;
+* BF16 MLP forward: logits vs the oracle's emulation of the same roundings;
+* gradient: loss and gradient vs the oracle's analytic gradient (whose own
+  formulas are checked against finite differences on the CPU);
+* Adam and the normalisation fit vs NumPy;
+* a small train / evaluate cycle on a vortex ensemble.
+"""
+import numpy as np
+import pytest
+
+from oracle import indicator_oracle as IO
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def random_net(seed, n):
+    rng = np.random.default_rng(seed)
+    p = (0.3 * rng.standard_normal(IO.NP)).astype(np.float32)
+    norm = np.concatenate([rng.standard_normal(12), 0.5 + rng.random(12)]).astype(np.float32)
+    X = (2 * rng.standard_normal((n, 12))).astype(np.float32)
+    y = (rng.random(n) < 0.3).astype(np.float32)
+    return p, norm, X, y
+
+
+def model_with(p, norm):
+    from oceano_gb300.indicator import LearnedIndicator
+    m = LearnedIndicator(seed=7)
+    m.params = p
+    m.normalization = norm
+    return m
+
+
+def test_features_match_oracle(gpu_lib):
+    import torch
+    from cases import VORTEX, hanging_mesh, mixed_degree
+    from oceano_gb300.indicator import cell_info, features
+    from oceano_gb300.operator import OceanoOperator
+    mesh = mixed_degree(hanging_mesh(2, seed=11))
+    member = (np.arange(mesh.n_cells) >= mesh.n_cells // 2).astype(np.int32)
+    info = cell_info(mesh, member)
+    orc = O.Oracle(mesh, bcs={0: ("wall",)}, vortex=VORTEX + [0, 0])
+    z, q = orc.project_vortex(0.0)
+    op = OceanoOperator(mesh)
+    op.set_wall_boundary(0)
+    f, fl, w = features(op, torch.from_numpy(z).cuda(), torch.from_numpy(q).cuda(),
+                        torch.from_numpy(info).cuda(), 2, 1e-5, want_vorticity=True)
+    f, fl, w = f.cpu().numpy(), fl.cpu().numpy(), w.cpu().numpy()
+    fo, flo, wo = IO.features(orc, mesh, z, q, info, 2, 1e-5)
+    assert np.allclose(f[:, :3], fo[:, :3], rtol=1e-6, atol=1e-7)
+    assert np.allclose(w, wo, rtol=1e-5, atol=1e-6)
+    assert np.allclose(f[:, 3], fo[:, 3], rtol=1e-5, atol=1e-6)
+    assert np.allclose(f[:, 6:10], fo[:, 6:10], rtol=1e-5, atol=1e-6)
+    gs = np.abs(fo[:, 4:6]).max()
+    assert np.abs(f[:, 4:6] - fo[:, 4:6]).max() <= 1e-5 * gs
+    assert np.array_equal(f[:, 10:], fo[:, 10:])
+    sure = np.abs(wo - 1e-5) > 1e-6  # flags away from the threshold
+    assert np.array_equal(fl[sure], flo[sure])
+
+
+def test_mlp_forward_matches_oracle(gpu_lib):
+    import torch
+    p, norm, X, _ = random_net(1, 3000)
+    m = model_with(p, norm)
+    z = m.forward(torch.from_numpy(X).cuda()).cpu().numpy()
+    zo, _ = IO.forward(p, norm, X)
+    assert np.abs(z - zo).max() <= 1e-5 * (1 + np.abs(zo).max())
+
+
+@pytest.mark.parametrize("n", [100, 1000, 70000])
+def test_mlp_gradient_matches_oracle(gpu_lib, n):
+    import torch
+    p, norm, X, y = random_net(2, n)
+    m = model_with(p, norm)
+    loss, g = m.gradient(torch.from_numpy(X).cuda(), torch.from_numpy(y).cuda(), 3.0)
+    lo, go = IO.loss_and_grad(p, norm, X, y, 3.0)
+    assert abs(loss - lo) <= 1e-5 * abs(lo)
+    assert np.linalg.norm(g - go) <= 1e-4 * np.linalg.norm(go)
+
+
+def test_adam_step_and_normalisation(gpu_lib):
+    import torch
+    p, norm, X, y = random_net(3, 500)
+    m = model_with(p, norm)
+    _, g = m.gradient(torch.from_numpy(X).cuda(), torch.from_numpy(y).cuda(), 1.0)
+    m.adam_step(1e-3)
+    # first Adam step: m = 0.1 g, v = 0.001 g^2, bias corrections 0.1 and 0.001
+    g64 = g.astype(np.float64)
+    expect = p - 1e-3 * g64 / (np.abs(g64) + 1e-8)
+    assert np.allclose(m.params, expect, rtol=1e-5, atol=1e-7)
+    m.fit_normalization(torch.from_numpy(X).cuda())
+    nrm = m.normalization
+    assert np.allclose(nrm[:12], X.mean(0), rtol=1e-4, atol=1e-5)
+    assert np.allclose(nrm[12:], 1 / X.std(0), rtol=1e-4)
+
+
+def test_train_and_evaluate_small_ensemble(gpu_lib):
+    """Train on 4 members (seeds 100..103), evaluate on 4 others (seeds 0..3):
+    the loss falls and the learned refinement set needs no more remeshes than
+    the vorticity indicator's."""
+    import torch
+    from oceano_gb300 import workloads as W
+    from oceano_gb300.indicator import (LearnedIndicator, cell_info, evaluate, member_of_cells,
+                                        run_and_record, training_pairs)
+
+    def small(seed0):
+        mem = W.ensemble_members(4, seed0)
+        for m in mem:
+            m["target"] = 5000.0
+        op, z, q, mem, meshes = W.ensemble(members=mem, precision="mixed")
+        info = torch.from_numpy(cell_info(op.mesh, member_of_cells(meshes))).cuda()
+        zt, qt = torch.from_numpy(z).cuda(), torch.from_numpy(q).cuda()
+        dt = 0.075 / op.compute_cell_transport_speed(zt, qt)
+        return op, zt, qt, info, dt, member_of_cells(meshes)
+
+    op, z, q, info, dt, _ = small(100)
+    recs = run_and_record(op, z, q, info, 4, dt, 60, every=1)
+    X, Y = training_pairs(recs, 10)
+    model = LearnedIndicator(seed=1)
+    model.fit_normalization(X)
+    pos = float((Y.numel() - Y.sum()) / max(float(Y.sum()), 1.0))
+    losses = model.train(X, Y, epochs=150, lr=3e-3, pos_weight=pos)
+    assert losses[-1] < 0.7 * losses[0]
+    op2, z2, q2, info2, dt2, members = small(0)
+    recs2 = run_and_record(op2, z2, q2, info2, 4, dt2, 40, every=1)
+    res = evaluate(model, recs2, 10, members, 4)
+    assert res["recall"] > 0.8
+    assert res["remesh_learned"] <= res["remesh_vorticity"]

@@ -1,0 +1,70 @@
+"""CPU checks of the learned-indicator oracle and host logic (no GPU)."""
+import numpy as np
+
+from oracle import indicator_oracle as IO
+
+
+def test_bf16_rounding_known_answers():
+    x = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -9, 1.0 + 2 ** -7 + 2 ** -8, -2.5, 0.0],
+                 np.float32)
+    # 1 + 2^-8 is a tie between 1 and 1 + 2^-7: to even (1); 1 + 3*2^-9 rounds up;
+    # 1 + 2^-7 + 2^-8 is a tie: to even (1 + 2^-6)
+    expect = np.array([1.0, 1.0, 1.0 + 2 ** -7, 1.0 + 2 ** -6, -2.5, 0.0], np.float32)
+    assert np.array_equal(IO.bf16(x), expect)
+
+
+def random_net(seed):
+    rng = np.random.default_rng(seed)
+    p = (0.3 * rng.standard_normal(IO.NP)).astype(np.float32)
+    norm = np.concatenate([rng.standard_normal(12), 1.0 + rng.random(12)]).astype(np.float32)
+    X = rng.standard_normal((64, 12)).astype(np.float32)
+    y = (rng.random(64) < 0.3).astype(np.float32)
+    return p, norm, X, y
+
+
+def test_analytic_gradient_matches_finite_differences():
+    """The oracle's backward formulas, on the FP64 network without roundings."""
+    p, norm, X, y = random_net(1)
+    p = p.astype(np.float64)
+    _, g = IO.loss_and_grad(p, norm, X, y, 3.0, exact=True)
+    rng = np.random.default_rng(2)
+    idx = np.concatenate([rng.choice(np.arange(IO.OB1), 8), rng.choice(np.arange(IO.OW2, IO.OB2), 8),
+                          [IO.OB1 + 3, IO.OB2 + 5, IO.OW3 + 7, IO.OB3]])
+    h = 1e-6
+    for e in idx:
+        pp, pm = p.copy(), p.copy()
+        pp[e] += h
+        pm[e] -= h
+        fd = (IO.loss_and_grad(pp, norm, X, y, 3.0, exact=True)[0] -
+              IO.loss_and_grad(pm, norm, X, y, 3.0, exact=True)[0]) / (2 * h)
+        assert abs(fd - g[e]) <= 1e-6 * max(1e-3, abs(g[e])), e
+
+
+def test_rounded_forward_close_to_exact():
+    p, norm, X, _ = random_net(3)
+    z, _ = IO.forward(p, norm, X)
+    ze, _ = IO.forward(p, norm, X, exact=True)
+    assert np.abs(z - ze).max() < 0.05 * (1 + np.abs(ze).max())
+
+
+def test_remesh_count():
+    from oceano_gb300.indicator import remesh_count
+    seq = [np.eye(1, 12, k, dtype=bool)[0] for k in range(8)]  # one flag moving right
+    assert remesh_count(seq) == 7
+    ahead = [seq[min(k + 1, 7)] | seq[min(k + 2, 7)] | seq[min(k + 3, 7)] for k in range(8)]
+    assert remesh_count(seq, ahead) == 1  # at t = 4: {4..7} covers the rest
+    members = np.array([0] * 6 + [1] * 6)
+    assert remesh_count(seq, None, members, 2) == 7
+
+
+def test_cell_info_neighbours_symmetric():
+    from cases import hanging_mesh
+    from oceano_gb300.indicator import cell_info
+    m = hanging_mesh(2)
+    info = cell_info(m)
+    for c in range(m.n_cells):
+        for f in range(4):
+            nb = info[c, f]
+            if nb >= 0:
+                assert c in info[nb, :4] or m.level[nb] != m.level[c]
+    assert (info[:, 4] == m.level).all()
