@@ -23,7 +23,9 @@ Secondary workloads (--workload; same JSON keys, not the headline line):
   channel   250x10 cells, p = 2, bump bathymetry, implicit Manning friction
             (ARK Giraldo / TR-BDF2);
   ensemble  64 vortices with seeded centres, radii and strengths on refined-disk
-            meshes of 5k-40k cells each (p = 1, 2), one operator over their union.
+            meshes of 5k-40k cells each (p = 1, 2), one operator over their union;
+  indicator the learned refinement indicator trained and evaluated on ensembles
+            (--steps = training epochs).
 """
 from __future__ import annotations
 
@@ -353,20 +355,86 @@ def run_reference(args, rank, world):
                 "build needs deal.II 9.5 + p4est + MPI, absent on this image"}))
 
 
+def run_indicator(args):
+    """Learned refinement indicator on the vortex ensemble: train the BF16 MLP on
+    20 members (seeds 100..119) to predict the vorticity flags 10 steps ahead,
+    evaluate it on the 64 members (seeds 1000..1063), time its kernels."""
+    import torch
+    import __graft_entry__ as ge
+    ge.build()
+    from oceano_gb300 import workloads as W
+    from oceano_gb300.indicator import (LearnedIndicator, cell_info, evaluate, member_of_cells,
+                                        run_and_record, training_pairs)
+
+    def setup(n, seed0):
+        op, z, q, mem, meshes = W.ensemble(n, "mixed", seed0)
+        info = torch.from_numpy(cell_info(op.mesh, member_of_cells(meshes))).cuda()
+        zt, qt = torch.from_numpy(z).cuda(), torch.from_numpy(q).cuda()
+        dt = CFL / op.compute_cell_transport_speed(zt, qt)
+        return op, zt, qt, info, dt, member_of_cells(meshes)
+
+    horizon, every = 10, 2
+    op, z, q, info, dt, _ = setup(20, 100)
+    recs = run_and_record(op, z, q, info, 20, dt, 100, every=every)
+    X, Y = training_pairs(recs, horizon // every)
+    del recs
+    model = LearnedIndicator(seed=1)
+    model.fit_normalization(X)
+    pos = float((Y.numel() - Y.sum()) / max(float(Y.sum()), 1.0))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = model.train(X, Y, epochs=args.steps, lr=3e-3, pos_weight=pos)
+    t_train = time.perf_counter() - t0
+    ev_op, z2, q2, info2, dt2, members = setup(64, 1000)
+    recs2 = run_and_record(ev_op, z2, q2, info2, 64, dt2, 60, every=1)
+    res = evaluate(model, recs2, horizon, members, 64)
+    f = recs2[0][0]
+    for _ in range(3):
+        model.forward(f)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 20
+    for _ in range(reps):
+        model.forward(f)
+    t_fwd = (time.perf_counter() - t0) / reps
+    flops_fwd = 2 * (12 * 64 + 64 * 64 + 64)
+    out = {
+        "metric": "learned refinement indicator: BF16 MLP forward cells/s",
+        "value": f.shape[0] / t_fwd, "unit": "cells/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": 3, "higher_is_better": True, "dtype": "bf16 (fp32 accumulate)",
+        "data": "synthetic",
+        "config": {"workload": "vortex ensemble: train 20 members (seeds 100..119), evaluate "
+                               "64 members (seeds 1000..1063); flags 10 steps ahead",
+                   "train_samples": int(X.shape[0]), "eval_cells": int(f.shape[0]),
+                   "epochs": args.steps},
+        "forward_tflops": f.shape[0] * flops_fwd / t_fwd / 1e12,
+        "train_samples_per_s": X.shape[0] * args.steps / t_train,
+        "loss_first_last": [losses[0], losses[-1]],
+        "eval": res,
+    }
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="vortex", choices=["vortex", "hp", "channel", "ensemble"])
+    ap.add_argument("--workload", default="vortex",
+                    choices=["vortex", "hp", "channel", "ensemble", "indicator"])
     ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--legs", default="mixed,fp64,e2e",
+                    help="timed legs (a subset of mixed,fp64,e2e; profiling runs use 'mixed')")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "indicator":
+        run_indicator(args)
         return
     import torch
     import __graft_entry__ as ge
@@ -375,11 +443,15 @@ def main():
     mesh, n, dt, z0, q0 = wl.mesh, wl.n, wl.dt, wl.z0, wl.q0
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     barrier(world)
+    legs = set(args.legs.split(","))
     with Clocks() as clk:  # samples over both timed loops (the mixed one alone is ~30 ms)
         ms_m, zm, qm, launches = time_device(wl.op_m, mesh, z0, q0, args.steps, args.warmup, dt,
                                              flush, wl.scheme)
-        ms_d, zd, qd, _ = time_device(wl.op_d, mesh, z0, q0, args.steps, args.warmup, dt, flush,
-                                      wl.scheme)
+        if "fp64" in legs:
+            ms_d, zd, qd, _ = time_device(wl.op_d, mesh, z0, q0, args.steps, args.warmup, dt,
+                                          flush, wl.scheme)
+        else:
+            ms_d, zd, qd = [float("nan")], zm, qm
     t_m = max_over_ranks(sum(ms_m) / 1e3, world)
     t_d = max_over_ranks(sum(ms_d) / 1e3, world)
     ndof = 3 * n
@@ -387,7 +459,8 @@ def main():
     units = ndof * stages * args.steps * world  # every rank advances its own replica
     value = units / t_m
     value_d = units / t_d
-    e2e_ms, io_bytes = time_e2e(wl.op_m, z0, q0, max(2, args.steps // 4), 2, dt, wl.scheme)
+    e2e_ms, io_bytes = time_e2e(wl.op_m, z0, q0, max(2, args.steps // 4), 2, dt, wl.scheme) \
+        if "e2e" in legs else (float("nan"), 0)
     e2e_ms = max_over_ranks(e2e_ms, world)
     e2e_value = ndof * stages * world / (e2e_ms / 1e3)
     peak, peak_kind = peaks()

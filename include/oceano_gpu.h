@@ -244,6 +244,19 @@ oc_status oc_set_launch_mode(oc_op *op, int32_t mode);
  * out[2..5] warps per block of the degree 1..4 groups, out[6] tuned (0/1) */
 oc_status oc_launch_config(const oc_op *op, int32_t *out);
 
+/* compute_errors_hydro (OceanDG.h:2380-2459) with the travelling vortex of
+ * oc_set_vortex as the exact solution at `time`: errors[0] = L2 error of the
+ * depth, errors[1] = L2 error of the discharge (both components), on the cell
+ * Gauss rule, zb from the cell static data (0 without). errors is a host array. */
+oc_status oc_errors_vortex(oc_op *op, double time, const double *height, const double *discharge,
+                           int32_t memory, double *errors);
+/* prepare_for_conservative_coarsening (OceanDG.h:2732-2778): on every cell with
+ * mark[c] != 0 (degree p -> 0 in the next remesh) all nodal height values become the
+ * average of zeta over the wet Gauss-Lobatto (p+2) points; cells with no wet point
+ * are left unchanged.  height is updated in place. */
+oc_status oc_conservative_coarsening(oc_op *op, const uint8_t *mark, double *height,
+                                     int32_t memory);
+
 /* ---- learned refinement indicator (no reference counterpart) -------------------
  * The reference refines where the vorticity indicator (hpTuner.h:247-305) exceeds
  * a fraction of its maximum (main.cc:749-765).  The functions below compute

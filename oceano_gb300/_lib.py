@@ -71,6 +71,9 @@ EXPORTS = {
                                          C.c_int32]),
     "oc_project_vortex": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_int32]),
     "oc_transport_speed_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "oc_errors_vortex": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_int32,
+                                   C.c_void_p]),
+    "oc_conservative_coarsening": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]),
     "oc_indicator_features": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_int32, C.c_float, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.c_int32]),

@@ -49,6 +49,10 @@ cudaError_t launch_velocity_field(const AuxArgs &, const double *, const double 
 cudaError_t launch_vorticity(const AuxArgs &, const double *, int, const double *,
                              const double *, float *, cudaStream_t);
 cudaError_t launch_project_vortex(const AuxArgs &, double, double *, double *, cudaStream_t);
+cudaError_t launch_errors(const AuxArgs &, double, const double *, const int *, const double *,
+                          const double *, double *, double *, cudaStream_t);
+cudaError_t launch_conservative_coarsening(const AuxArgs &, const unsigned char *, double *,
+                                           cudaStream_t);
 cudaError_t launch_features(const AuxArgs &, const double *, const double *, const float *,
                             const int *, int, unsigned *, float, float *, float *, float *,
                             cudaStream_t);
@@ -155,6 +159,7 @@ struct oc_op {
   double *d_ivel = nullptr;
   float *d_ivort = nullptr;
   unsigned *d_imax = nullptr;
+  double *d_epart = nullptr;  // per-cell squared errors + the two results
   int imax_n = 0;
   // graph cache of oc_perform_time_step
   int64_t graph_launches = 0;
@@ -597,6 +602,7 @@ static void fill_common(oc_op *op, StageArgs &a) {
   a.sdo0 = op->d_sdo[0]; a.sdo1 = op->d_sdo[1]; a.sdo2 = op->d_sdo[2];
   a.cfrec = op->d_cfrec;
   a.geof = op->prm.precision == OC_PREC_MIXED ? op->d_geof : nullptr;
+  a.uniform_nn = op->uniform_deg ? (op->uniform_deg + 1) * (op->uniform_deg + 1) : 0;
   a.dscratch = op->d_dscratch;
   a.cfsdo = (op->d_sd[3] || op->d_sd[4]) ? op->d_cfsdo : nullptr;
   const double cu = op->prm.threshold_wetdry;
@@ -1147,6 +1153,49 @@ extern "C" oc_status oc_vorticity_indicator(oc_op *op, const double *u, int32_t 
     OC_TRY(cudaMemcpyAsync(ind, tmp, op->n_cells * sizeof(float), cudaMemcpyDeviceToHost, op->stream));
   oc_status st = read_error(op);
   if (tmp) cudaFree(tmp);
+  return st;
+}
+
+extern "C" oc_status oc_errors_vortex(oc_op *op, double time, const double *z, const double *q,
+                                      int32_t memory, double *errors) {
+  if (!op || !z || !q || !errors) return OC_ERR_INVALID_ARG;
+  const size_t nz = op->n_dofs, nq = 2 * nz;
+  const double *dz = z, *dq = q;
+  if (memory == OC_MEM_HOST) {
+    if (ensure(op, &op->st_rz, nz) || ensure(op, &op->st_rq, nq)) return OC_ERR_CUDA;
+    OC_TRY(cudaMemcpyAsync(op->st_rz, z, nz * 8, cudaMemcpyHostToDevice, op->stream));
+    OC_TRY(cudaMemcpyAsync(op->st_rq, q, nq * 8, cudaMemcpyHostToDevice, op->stream));
+    dz = op->st_rz; dq = op->st_rq;
+  }
+  if (ensure(op, &op->d_epart, 2 * (size_t)op->n_cells + 2)) return OC_ERR_CUDA;
+  double *dout = op->d_epart + 2 * (size_t)op->n_cells;
+  OC_TRY(launch_errors(aux_args(op), time, op->d_sd[0], op->d_sdo[0], dz, dq, op->d_epart, dout,
+                       op->stream));
+  op->launches += 2;
+  OC_TRY(cudaMemcpyAsync(errors, dout, 2 * sizeof(double), cudaMemcpyDeviceToHost, op->stream));
+  return read_error(op);
+}
+
+extern "C" oc_status oc_conservative_coarsening(oc_op *op, const uint8_t *mark, double *z,
+                                                int32_t memory) {
+  if (!op || !mark || !z) return OC_ERR_INVALID_ARG;
+  const size_t nz = op->n_dofs, nc = op->n_cells;
+  const unsigned char *dmark = mark;
+  double *dz = z;
+  unsigned char *tmark = nullptr;
+  if (memory == OC_MEM_HOST) {
+    if (ensure(op, &op->st_rz, nz)) return OC_ERR_CUDA;
+    OC_TRY(cudaMalloc((void **)&tmark, nc));
+    OC_TRY(cudaMemcpyAsync(tmark, mark, nc, cudaMemcpyHostToDevice, op->stream));
+    OC_TRY(cudaMemcpyAsync(op->st_rz, z, nz * 8, cudaMemcpyHostToDevice, op->stream));
+    dmark = tmark; dz = op->st_rz;
+  }
+  OC_TRY(launch_conservative_coarsening(aux_args(op), dmark, dz, op->stream));
+  op->launches++;
+  if (memory == OC_MEM_HOST)
+    OC_TRY(cudaMemcpyAsync(z, dz, nz * 8, cudaMemcpyDeviceToHost, op->stream));
+  oc_status st = read_error(op);
+  if (tmark) cudaFree(tmark);
   return st;
 }
 

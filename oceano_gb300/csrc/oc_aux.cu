@@ -213,6 +213,113 @@ cudaError_t launch_velocity_field(const AuxArgs &a, const double *z, const doubl
   return cudaGetLastError();
 }
 
+// compute_errors_hydro (OceanDG.h:2380-2459) with the vortex as exact solution:
+// per cell the squared L2 errors of depth and discharge on the cell Gauss rule,
+// written to part[2c], part[2c+1] (summed by errors_reduce_kernel in a fixed order).
+__global__ void errors_kernel(const AuxArgs a, double time, const double *sd0, const int *sdo0,
+                              const double *z, const double *q, double *part) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.n_cells) return;
+  const int p = a.deg[c], N = p + 1, n = N * N, Q = (3 * p) / 2 + 1;
+  const DegTables<double> &tb = tab<double>(p);
+  const double *J = a.geo + 11 * (int64_t)c;
+  const int64_t zo = a.off[c];
+  const double *zc = z + zo, *q0 = q + 2 * zo, *q1 = q + 2 * zo + n;
+  const double *sd = sd0 ? sd0 + sdo0[c] : nullptr;
+  const VortexParams vp = vortex_params(a.vortex);
+  double e0 = 0., e1 = 0.;
+  for (int qy = 0; qy < Q; ++qy)
+    for (int qx = 0; qx < Q; ++qx) {
+      double zv = 0., a0 = 0., a1 = 0.;
+      for (int iy = 0; iy < N; ++iy)
+        for (int ix = 0; ix < N; ++ix) {
+          const double b = tb.BQ[qy][iy] * tb.BQ[qx][ix];
+          zv += b * zc[iy * N + ix];
+          a0 += b * q0[iy * N + ix];
+          a1 += b * q1[iy * N + ix];
+        }
+      const double x = J[0] + J[2] * tb.xQ[qx] + J[3] * tb.xQ[qy];
+      const double y = J[1] + J[4] * tb.xQ[qx] + J[5] * tb.xQ[qy];
+      const double zb = sd ? sd[5 * (qy * Q + qx)] : 0.;
+      const double f0 = vortex_value(vp, a.g, x, y, time, 0);
+      const double hq = depth<double>(f0, zb);
+      const double jxw = tb.wQ[qx] * tb.wQ[qy] * J[10];
+      const double d0 = hq - depth<double>(zv, zb);
+      const double u = vortex_value(vp, a.g, x, y, time, 1) * hq - a0;
+      const double v = vortex_value(vp, a.g, x, y, time, 2) * hq - a1;
+      e0 += d0 * d0 * jxw;
+      e1 += (u * u + v * v) * jxw;
+    }
+  part[2 * (int64_t)c] = e0;
+  part[2 * (int64_t)c + 1] = e1;
+}
+
+// one block: strided partial sums, then a fixed tree (deterministic order)
+__global__ void errors_reduce_kernel(int n, const double *part, double *out) {
+  __shared__ double s0[256], s1[256];
+  double a0 = 0., a1 = 0.;
+  for (int c = threadIdx.x; c < n; c += blockDim.x) {
+    a0 += part[2 * (int64_t)c];
+    a1 += part[2 * (int64_t)c + 1];
+  }
+  s0[threadIdx.x] = a0;
+  s1[threadIdx.x] = a1;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) {
+      s0[threadIdx.x] += s0[threadIdx.x + h];
+      s1[threadIdx.x] += s1[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = sqrt(s0[0]);
+    out[1] = sqrt(s1[0]);
+  }
+}
+
+// prepare_for_conservative_coarsening (OceanDG.h:2732-2778) on marked cells
+__global__ void conservative_coarsening_kernel(const AuxArgs a, const unsigned char *mark,
+                                               double *z) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.n_cells || !mark[c]) return;
+  const int p = a.deg[c], N = p + 1, n = N * N, G = p + 2;
+  const DegTables<double> &tb = tab<double>(p);
+  const double det = a.geo[11 * (int64_t)c + 10];
+  double *zc = z + a.off[c];
+  const double *sd = a.sd1 ? a.sd1 + a.sdo1[c] : nullptr;
+  double area = 0., integral = 0.;
+  for (int gy = 0; gy < G; ++gy)
+    for (int gx = 0; gx < G; ++gx) {
+      double zv = 0.;
+      for (int iy = 0; iy < N; ++iy)
+        for (int ix = 0; ix < N; ++ix) zv += tb.BG[gy][iy] * tb.BG[gx][ix] * zc[iy * N + ix];
+      const double zb = sd ? sd[gy * G + gx] : 0.;
+      const double mask = zv <= -zb ? 0. : 1.;
+      const double jxw = tb.wG[gx] * tb.wG[gy] * det;
+      area += mask * jxw;
+      integral += zv * mask * jxw;
+    }
+  if (area > 0.) {
+    const double v = integral * (1. / area);
+    for (int i = 0; i < n; ++i) zc[i] = v;
+  }
+}
+
+cudaError_t launch_errors(const AuxArgs &a, double time, const double *sd0, const int *sdo0,
+                          const double *z, const double *q, double *part, double *out,
+                          cudaStream_t st) {
+  errors_kernel<<<(a.n_cells + 127) / 128, 128, 0, st>>>(a, time, sd0, sdo0, z, q, part);
+  errors_reduce_kernel<<<1, 256, 0, st>>>(a.n_cells, part, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_conservative_coarsening(const AuxArgs &a, const unsigned char *mark, double *z,
+                                           cudaStream_t st) {
+  conservative_coarsening_kernel<<<(a.n_cells + 127) / 128, 128, 0, st>>>(a, mark, z);
+  return cudaGetLastError();
+}
+
 // Largest vorticity of each member (non-negative floats order like their bits).
 __global__ void member_max_kernel(int n, const float *w, const int *info, int n_members,
                                   unsigned *vmax) {

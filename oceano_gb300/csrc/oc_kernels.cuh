@@ -182,6 +182,17 @@ __device__ __forceinline__ R load_r(const void *p, int64_t i, int is_float, doub
 
 // stage-input load with the input precision fixed at compile time (a runtime
 // switch would let the compiler evaluate both branches)
+// Asynchronous 4-byte global -> shared copy (cp.async, completes without a wait
+// loop of ours; cp_async_wait_all() + __syncwarp() before the data is read).
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 template <typename RIN, typename R>
 __device__ __forceinline__ R load_in(const void *p, int64_t i, double ref) {
   if constexpr (sizeof(RIN) == 4) {
@@ -200,11 +211,12 @@ struct Dims {
   static constexpr int T = Q > G ? Q : G;
   static constexpr int NN = N * N, NT = N * T;
   static constexpr int CPW = 32 / T;
-  // scratch tiles; during the face phase they hold the neighbour traces of the
-  // 8 face slots (3 variables x up to 5 nodes each)
+  // scratch tiles of the sum factorisation
   static constexpr int XS = 6 * NT > 8 * 3 * OC_MAXN ? 6 * NT : 8 * 3 * OC_MAXN;
+  // neighbour traces of the 8 face slots (3 variables x up to 5 nodes each)
+  static constexpr int NBS = 8 * 3 * OC_MAXN;
   // per-cell shared memory: compute-type region and FP64 region (elements)
-  static constexpr int SZR = 10 * NN + XS + 3 * FVS;  // U 3, RES 3, RST 2, BZ 1, ZN 1; X; FV
+  static constexpr int SZR = 10 * NN + XS + 3 * FVS + NBS;  // U 3, RES 3, RST 2, BZ 1, ZN 1; X; FV; NB
   static constexpr int SZD = NN + 3 * NT + T + 2;
   // Team strides: padded so that the 32/T teams of a warp start on different
   // shared-memory banks (stride mod 32 chosen per degree and element size to
@@ -213,7 +225,7 @@ struct Dims {
   static constexpr int pad_d = P == 1 ? 5 : P == 2 ? 2 : P == 3 ? 3 : 4;
   template <typename R>
   static constexpr int bytes_r() {
-    return (((SZR + 31) / 32) * 32 + (sizeof(R) == 4 ? pad_f : pad_d)) * (int)sizeof(R);
+    return (((SZR + 7) / 8) * 8 + (sizeof(R) == 4 ? pad_f : pad_d)) * (int)sizeof(R);
   }
   static constexpr int bytes_d() { return (((SZD + 31) / 32) * 32 + pad_d) * 8; }
   static_assert(SZD <= OC_DSTRIDE, "FP64 zeta work area exceeds its global stride");
@@ -522,6 +534,10 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   R fR[OC_MAXSTAGES];  // coefficients in the compute type, converted once
 #pragma unroll
   for (int j = 0; j < OC_MAXSTAGES; ++j) fR[j] = (R)dy.f[j];
+  R fRs = fR[0];  // f_s
+#pragma unroll
+  for (int j = 1; j < OC_MAXSTAGES; ++j)
+    if (j == a.stage) fRs = fR[j];
   // the mixed time-step path (FP32 registers) forms internal stage inputs in FP32
   constexpr bool fast = MIX && sizeof(KT) == 4;
   const double zref = MIX ? a.zeta_ref : 0.0;
@@ -539,8 +555,10 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   R *RST = RES + 3 * NN;      // 2*NN stiff residual (ARK)
   R *BZ = RST + 2 * NN;       // NN zeta right-hand side b = sum f k (mixed: then delta)
   R *ZN = BZ + NN;            // NN mixed form: zeta^n - zeta_ref
-  R *X = ZN + NN;             // scratch tiles / neighbour traces
+  R *X = ZN + NN;             // scratch tiles
   R *FV = X + D::XS;          // 3*FVS face point values
+  R *NB = FV + 3 * FVS;       // neighbour traces [slot][var][node]
+  R *QB = RST;                // fast ERK path: discharge partial update (RST is ARK-only)
   auto Dreg = [&](int j) {  // FP64 team region of team j: shared (FP64 form) or global slot
     if constexpr (MIX)
       return a.dscratch + ((int64_t)(blockIdx.x * wpb + warp) * OC_MAXCPW + j) * OC_DSTRIDE;
@@ -554,7 +572,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     const int gi = nvalid > 0 ? gi0 + (j < nvalid ? j : 0) : 0;  // idle warps read cell 0
     const int c = group_cells ? group_cells[gi] : group_first + gi;
     w_cell[j] = c;
-    w_off[j] = a.off[c];
+    w_off[j] = a.uniform_nn ? c * a.uniform_nn : a.off[c];
     w_flag[j] = 0;
   }
   __syncwarp();
@@ -563,6 +581,13 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   double *DZ = Dreg(team);        // NN FP64 iterate
   double *DX = DZ + NN;           // 3 tiles N*T
   double *DRED = DX + 3 * NT;     // T+1
+  const double *geo = a.geo + 11 * (int64_t)cell;
+  R gR[11];  // geometry in the compute type (FP32 copy in the mixed form); loads issued early
+#pragma unroll
+  for (int k = 0; k < 11; ++k) {
+    if constexpr (MIX) gR[k] = (R)a.geof[11 * (int64_t)cell + k];
+    else gR[k] = (R)geo[k];
+  }
   for (int e = lane; e < nvalid * 16; e += 32) {  // face records (invalid teams: empty)
     const int j = e >> 4, k = e & 15;
     w_rec[j * 16 + k] = a.cfrec[16 * (int64_t)w_cell[j] + k];
@@ -584,9 +609,11 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     Uj[2 * NN + d] = load_in<RIN, R>(a.rq, oq + NN, 0.0);
     if (!a.apply_mode) {
       R bprev = 0;  // sum_{j<s} f_j kz_j in the reference's order
-      for (int jj = 0; jj < s; ++jj)
-        bprev = jj == 0 ? fR[0] * (R) static_cast<const KT *>(a.kz[1])[oz]
-                        : bprev + fR[jj] * (R) static_cast<const KT *>(a.kz[jj + 1])[oz];
+#pragma unroll
+      for (int jj = 0; jj < OC_MAXSTAGES; ++jj)  // compile-time indices: fR stays in registers
+        if (jj < s)
+          bprev = jj == 0 ? fR[0] * (R) static_cast<const KT *>(a.kz[1])[oz]
+                          : bprev + fR[jj] * (R) static_cast<const KT *>(a.kz[jj + 1])[oz];
       Uj[8 * NN + d] = bprev;
       if constexpr (fast) {
         Uj[9 * NN + d] = s == 0 ? Uj[d] : (R)a.un_zf[oz];
@@ -595,14 +622,43 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       }
     }
   }
-  __syncwarp();
-
-  const double *geo = a.geo + 11 * (int64_t)cell;
-  R gR[11];  // geometry in the compute type (FP32 copy in the mixed form)
+  // fast ERK path: the discharge part of the update known before this stage,
+  // QB = (last stage ? 0 : q^n) + sum_{j<s} f_j k_q[j+1], so that the epilogue loads nothing
+  if (fast && !a.ark && !a.apply_mode) {
+    __syncwarp();  // U of every team is written
+#pragma unroll 4
+    for (int e = lane; e < nvalid * 2 * NN; e += 32) {
+      const int j = e / (2 * NN), d = e - j * 2 * NN;
+      const int64_t gq = 2 * (int64_t)w_off[j] + d;
+      R qb = 0;
 #pragma unroll
-  for (int k = 0; k < 11; ++k) {
-    if constexpr (MIX) gR[k] = (R)a.geof[11 * (int64_t)cell + k];
-    else gR[k] = (R)geo[k];
+      for (int jj = 0; jj < OC_MAXSTAGES; ++jj)
+        if (jj < s) qb += fR[jj] * (R) static_cast<const KT *>(a.kq[jj + 1])[gq];
+      if (!a.last) qb += s == 0 ? Rreg(j)[NN + d] : (R)a.un_qf[gq];
+      Rreg(j)[3 * NN + 3 * NN + d] = qb;  // QB of team j
+    }
+  }
+  __syncwarp();
+  // neighbour traces: FP32 stage inputs are copied asynchronously (cp.async) and
+  // land while the cell integrals run; other inputs are loaded before the faces
+  constexpr bool async_nb = sizeof(RIN) == 4;
+  if constexpr (async_nb) {
+    if (member) {
+      for (int e = t; e < 8 * OC_MAXN; e += T) {
+        const int sl = e / OC_MAXN, i = e - sl * OC_MAXN;
+        const FaceRec r = reinterpret_cast<const FaceRec *>(w_rec + 16 * team)[sl];
+        const int Nn = r.nb_deg() + 1;
+        if (r.kind() == 1 && i < Nn) {
+          const int d = face_dof(Nn, r.nb_face(), i);
+          const int64_t oz = r.other, oq = 2 * (int64_t)r.other;
+          cp_async4(&NB[(sl * 3 + 0) * OC_MAXN + i], static_cast<const float *>(a.rz) + oz + d);
+          cp_async4(&NB[(sl * 3 + 1) * OC_MAXN + i], static_cast<const float *>(a.rq) + oq + d);
+          cp_async4(&NB[(sl * 3 + 2) * OC_MAXN + i],
+                    static_cast<const float *>(a.rq) + oq + Nn * Nn + d);
+        }
+      }
+    }
+    cp_async_commit();
   }
   const R Ji00 = gR[6], Ji01 = gR[7], Ji10 = gR[8], Ji11 = gR[9];
   const R det = gR[10];
@@ -805,9 +861,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   // ---- 2. faces: local_apply_face_* (OceanDG.h:936-1050) and
   //         local_apply_boundary_face_* (:1105-1339) ----------------------------
   const FaceRec *recs = reinterpret_cast<const FaceRec *>(w_rec + 16 * team);
-  // 2a. neighbour traces of every inner slot into X: [slot][var][node]
-  R *NB = X;
-  if (member) {
+  // 2a. neighbour traces of every inner slot: [slot][var][node]
+  if constexpr (async_nb) cp_async_wait_all();
+  if (!async_nb && member) {
     for (int e = t; e < 8 * OC_MAXN; e += T) {
       const int sl = e / OC_MAXN, i = e - sl * OC_MAXN;
       const FaceRec r = recs[sl];
@@ -824,11 +880,27 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   __syncwarp();
   // own outward normals and face lengths of the affine cell
   const R J00 = gR[2], J01 = gR[3], J10 = gR[4], J11 = gR[5];
+  // Conforming faces between cells of this degree (the common case): the trace
+  // row of point k = t (both sides: no subface, standard orientation) and the
+  // integration column of node t, held in registers so that the face loop reads
+  // no lane-dependent constant-bank address.
+  R frow[N], fcol[G], fw;
+  {
+    const int kk = t < G ? t : 0, tt = t < N ? t : 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) frow[i] = tb.F[0][G][kk][i];
+#pragma unroll
+    for (int k = 0; k < G; ++k) fcol[k] = tb.F[0][G][k][tt];
+    fw = tb.wF[G][kk];
+  }
 #pragma unroll 1
   for (int sl = 0; sl < 8; ++sl) {
     const FaceRec r = recs[sl];
     const int kind = member ? r.kind() : 0;
     const int fo = r.own_face();
+    // DoF of node i on face fo: fbase + i * fstride (face_dof)
+    const int fbase = fo == 0 ? 0 : fo == 1 ? N - 1 : fo == 2 ? 0 : (N - 1) * N;
+    const int fstride = fo < 2 ? N : 1;
     int nfo = 0, tsel = 0;
     if (kind != 0) {
       // outward normal of the own face: J^-T n_ref / |.|; tangent length |J t_ref|
@@ -848,6 +920,39 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         const int sdo = a.cfsdo ? w_sdo[8 * team + sl] : 0;
         nfo = nf;
         tsel = side ? sub + 1 : 0;
+        if (sub < 0 && pn == P && orient == 0) {  // conforming, same degree: nf == G <= T
+          if (t < G) {
+            const int k = t;
+            R zo_ = 0, qo0 = 0, qo1 = 0, zn = 0, qn0 = 0, qn1 = 0;
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+              const int d = fbase + i * fstride;
+              const R l = frow[i];
+              zo_ += l * U[d];
+              qo0 += l * U[NN + d];
+              qo1 += l * U[2 * NN + d];
+              zn += l * NB[(sl * 3 + 0) * OC_MAXN + i];
+              qn0 += l * NB[(sl * 3 + 1) * OC_MAXN + i];
+              qn1 += l * NB[(sl * 3 + 2) * OC_MAXN + i];
+            }
+            const R zm = side ? zn : zo_, qm0 = side ? qn0 : qo0, qm1 = side ? qn1 : qo1;
+            const R zp = side ? zo_ : zn, qp0 = side ? qo0 : qn0, qp1 = side ? qo1 : qn1;
+            R zbm = MIX ? zbe_flat : R(0), zbp = zbm;
+            if (MIX && a.sdfe) {
+              zbm = (R)a.sdfe[sdo + 2 * k]; zbp = (R)a.sdfe[sdo + 2 * k + 1];
+            } else if (!MIX && a.sdf) {
+              zbm = (R)a.sdf[sdo + 2 * k]; zbp = (R)a.sdf[sdo + 2 * k + 1];
+            }
+            R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
+            face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1, Pm0,
+                         Pm1, Pp0, Pp1);
+            const R jxw = fw * len;
+            const R sg = side ? R(1) : R(-1);
+            FV[k] = sg * F * jxw;
+            FV[FVS + k] = sg * (Fa0 + (side ? Pp0 : Pm0)) * jxw;
+            FV[2 * FVS + k] = sg * (Fa1 + (side ? Pp1 : Pm1)) * jxw;
+          }
+        } else
         for (int k = t; k < nf; k += T) {
           const int kp = orient ? nf - 1 - k : k;  // point index on the plus side
           const int ko = side ? kp : k, kn = side ? k : kp;
@@ -923,13 +1028,22 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     __syncwarp();
     if (nfo > 0 && t < N) {  // integrate the own-side values against the own basis
       R cz = 0, c0 = 0, c1 = 0;
-      for (int k = 0; k < nfo; ++k) {
-        const R l = tsel < 0 ? tb.BQ[k][t] : tb.F[tsel][nfo][k][t];
-        cz += l * FV[k];
-        c0 += l * FV[FVS + k];
-        c1 += l * FV[2 * FVS + k];
+      if (tsel == 0 && nfo == G) {  // full face of this degree's point set
+#pragma unroll
+        for (int k = 0; k < G; ++k) {
+          cz += fcol[k] * FV[k];
+          c0 += fcol[k] * FV[FVS + k];
+          c1 += fcol[k] * FV[2 * FVS + k];
+        }
+      } else {
+        for (int k = 0; k < nfo; ++k) {
+          const R l = tsel < 0 ? tb.BQ[k][t] : tb.F[tsel][nfo][k][t];
+          cz += l * FV[k];
+          c0 += l * FV[FVS + k];
+          c1 += l * FV[2 * FVS + k];
+        }
       }
-      const int d = face_dof(N, fo, t);
+      const int d = fbase + t * fstride;
       RES[d] += cz;
       RES[NN + d] += c0;
       RES[2 * NN + d] += c1;
@@ -994,7 +1108,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
     for (int ix = 0; ix < N; ++ix) {
       const int d = t * N + ix;
-      BZ[d] = s == 0 ? fR[0] * RES[d] : BZ[d] + fR[s] * RES[d];
+      BZ[d] = s == 0 ? fR[0] * RES[d] : BZ[d] + fRs * RES[d];
     }
   }
   __syncwarp();
@@ -1143,7 +1257,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           R bsum = s == 0 ? (R)dy.f[0] * kex + (R)dy.ft[0] * kim
                           : (R)dy.f[0] * (R) static_cast<const KT *>(a.kq[1])[gidx] +
                                 (R)dy.ft[0] * (R) static_cast<const KT *>(a.kq[2])[gidx];
-          for (int j = 1; j < s + 1; ++j) {
+#pragma unroll
+          for (int j = 1; j < OC_MAXSTAGES; ++j) {
+            if (j > s) break;
             const R ke = j == s ? kex : (R) static_cast<const KT *>(a.kq[2 * j + 1])[gidx];
             const R ki = j == s ? kim : (R) static_cast<const KT *>(a.kq[2 * j + 2])[gidx];
             bsum += (R)dy.f[j] * ke + (R)dy.ft[j] * ki;
@@ -1163,7 +1279,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           const R kex = RES[(1 + e) * NN + d];
           if (valid) static_cast<KT *>(a.kq[2 * s + 1])[gidx] = (KT)kex;
           R bsum = (R)dy.f[0] * (s == 0 ? kex : (R) static_cast<const KT *>(a.kq[1])[gidx]);
-          for (int j = 1; j < s + 1; ++j) {
+#pragma unroll
+          for (int j = 1; j < OC_MAXSTAGES; ++j) {
+            if (j > s) break;
             const R ke = j == s ? kex : (R) static_cast<const KT *>(a.kq[2 * j + 1])[gidx];
             const R ki = (R) static_cast<const KT *>(a.kq[2 * j])[gidx];
             bsum += (R)dy.f[j] * ke + (R)dy.f[j - 1] * ki;
@@ -1381,15 +1499,11 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       R *Rj = Rreg(j);
       const R v = Rj[4 * NN + d];
       if (wkq) static_cast<KT *>(a.kq[s + 1])[gq] = (KT)v;
-      R dl = fR[0] * (s == 0 ? v : (R) static_cast<const KT *>(a.kq[1])[gq]);
-      for (int jj = 1; jj < s + 1; ++jj)
-        dl += fR[jj] * (jj == s ? v : (R) static_cast<const KT *>(a.kq[jj + 1])[gq]);
+      // QB (prologue) = q^n + sum_{j<s} f_j k_q[j+1] (internal stages) or the sum alone
+      const R up = Rj[6 * NN + d] + fRs * v;
       if (s == 0 && a.out_unqf) a.out_unqf[gq] = (float)Rj[NN + d];
-      if (a.out_rq) {
-        const R qn = s == 0 ? Rj[NN + d] : (R)a.un_qf[gq];
-        a.out_rq[gq] = (float)(qn + dl);
-      }
-      Rj[4 * NN + d] = dl;
+      if (a.out_rq) a.out_rq[gq] = (float)up;
+      Rj[4 * NN + d] = up;  // last stage: delta for the FP64 accumulation
     }
     if (a.out_q) {
 #pragma unroll 2
@@ -1412,8 +1526,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       const double kc = (double)(KT)v;
       if (wkq) static_cast<KT *>(a.kq[s + 1])[gq] = (KT)v;
       double acc = a.un_q[gq] + dy.f[0] * (s == 0 ? kc : (double)static_cast<const KT *>(a.kq[1])[gq]);
-      for (int jj = 1; jj < s + 1; ++jj)
-        acc += dy.f[jj] * (jj == s ? kc : (double)static_cast<const KT *>(a.kq[jj + 1])[gq]);
+#pragma unroll
+      for (int jj = 1; jj < OC_MAXSTAGES; ++jj)
+        if (jj <= s) acc += dy.f[jj] * (jj == s ? kc : (double)static_cast<const KT *>(a.kq[jj + 1])[gq]);
       nxt = acc;
     } else if (!a.last) {
       nxt = MIX ? a.un_q[gq] + (double)v : (double)v;

@@ -45,6 +45,7 @@ struct StageArgs {
   int n_group;                 // cells processed by this launch
   const int *group_cells;      // their ids (NULL: identity starting at group_first)
   int group_first;
+  int uniform_nn;              // (p+1)^2 when every cell has degree p: offset = cell * uniform_nn
   const int *deg;              // [n_cells]
   const int *off;              // [n_cells] zeta offset (discharge: 2*off)
   const double *geo;           // [n_cells*11]: x0,y0,J00,J01,J10,J11,Ji00,Ji01,Ji10,Ji11,det

@@ -215,6 +215,20 @@ class OceanoOperator:
         return {"one_launch": bool(out[0]), "one_launch_warps": int(out[1]),
                 "group_warps": {p: int(out[1 + p]) for p in range(1, 5)}, "tuned": bool(out[6])}
 
+    def compute_errors_hydro(self, time, height, discharge):
+        """OceanDG.h:2380-2459 against the vortex set by set_vortex: (depth, discharge)."""
+        out = np.zeros(2)
+        check(lib().oc_errors_vortex(self.h, time, _ptr(height), _ptr(discharge),
+                                     _memory(height, discharge), _ptr(out)), self.h)
+        return out
+
+    def prepare_for_conservative_coarsening(self, mark, height):
+        """OceanDG.h:2732-2778 on the cells with mark != 0 (height updated in place)."""
+        mem = OC_MEM_DEVICE if _is_device(height) else OC_MEM_HOST
+        if mem == OC_MEM_HOST:
+            mark = np.ascontiguousarray(mark, np.uint8)
+        check(lib().oc_conservative_coarsening(self.h, _ptr(mark), _ptr(height), mem), self.h)
+
     def synchronize(self):
         check(lib().oc_synchronize(self.h), self.h)
 

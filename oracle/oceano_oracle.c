@@ -1375,6 +1375,80 @@ void oc_oracle_vorticity(void *h, const double *u, int n_q_1d, float *out)
   }
 }
 
+/* OceanDG.h:2380-2459 compute_errors_hydro with the travelling vortex as the
+   exact solution: out[0] = sqrt(sum_cells int (depth(f0, zb) - depth(zeta_h, zb))^2),
+   out[1] = sqrt(sum_cells int sum_d (f_{d+1} depth(f0, zb) - q_h,d)^2), on the
+   cell Gauss rule (n_points_1d = floor(1.5 p) + 1), zb from the cell static data
+   (data_quadrature_cell_0, component 0); cells summed in order. */
+void oc_oracle_errors_vortex(void *h, double t, const double *z, const double *q, double *out)
+{
+  oracle_t *o = (oracle_t *)h;
+  double e0 = 0., e1 = 0.;
+  for (int c = 0; c < o->n_cells; ++c) {
+    const shape_t *s = &o->sh[o->deg[c]];
+    const int N = s->N, n = N * N, Q = s->Q;
+    const double *J = o->jac + 11 * c;
+    double zv[MAXQ * MAXQ], q0[MAXQ * MAXQ], q1[MAXQ * MAXQ];
+    eval2d(N, Q, s->BQ, s->BQ, z + o->off[c], zv);
+    eval2d(N, Q, s->BQ, s->BQ, q + 2 * o->off[c], q0);
+    eval2d(N, Q, s->BQ, s->BQ, q + 2 * o->off[c] + n, q1);
+    const double *sd = o->sd0 ? o->sd0 + o->sdo0[c] : NULL;
+    double c0 = 0., c1 = 0.;
+    for (int qy = 0; qy < Q; ++qy)
+      for (int qx = 0; qx < Q; ++qx) {
+        const int k = qy * Q + qx;
+        double xi[2] = {s->xQ[qx], s->xQ[qy]}, x[2];
+        map_point(J, xi, x);
+        const double zb = sd ? sd[5 * k] : 0.;
+        const double f0 = vortex_value(o, x[0], x[1], t, 0);
+        const double hq = depth(&o->prm, f0, zb);
+        const double jxw = s->wQ[qx] * s->wQ[qy] * J[10];
+        const double d0 = hq - depth(&o->prm, zv[k], zb);
+        const double a = vortex_value(o, x[0], x[1], t, 1) * hq - q0[k];
+        const double b = vortex_value(o, x[0], x[1], t, 2) * hq - q1[k];
+        c0 += d0 * d0 * jxw;
+        c1 += (a * a + b * b) * jxw;
+      }
+    e0 += c0;
+    e1 += c1;
+  }
+  out[0] = sqrt(e0);
+  out[1] = sqrt(e1);
+}
+
+/* OceanDG.h:2732-2778 prepare_for_conservative_coarsening: on every cell marked
+   for the degree p -> 0 transfer, all nodal zeta values become the average of
+   zeta over the wet Gauss-Lobatto (p+2) points (wet: zeta > -zb, zb from
+   data_quadrature_cell_1); cells without a wet point are left unchanged. */
+void oc_oracle_conservative_coarsening(void *h, const unsigned char *mark, double *z)
+{
+  oracle_t *o = (oracle_t *)h;
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < o->n_cells; ++c) {
+    if (!mark[c]) continue;
+    const shape_t *s = &o->sh[o->deg[c]];
+    const int N = s->N, n = N * N, G = s->G;
+    const double *J = o->jac + 11 * c;
+    double zv[MAXF * MAXF];
+    eval2d(N, G, s->BG, s->BG, z + o->off[c], zv);
+    const double *sd = o->sd1 ? o->sd1 + o->sdo1[c] : NULL;
+    double area = 0., integral = 0.;
+    for (int gy = 0; gy < G; ++gy)
+      for (int gx = 0; gx < G; ++gx) {
+        const int k = gy * G + gx;
+        const double zb = sd ? sd[k] : 0.;
+        const double mask = zv[k] <= -zb ? 0. : 1.;
+        const double jxw = s->wG[gx] * s->wG[gy] * J[10];
+        area += mask * jxw;
+        integral += zv[k] * mask * jxw;
+      }
+    if (area > 0.) {
+      const double v = integral * (1. / area);
+      for (int i = 0; i < n; ++i) z[o->off[c] + i] = v;
+    }
+  }
+}
+
 int oc_oracle_num_threads(void)
 {
 #ifdef _OPENMP

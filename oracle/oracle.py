@@ -66,6 +66,9 @@ def lib():
         L.oc_oracle_project_vortex.argtypes = [C.c_void_p, C.c_double, _dp, _dp]
         L.oc_oracle_velocity_field.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.oc_oracle_vorticity.argtypes = [C.c_void_p, _dp, C.c_int, _fp]
+        L.oc_oracle_errors_vortex.argtypes = [C.c_void_p, C.c_double, _dp, _dp, _dp]
+        L.oc_oracle_conservative_coarsening.argtypes = [C.c_void_p,
+                                                        np.ctypeslib.ndpointer(np.uint8), _dp]
         L.oc_oracle_num_threads.restype = C.c_int
     return _lib
 
@@ -161,6 +164,16 @@ class Oracle:
         u = np.zeros(2 * self.n)
         lib().oc_oracle_velocity_field(self.h, z, q, u)
         return u
+
+    def errors_vortex(self, z, q, t):
+        out = np.zeros(2)
+        lib().oc_oracle_errors_vortex(self.h, t, z, q, out)
+        return out
+
+    def conservative_coarsening(self, mark, z):
+        z = np.ascontiguousarray(z, np.float64).copy()
+        lib().oc_oracle_conservative_coarsening(self.h, np.ascontiguousarray(mark, np.uint8), z)
+        return z
 
     def vorticity(self, u, n_q_1d):
         out = np.zeros(self.mesh.n_cells, np.float32)
