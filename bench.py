@@ -86,9 +86,7 @@ class Workload:
             self.oracle_kw = dict(friction=2, bcs=W.CHANNEL_BCS)
         elif name == "ensemble":
             self.op_m, self.z0, self.q0, members, meshes = W.ensemble(64, "mixed")
-            from oceano_gb300.operator import OceanoOperator
-            self.op_d = OceanoOperator(self.op_m.mesh, precision="fp64")
-            self.op_d.set_wall_boundary(0)
+            self.op_d = W.vortex_operator(self.op_m.mesh, "fp64", members[0]["vortex"])
             self.desc = (f"64-member vortex ensemble, {self.op_d.mesh.n_cells} cells "
                          f"(5k-40k per member, p=1,2), one operator, SSP-RK3 step")
             self.oracle_kw = dict(bcs={0: ("wall",)})
@@ -128,11 +126,8 @@ class Workload:
 
 
 def make_op(mesh, vx, precision):
-    from oceano_gb300.operator import OceanoOperator
-    op = OceanoOperator(mesh, precision=precision, zeta_reference=1.0 if precision == "mixed" else 0.0)
-    op.set_wall_boundary(0)
-    op.set_vortex(*vx)
-    return op
+    from oceano_gb300.workloads import vortex_operator
+    return vortex_operator(mesh, precision, vx)
 
 
 def algorithmic_bytes(n_dofs_var, n_cells, mixed, static_bytes=0):

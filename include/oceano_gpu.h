@@ -229,6 +229,15 @@ oc_status oc_project_vortex(oc_op *op, double time, double *height, double *disc
 oc_status oc_transport_speed_noalloc(oc_op *op, const double *height, const double *discharge,
                                      double *speed);
 
+/* Reference state of the mixed form (no reference counterpart; ignored by the
+ * FP64 form): a constant depth h_ref = zeta_ref + zb_ref and discharge (qx, qy),
+ * typically the undisturbed background of the run (h0, h0 u_inf).  The FP32
+ * stage inputs hold q - q_ref and every flux is evaluated minus its value at
+ * the reference state, which has no weak divergence: exact arithmetic is
+ * unchanged, while FP32 rounding scales with the deviation.  The values are
+ * rounded to FP32-representable numbers.  Default: depth 1, discharge 0. */
+oc_status oc_set_reference_state(oc_op *op, double depth, double qx, double qy);
+
 /* Launch configuration of the stage kernels (no reference counterpart: deal.II's
  * MatrixFree loops have no launch shape).  OC_LAUNCH_AUTO (default) times, at the
  * first oc_perform_time_step, one launch per degree group with 1, 2 or 4 warps

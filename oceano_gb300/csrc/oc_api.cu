@@ -146,6 +146,8 @@ struct oc_op {
   double *ts_z = nullptr, *ts_q = nullptr;  // solution when the caller passes host memory
   double *ts_aux = nullptr;
   float *ts_unzf = nullptr, *ts_unqf = nullptr;  // FP32 copies of u^n (mixed time step)
+  // mixed form reference state (FP32-representable values)
+  double ref_h = 1.0, ref_q[2] = {0.0, 0.0};
   // launch configuration: OC_LAUNCH_AUTO tunes it at the first time step
   int launch_mode = OC_LAUNCH_AUTO;
   int tuned = 0;
@@ -236,6 +238,16 @@ const char *oc_last_error(const oc_op *op) { return op ? op->err.c_str() : "null
 int64_t oc_n_dofs(const oc_op *op) { return op ? op->n_dofs : -1; }
 int64_t oc_launch_count(const oc_op *op) { return op ? op->launches : -1; }
 void *oc_stream(oc_op *op) { return op ? (void *)op->stream : nullptr; }
+
+oc_status oc_set_reference_state(oc_op *op, double depth, double qx, double qy) {
+  if (!op || !(depth > 0.) || !std::isfinite(qx) || !std::isfinite(qy))
+    return OC_ERR_INVALID_ARG;
+  op->ref_h = (double)(float)depth;
+  op->ref_q[0] = (double)(float)qx;
+  op->ref_q[1] = (double)(float)qy;
+  if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
+  return OC_OK;
+}
 
 oc_status oc_set_launch_mode(oc_op *op, int32_t mode) {
   if (!op) return OC_ERR_INVALID_ARG;
@@ -603,6 +615,16 @@ static void fill_common(oc_op *op, StageArgs &a) {
   a.cfrec = op->d_cfrec;
   a.geof = op->prm.precision == OC_PREC_MIXED ? op->d_geof : nullptr;
   a.uniform_nn = op->uniform_deg ? (op->uniform_deg + 1) * (op->uniform_deg + 1) : 0;
+  a.h_ref = op->ref_h;
+  a.q_ref[0] = op->ref_q[0];
+  a.q_ref[1] = op->ref_q[1];
+  a.ref.hr = (float)op->ref_h;
+  a.ref.qr0 = (float)op->ref_q[0];
+  a.ref.qr1 = (float)op->ref_q[1];
+  a.ref.ur0 = a.ref.qr0 / a.ref.hr;
+  a.ref.ur1 = a.ref.qr1 / a.ref.hr;
+  a.ref.rr0 = std::fmaf(-a.ref.ur0, a.ref.hr, a.ref.qr0);  // exact residual (IEEE fma)
+  a.ref.rr1 = std::fmaf(-a.ref.ur1, a.ref.hr, a.ref.qr1);
   a.dscratch = op->d_dscratch;
   a.cfsdo = (op->d_sd[3] || op->d_sd[4]) ? op->d_cfsdo : nullptr;
   const double cu = op->prm.threshold_wetdry;

@@ -52,6 +52,8 @@ __device__ __forceinline__ float m_exp(float x) { return expf(x); }
 __device__ __forceinline__ double m_exp(double x) { return exp(x); }
 __device__ __forceinline__ float m_log(float x) { return logf(x); }
 __device__ __forceinline__ double m_log(double x) { return log(x); }
+__device__ __forceinline__ float m_fma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double m_fma(double a, double b, double c) { return fma(a, b, c); }
 
 template <typename R>
 __device__ __forceinline__ R mx(R a, R b) { return a < b ? b : a; }  // std::max
@@ -122,6 +124,93 @@ __device__ __forceinline__ void face_flux(R g, R cu4, R zm, R qm0, R qm1, R zp, 
   Fa1 = R(0.5) * (hum1 * unm + hup1 * unp) + R(0.5) * lambda * (hum1 - hup1);
   const R s = g * R(0.25) * (hp + hm);
   const R sm = s * (cp - cm), sp = s * (cm - cp);
+  Pm0 = sm * n0; Pm1 = sm * n1;
+  Pp0 = sp * n0; Pp1 = sp * n1;
+}
+
+// ---------------------------------------------------------------------------
+// Mixed form: discharge carried as a deviation from a constant reference state.
+// The FP32 state is (zeta - zeta_ref, q - q_r); depth = h_r + dh with
+// dh = (zeta - zeta_ref) + (zbe - h_r) (zbe = zb + zeta_ref).  The fluxes are
+// evaluated minus their value at the reference state (q_r, u_r): a constant
+// flux has no weak divergence (cell Gauss and face Gauss-Lobatto rules are
+// exact for it), so this changes nothing in exact arithmetic, but the FP32
+// rounding now scales with |q - q_r| instead of |q|.
+// ---------------------------------------------------------------------------
+// (RefStateF, oc_layout.h: set on the host, read from the kernel parameter bank)
+template <typename R>
+using RefState = RefStateF;
+
+// du = u - u_r for q = q_r + dq at depth h = h_r + dh (ShallowWater.h:322-336,
+// desingularised below Threshold_for_wetdry); also returns h.
+template <typename R>
+__device__ __forceinline__ void vel_dev(const RefState<R> &rf, R cu4, R dh, R dq0, R dq1, R &du0,
+                                        R &du1, R &h) {
+  h = mx<R>(rf.hr + dh, R(1e-12));
+  const R h2 = h * h, h4 = h2 * h2;
+  if (h4 >= cu4) {  // sqrt(2) h / sqrt(h^4 + max(h^4, cu^4)) = 1 / h
+    const R s = R(1) / h;
+    du0 = (dq0 + (rf.rr0 - rf.ur0 * dh)) * s;
+    du1 = (dq1 + (rf.rr1 - rf.ur1 * dh)) * s;
+  } else {
+    const R s = R(1.4142135623730951) * h / m_sqrt(h4 + cu4);
+    du0 = s * (rf.qr0 + dq0) - rf.ur0;
+    du1 = s * (rf.qr1 + dq1) - rf.ur1;
+  }
+}
+
+// face_flux on deviations: F - q_r.n, Fa - q_r (u_r.n), P unchanged.  zm, zp are
+// zeta - zeta_ref, dq* = q - q_r, zbm, zbp = zb + zeta_ref.
+template <typename R>
+__device__ __forceinline__ void face_flux_dev(const RefState<R> &rf, R g, R cu4, R zm, R dqm0,
+                                              R dqm1, R zp, R dqp0, R dqp1, R n0, R n1, R zbm,
+                                              R zbp, R &F, R &Fa0, R &Fa1, R &Pm0, R &Pm1,
+                                              R &Pp0, R &Pp1) {
+  const R dzbm = zbm - rf.hr, dzbp = zbp - rf.hr;
+  R dvm0, dvm1, hmo, dvp0, dvp1, hpo;  // own-bathymetry velocities and depths
+  vel_dev<R>(rf, cu4, zm + dzbm, dqm0, dqm1, dvm0, dvm1, hmo);
+  vel_dev<R>(rf, cu4, zp + dzbp, dqp0, dqp1, dvp0, dvp1, hpo);
+  const R vm0 = rf.ur0 + dvm0, vm1 = rf.ur1 + dvm1, vp0 = rf.ur0 + dvp0, vp1 = rf.ur1 + dvp1;
+  const R lm = m_abs(vm0 * n0 + vm1 * n1) + m_sqrt(g * hmo);
+  const R lp = m_abs(vp0 * n0 + vp1 * n1) + m_sqrt(g * hpo);
+  const R lambda = mx<R>(lp, lm);
+  const R zbs = mn<R>(zbm, zbp), dzbs = zbs - rf.hr;
+  const R dhm = zm + dzbs, dhp = zp + dzbs;
+  const R hm = mx<R>(rf.hr + dhm, R(1e-12)), hp = mx<R>(rf.hr + dhp, R(1e-12));
+  // reconstructed discharge deviations hu - q_r, hu = h_s u (hydrostatic reconstruction)
+  R dhum0, dhum1, dhup0, dhup1;
+  const R cu = R(1e-12);
+  if (hmo * hmo * hmo * hmo >= cu4 && hm > cu) {  // u = q / h_own: hu = (h_s / h_own) q
+    const R r = hm / hmo, c = (dzbs - dzbm) / hmo;
+    dhum0 = r * dqm0 + rf.qr0 * c;
+    dhum1 = r * dqm1 + rf.qr1 * c;
+  } else {
+    dhum0 = hm * vm0 - rf.qr0;
+    dhum1 = hm * vm1 - rf.qr1;
+  }
+  if (hpo * hpo * hpo * hpo >= cu4 && hp > cu) {
+    const R r = hp / hpo, c = (dzbs - dzbp) / hpo;
+    dhup0 = r * dqp0 + rf.qr0 * c;
+    dhup1 = r * dqp1 + rf.qr1 * c;
+  } else {
+    dhup0 = hp * vp0 - rf.qr0;
+    dhup1 = hp * vp1 - rf.qr1;
+  }
+  const R cm = mx<R>(zm, -zbs), cp = mx<R>(zp, -zbs);
+  F = R(0.5) * ((dhum0 * n0 + dhum1 * n1) + (dhup0 * n0 + dhup1 * n1)) + R(0.5) * lambda * (cm - cp);
+  // advective flux: velocity recomputed from hu at the reconstructed depth
+  R dwm0, dwm1, dwp0, dwp1, hh;
+  vel_dev<R>(rf, cu4, dhm, dhum0, dhum1, dwm0, dwm1, hh);
+  vel_dev<R>(rf, cu4, dhp, dhup0, dhup1, dwp0, dwp1, hh);
+  const R dunm = dwm0 * n0 + dwm1 * n1, dunp = dwp0 * n0 + dwp1 * n1;
+  const R urn = rf.ur0 * n0 + rf.ur1 * n1;
+  // hu (w.n) - q_r (u_r.n) = q_r (dw.n) + d(hu) ((u_r + dw).n)
+  const R Xm0 = rf.qr0 * dunm + dhum0 * (urn + dunm), Xm1 = rf.qr1 * dunm + dhum1 * (urn + dunm);
+  const R Xp0 = rf.qr0 * dunp + dhup0 * (urn + dunp), Xp1 = rf.qr1 * dunp + dhup1 * (urn + dunp);
+  Fa0 = R(0.5) * (Xm0 + Xp0) + R(0.5) * lambda * (dhum0 - dhup0);
+  Fa1 = R(0.5) * (Xm1 + Xp1) + R(0.5) * lambda * (dhum1 - dhup1);
+  const R sg = g * R(0.25) * (hp + hm);
+  const R sm = sg * (cp - cm), sp = sg * (cm - cp);
   Pm0 = sm * n0; Pm1 = sm * n1;
   Pp0 = sp * n0; Pp1 = sp * n1;
 }
@@ -427,13 +516,22 @@ __device__ __noinline__ void boundary_flux(const StageArgs &a, int bid, int bkin
   const double e1 = fo < 2 ? sx : fo == 2 ? 0. : 1.;
   const double px = geo[0] + geo[2] * e0 + geo[3] * e1;
   const double py = geo[1] + geo[4] * e0 + geo[5] * e1;
+  // MIX: qm0, qm1 arrive as q - q_r; the ghost state is built on absolute values
+  // and its deviation kept exact where the ghost copies or reflects the inner state
+  const RefStateF &rf = a.ref;
+  const R dqm0 = qm0, dqm1 = qm1;
+  if constexpr (MIX) {
+    qm0 += rf.qr0;
+    qm1 += rf.qr1;
+  }
   const R un = qm0 * n0 + qm1 * n1;
   R zp = zm, qp0 = qm0, qp1 = qm1;
-  bool at_outflow = false;
+  bool at_outflow = false, ghost_abs = false;  // ghost_abs: deviation from the absolute ghost
   if (bkind == OC_BC_WALL_) {
     qp0 = qm0 - R(2.) * un * n0;
     qp1 = qm1 - R(2.) * un * n1;
   } else if (bkind == OC_BC_SUPIN_) {
+    ghost_abs = true;
     const double zd = bc_value(a, bid, px, py, 0);
     zp = (R)(zd - zref);
     const R hh = depth<R>(zp, zbm);
@@ -444,10 +542,12 @@ __device__ __noinline__ void boundary_flux(const StageArgs &a, int bid, int bkin
   } else if (bkind == OC_BC_HEIGHT_) {
     zp = (R)(bc_value(a, bid, px, py, 0) - zref);
   } else if (bkind == OC_BC_DISCHARGE_) {
+    ghost_abs = true;
     const R qn = (R)bc_value(a, bid, px, py, 1);
     qp0 = qn * -n0;
     qp1 = qn * -n1;
   } else if (bkind == OC_BC_ABSORB_) {
+    ghost_abs = true;
     const R zf = (R)(bc_value(a, bid, px, py, 0) - zref);
     const R hf = depth<R>(zf, zbm);
     const R qf0 = (R)bc_value(a, bid, px, py, 1) * hf;
@@ -464,11 +564,32 @@ __device__ __noinline__ void boundary_flux(const StageArgs &a, int bid, int bkin
     qp1 = ub * hd * n1;
   }
   R Pm0, Pm1, Pp0, Pp1;
-  face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbm, F, Fa0, Fa1, Pm0, Pm1, Pp0,
-               Pp1);
+  if constexpr (MIX) {  // fluxes minus the reference flux (q_r.n, q_r (u_r.n))
+    R dqp0 = dqm0 - R(2.) * un * n0, dqp1 = dqm1 - R(2.) * un * n1;  // wall
+    if (ghost_abs) {
+      dqp0 = qp0 - rf.qr0;
+      dqp1 = qp1 - rf.qr1;
+    } else if (bkind != OC_BC_WALL_) {  // ghost discharge = inner discharge
+      dqp0 = dqm0;
+      dqp1 = dqm1;
+    }
+    face_flux_dev<R>(rf, g, cu4, zm, dqm0, dqm1, zp, dqp0, dqp1, n0, n1, zbm, zbm, F, Fa0, Fa1,
+                     Pm0, Pm1, Pp0, Pp1);
+  } else {
+    face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbm, F, Fa0, Fa1, Pm0, Pm1,
+                 Pp0, Pp1);
+  }
   Fa0 += Pm0;
   Fa1 += Pm1;
-  if (at_outflow && un < R(-1e-12)) Fa0 = Fa1 = 0;
+  if (at_outflow && un < R(-1e-12)) {  // no advective or pressure flux through the outflow
+    if constexpr (MIX) {
+      const R urn = rf.ur0 * n0 + rf.ur1 * n1;
+      Fa0 = -rf.qr0 * urn;
+      Fa1 = -rf.qr1 * urn;
+    } else {
+      Fa0 = Fa1 = 0;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -543,6 +664,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   const double zref = MIX ? a.zeta_ref : 0.0;
   const R g = (R)a.g, cu4 = (R)a.cu4;
   const R zbe_flat = (R)zref;  // zb + zeta_ref where no bathymetry is given
+  // mixed form: discharge stored as q - q_r (reference state (h_r, q_r))
+  const RefStateF &rf = a.ref;
+  const double qref0 = MIX ? a.q_ref[0] : 0.0, qref1 = MIX ? a.q_ref[1] : 0.0;
 
   unsigned char *wbase = smem_raw + warp * D::template warp_bytes<R>();
   auto Rreg = [&](int j) { return reinterpret_cast<R *>(wbase + j * D::template bytes_r<R>()); };
@@ -605,8 +729,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     const int64_t oz = w_off[j] + d, oq = 2 * (int64_t)w_off[j] + d;
     R *Uj = Rreg(j);
     Uj[d] = load_in<RIN, R>(a.rz, oz, zref);
-    Uj[NN + d] = load_in<RIN, R>(a.rq, oq, 0.0);
-    Uj[2 * NN + d] = load_in<RIN, R>(a.rq, oq + NN, 0.0);
+    Uj[NN + d] = load_in<RIN, R>(a.rq, oq, qref0);
+    Uj[2 * NN + d] = load_in<RIN, R>(a.rq, oq + NN, qref1);
     if (!a.apply_mode) {
       R bprev = 0;  // sum_{j<s} f_j kz_j in the reference's order
 #pragma unroll
@@ -723,15 +847,24 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         // height: int q . grad(phi)   (mass_flux = q, ShallowWater.h:349-357)
         const R gz0 = (Ji00 * q0 + Ji01 * q1) * w, gz1 = (Ji10 * q0 + Ji11 * q1) * w;
         // discharge: advective flux (ShallowWater.h:378-403, nu = 0) and sources (:405-472)
-        R v0, v1;
-        velocity<R>(z, q0, q1, zb, cu4, v0, v1);
-        const R h = depth<R>(z, zb);
+        R v0, v1, h, F00, F01, F10, F11, qa0 = q0, qa1 = q1;
+        if constexpr (MIX) {  // q0, q1 are q - q_r: flux minus the reference flux q_r u_r
+          R du0, du1;
+          vel_dev<R>(rf, cu4, z + (zb - rf.hr), q0, q1, du0, du1, h);
+          v0 = rf.ur0 + du0; v1 = rf.ur1 + du1;
+          qa0 = rf.qr0 + q0; qa1 = rf.qr1 + q1;
+          F00 = rf.qr0 * du0 + q0 * v0; F01 = rf.qr0 * du1 + q0 * v1;
+          F10 = rf.qr1 * du0 + q1 * v0; F11 = rf.qr1 * du1 + q1 * v1;
+        } else {
+          velocity<R>(z, q0, q1, zb, cu4, v0, v1);
+          h = depth<R>(z, zb);
+          F00 = q0 * v0; F01 = q0 * v1; F10 = q1 * v0; F11 = q1 * v1;
+        }
         const R dz0 = Ji00 * zx + Ji10 * zy, dz1 = Ji01 * zx + Ji11 * zy;
         R fr0 = 0, fr1 = 0;
         if (a.friction && !split) friction<R>(a.friction, g, v0, v1, cf, h, fr0, fr1);
-        const R s0 = -g * h * dz0 - fr0 + w0 + fc * q1;
-        const R s1 = -g * h * dz1 - fr1 + w1 - fc * q0;
-        const R F00 = q0 * v0, F01 = q0 * v1, F10 = q1 * v0, F11 = q1 * v1;
+        const R s0 = -g * h * dz0 - fr0 + w0 + fc * qa1;
+        const R s1 = -g * h * dz1 - fr1 + w1 - fc * qa0;
         const R g00 = (Ji00 * F00 + Ji01 * F01) * w, g01 = (Ji10 * F00 + Ji11 * F01) * w;
         const R g10 = (Ji00 * F10 + Ji01 * F11) * w, g11 = (Ji10 * F10 + Ji11 * F11) * w;
         const R sv0 = s0 * w, sv1 = s1 * w;
@@ -822,7 +955,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         if (MIX && sd0e) { zb = (R)sd0e[5 * k]; cf = (R)sd0e[5 * k + 1]; }
         else if (!MIX && sd0) { zb = (R)sd0[5 * k]; cf = (R)sd0[5 * k + 1]; }
         R v0, v1, fr0 = 0, fr1 = 0;
-        velocity<R>(z, q0, q1, zb, cu4, v0, v1);
+        if constexpr (MIX) velocity<R>(z, rf.qr0 + q0, rf.qr1 + q1, zb, cu4, v0, v1);
+        else velocity<R>(z, q0, q1, zb, cu4, v0, v1);
         if (a.friction) friction<R>(a.friction, g, v0, v1, cf, depth<R>(z, zb), fr0, fr1);
         const R w = tb.wQ[t] * tb.wQ[qy] * det;
         const R st0 = -fr0 * w, st1 = -fr1 * w;
@@ -872,8 +1006,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         const int d = face_dof(Nn, r.nb_face(), i);
         const int64_t oz = r.other, oq = 2 * (int64_t)r.other;
         NB[(sl * 3 + 0) * OC_MAXN + i] = load_in<RIN, R>(a.rz, oz + d, zref);
-        NB[(sl * 3 + 1) * OC_MAXN + i] = load_in<RIN, R>(a.rq, oq + d, 0.0);
-        NB[(sl * 3 + 2) * OC_MAXN + i] = load_in<RIN, R>(a.rq, oq + Nn * Nn + d, 0.0);
+        NB[(sl * 3 + 1) * OC_MAXN + i] = load_in<RIN, R>(a.rq, oq + d, qref0);
+        NB[(sl * 3 + 2) * OC_MAXN + i] = load_in<RIN, R>(a.rq, oq + Nn * Nn + d, qref1);
       }
     }
   }
@@ -944,8 +1078,12 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
               zbm = (R)a.sdf[sdo + 2 * k]; zbp = (R)a.sdf[sdo + 2 * k + 1];
             }
             R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
-            face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1, Pm0,
-                         Pm1, Pp0, Pp1);
+            if constexpr (MIX)
+              face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0,
+                               Fa1, Pm0, Pm1, Pp0, Pp1);
+            else
+              face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1,
+                           Pm0, Pm1, Pp0, Pp1);
             const R jxw = fw * len;
             const R sg = side ? R(1) : R(-1);
             FV[k] = sg * F * jxw;
@@ -981,8 +1119,12 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
             zbm = (R)a.sdf[sdo + 2 * k]; zbp = (R)a.sdf[sdo + 2 * k + 1];
           }
           R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
-          face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1, Pm0,
-                       Pm1, Pp0, Pp1);
+          if constexpr (MIX)
+            face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1,
+                             Pm0, Pm1, Pp0, Pp1);
+          else
+            face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1, Pm0,
+                         Pm1, Pp0, Pp1);
           const R jxw = tb.wF[nf][k] * len;
           if (side == 0) {
             FV[ko] = -F * jxw;
@@ -1346,7 +1488,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         if (MIX && sd2e) { zb = (R)sd2e[2 * k]; cf = (R)sd2e[2 * k + 1]; }
         else if (!MIX && sd2) { zb = (R)sd2[2 * k]; cf = (R)sd2[2 * k + 1]; }
         R u0, u1;
-        velocity<R>(vz, v0, v1, zb, cu4, u0, u1);
+        if constexpr (MIX) velocity<R>(vz, rf.qr0 + v0, rf.qr1 + v1, zb, cu4, u0, u1);
+        else velocity<R>(vz, v0, v1, zb, cu4, u0, u1);
         const R jf = friction_jac<R>(a.friction, g, u0, u1, cf, depth<R>(vz, zb));
         const R jxw = tb.wM[t] * tb.wM[qy] * det;
         coef[qy] = R(1) / jxw;
@@ -1537,7 +1680,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       nxt = a.un_q[gq] + (double)v;
     }
     if (a.out_q) a.out_q[gq] = nxt;
-    if (MIX && a.out_rq) a.out_rq[gq] = (float)nxt;
+    if (MIX && a.out_rq) a.out_rq[gq] = (float)(nxt - (d < NN ? qref0 : qref1));
   }
 }
 

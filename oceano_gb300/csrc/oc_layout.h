@@ -38,6 +38,12 @@ struct StageDyn {
   double fm, time;
 };
 
+// FP32 reference state of the mixed form: depth, discharge, velocity q/h and the
+// residual q - u h of the rounded pair (computed with one fused multiply-add).
+struct RefStateF {
+  float hr, qr0, qr1, ur0, ur1, rr0, rr1;
+};
+
 // Face references of a cell slot: >= 0: 2*inner_face + side (0 minus, 1 plus);
 // < -1: boundary face b encoded as -(b+2); -1: empty.
 struct StageArgs {
@@ -83,6 +89,10 @@ struct StageArgs {
   // per (launch-wide warp, team) slot, OC_MAXCPW slots per warp (only cells that
   // are not fully wet touch it)
   double *dscratch;
+  // mixed form: reference state (depth h_ref, discharge q_ref); the FP32 discharge
+  // is q - q_ref and the fluxes are evaluated minus their reference value
+  double h_ref, q_ref[2];
+  RefStateF ref;  // the same state in FP32 with u_ref = q_ref / h_ref (read from the parameter bank)
   // one-launch hp stage (stage_kernel_hp): per degree p the first block, the
   // number of blocks, the cells and the cell list of the group
   int hp_first_block[OC_MAXDEG + 1], hp_blocks[OC_MAXDEG + 1], hp_n[OC_MAXDEG + 1];

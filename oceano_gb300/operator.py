@@ -203,6 +203,11 @@ class OceanoOperator:
         mem = _memory(height, discharge)
         check(lib().oc_project_vortex(self.h, time, _ptr(height), _ptr(discharge), mem), self.h)
 
+    # ---- mixed form: reference state (no reference counterpart) ----------------------
+    def set_reference_state(self, depth=1.0, discharge=(0.0, 0.0)):
+        """Background (depth, discharge) the FP32 deviations are taken from."""
+        check(lib().oc_set_reference_state(self.h, depth, discharge[0], discharge[1]), self.h)
+
     # ---- launch configuration (GB300-specific; no reference counterpart) -------------
     def set_launch_mode(self, mode: str):
         """"auto" (tuned at the first time step), "per_group" or "one" (hp meshes)."""

@@ -47,13 +47,25 @@ def apply_bcs(op, bcs):
             op.set_boundary(bid, kind, "constant", spec[1] if len(spec) > 1 else (0, 0, 0))
 
 
+def vortex_operator(mesh, precision, vx=None):
+    """Operator of the vortex runs: walls (id 0), the vortex data; the mixed form
+    measures zeta and q from the undisturbed background (depth h0, discharge
+    h0 u_inf)."""
+    vx = vx or vortex_params()
+    op = OceanoOperator(mesh, precision=precision,
+                        zeta_reference=vx[0] if precision == "mixed" else 0.0)
+    if precision == "mixed":
+        op.set_reference_state(vx[0], (vx[0] * vx[1], 0.0))
+    op.set_wall_boundary(0)
+    op.set_vortex(*vx)
+    return op
+
+
 def vortex(refine=4, degree=3, precision="fp64"):
     """Travelling vortex on [0,2]x[0,1], periodic in x, walls in y."""
     mesh = vortex_mesh(refine, degree)
     vx = vortex_params()
-    op = OceanoOperator(mesh, precision=precision,
-                        zeta_reference=1.0 if precision == "mixed" else 0.0)
-    op.set_wall_boundary(0)
+    op = vortex_operator(mesh, precision, vx)
     op.set_vortex(*vx)
     n = op.n_dofs
     z, q = np.zeros(n), np.zeros(2 * n)
@@ -65,10 +77,7 @@ def hp_vortex(precision="mixed", target=60000, seed=20261203):
     """The vortex on the seeded random hp mesh (degrees 1-4, hanging faces)."""
     mesh = random_hp_mesh(seed=seed, target=target)
     vx = vortex_params()
-    op = OceanoOperator(mesh, precision=precision,
-                        zeta_reference=1.0 if precision == "mixed" else 0.0)
-    op.set_wall_boundary(0)
-    op.set_vortex(*vx)
+    op = vortex_operator(mesh, precision, vx)
     n = op.n_dofs
     z, q = np.zeros(n), np.zeros(2 * n)
     op.project_vortex(0.0, z, q)
@@ -82,6 +91,8 @@ def channel(precision="fp64", nx=250, ny=10, degree=2, lake=False):
     (`lake=True`): walls everywhere, zeta = 0, q = 0."""
     mesh = channel_mesh(degree, nx, ny)
     op = OceanoOperator(mesh, friction="manning", precision=precision)
+    if precision == "mixed":  # background: 2 m depth at rest level, the inflow discharge
+        op.set_reference_state(2.0, (0.0 if lake else CHANNEL_Q_IN, 0.0))
     apply_bcs(op, LAKE_BCS if lake else CHANNEL_BCS)
     op.initialize_data_at_quadrature(channel_problem_data(CHANNEL_MANNING))
     z, q = uniform_state(mesh, 0.0, (0.0, 0.0) if lake else (CHANNEL_Q_IN, 0.0))
@@ -134,8 +145,6 @@ def ensemble(n=64, precision="mixed", seed0=1000, members=None):
     members = members or ensemble_members(n, seed0)
     meshes = [member_mesh(m) for m in members]
     mesh = concatenate_meshes(meshes)
-    op = OceanoOperator(mesh, precision=precision,
-                        zeta_reference=1.0 if precision == "mixed" else 0.0)
-    op.set_wall_boundary(0)
+    op = vortex_operator(mesh, precision, members[0]["vortex"])
     zs, qs = zip(*[vortex_nodal_state(m, mm["vortex"]) for m, mm in zip(meshes, members)])
     return op, np.concatenate(zs), np.concatenate(qs), members, meshes

@@ -20,7 +20,7 @@ def rel(a, b):
     return np.linalg.norm(a - b) / (n if n > 0 else 1.0)
 
 
-def setup(name, precision="fp64", batch=1, zeta_reference=0.0):
+def setup(name, precision="fp64", batch=1, zeta_reference=0.0, reference_state=None):
     from oceano_gb300.operator import OceanoOperator
     mesh_f, bcs, pdata, friction = CASES[name]
     mesh = mesh_f()
@@ -35,6 +35,8 @@ def setup(name, precision="fp64", batch=1, zeta_reference=0.0):
         else:
             op.set_boundary(b, spec[0])
     op.set_vortex(*VORTEX)
+    if reference_state is not None:
+        op.set_reference_state(*reference_state)
     if pdata is not None:
         arrs = static_arrays(orc, pdata)
         orc.set_static(*arrs)
@@ -145,13 +147,21 @@ def test_ark_stage_fp64(gpu_lib, name, stage):
         assert rel(g["nq"], o["nq"]) < TOL_FP64
 
 
+# reference states of the mixed form: none (q_r = 0) and a background flow that
+# is not aligned with the mesh (exercises every deviation term)
+REF_STATES = {"no_ref": None, "ref": (1.0, (0.8, 0.3))}
+
+
+@pytest.mark.parametrize("ref", sorted(REF_STATES))
 @pytest.mark.parametrize("name", ["vortex_p1", "vortex_p3", "vortex_p4", "hanging_p2",
-                                  "mixed_degree", "hanging_p3_bathy"])
-def test_mixed_stage_error(gpu_lib, name):
+                                  "mixed_degree", "hanging_p3_bathy", "open_bcs_p2",
+                                  "absorbing_p3", "discharge_in_p2"])
+def test_mixed_stage_error(gpu_lib, name, ref):
     """Mixed form vs the FP64 oracle on wet states: stage output within 1e-6
     relative L2 (FP32 bulk), residual registers within 1e-4 (FP32 rounding of
     a residual that is itself a difference of O(1) fluxes)."""
-    mesh, orc, op = setup(name, precision="mixed", zeta_reference=1.0)
+    mesh, orc, op = setup(name, precision="mixed", zeta_reference=1.0,
+                          reference_state=REF_STATES[ref])
     r = run_erk_stage(orc, op, 1, np.array([0.001, 0.001]), seed=9, k_amp=1e-4)
     o, g = r["oracle"], r["gpu"]
     assert rel(g["nz"], o["nz"]) < 1e-6
@@ -175,17 +185,25 @@ def test_mixed_trajectory(gpu_lib, name):
     oracle: relative L2 state error <= 1e-6."""
     mesh, orc, op = setup(name, precision="mixed", zeta_reference=1.0)
     _, _, op64 = setup(name)
+    _, _, opr = setup(name, precision="mixed", zeta_reference=1.0,
+                      reference_state=(1.0, (1.0, 0.0)))  # the vortex background
     z0, q0 = orc.project_vortex(0.0)
     dt = 0.075 / orc.transport_speed(z0, q0)  # stable SSP-RK3 Courant number up to p = 4
     zo, qo = z0.copy(), q0.copy()
     zm, qm = z0.copy(), q0.copy()
     zd, qd = z0.copy(), q0.copy()
+    zr, qr = z0.copy(), q0.copy()
     for it in range(10):
         O.erk_step(orc, TAB["a"], TAB["b"], TAB["c"], it * dt, dt, zo, qo)
         op.perform_time_step("ssp33", it * dt, dt, zm, qm)
         op64.perform_time_step("ssp33", it * dt, dt, zd, qd)
+        opr.perform_time_step("ssp33", it * dt, dt, zr, qr)
     assert rel(zd, zo) < 1e-12 and rel(qd, qo) < 1e-12
     assert rel(zm, zo) < 1e-6 and rel(qm, qo) < 5e-6
+    # deviations from the background: the FP32 error of the discharge drops (its
+    # rounding no longer scales with |q| ~ 1 but with |q - q_r| ~ 0.1)
+    assert rel(zr, zo) < 1e-6 and rel(qr, qo) < 1e-6
+    assert rel(qr, qo) < 0.5 * rel(qm, qo)
 
 
 @pytest.mark.parametrize("name", ["vortex_p1", "hanging_p2", "mixed_degree", "hanging_p3_bathy"])
