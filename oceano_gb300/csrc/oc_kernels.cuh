@@ -142,34 +142,60 @@ template <typename R>
 using RefState = RefStateF;
 
 // du = u - u_r for q = q_r + dq at depth h = h_r + dh (ShallowWater.h:322-336,
-// desingularised below Threshold_for_wetdry); also returns h.
+// desingularised below Threshold_for_wetdry); also returns h and 1/h on wet
+// points (wet = h^4 >= cu^4, where the velocity is q / h; rh = 0 otherwise).
 template <typename R>
 __device__ __forceinline__ void vel_dev(const RefState<R> &rf, R cu4, R dh, R dq0, R dq1, R &du0,
-                                        R &du1, R &h) {
+                                        R &du1, R &h, R &rh) {
   h = mx<R>(rf.hr + dh, R(1e-12));
   const R h2 = h * h, h4 = h2 * h2;
   if (h4 >= cu4) {  // sqrt(2) h / sqrt(h^4 + max(h^4, cu^4)) = 1 / h
-    const R s = R(1) / h;
-    du0 = (dq0 + (rf.rr0 - rf.ur0 * dh)) * s;
-    du1 = (dq1 + (rf.rr1 - rf.ur1 * dh)) * s;
+    rh = R(1) / h;
+    du0 = (dq0 + (rf.rr0 - rf.ur0 * dh)) * rh;
+    du1 = (dq1 + (rf.rr1 - rf.ur1 * dh)) * rh;
   } else {
+    rh = R(0);
     const R s = R(1.4142135623730951) * h / m_sqrt(h4 + cu4);
     du0 = s * (rf.qr0 + dq0) - rf.ur0;
     du1 = s * (rf.qr1 + dq1) - rf.ur1;
   }
 }
+template <typename R>
+__device__ __forceinline__ void vel_dev(const RefState<R> &rf, R cu4, R dh, R dq0, R dq1, R &du0,
+                                        R &du1, R &h) {
+  R rh;
+  vel_dev<R>(rf, cu4, dh, dq0, dq1, du0, du1, h, rh);
+}
 
 // face_flux on deviations: F - q_r.n, Fa - q_r (u_r.n), P unchanged.  zm, zp are
-// zeta - zeta_ref, dq* = q - q_r, zbm, zbp = zb + zeta_ref.
+// zeta - zeta_ref, dq* = q - q_r, zbm, zbp = zb + zeta_ref.  flat: zbm == zbp
+// (no bathymetry data), where the hydrostatic reconstruction leaves the states
+// unchanged (hu = q, velocity recomputed from hu = velocity).
 template <typename R>
 __device__ __forceinline__ void face_flux_dev(const RefState<R> &rf, R g, R cu4, R zm, R dqm0,
                                               R dqm1, R zp, R dqp0, R dqp1, R n0, R n1, R zbm,
                                               R zbp, R &F, R &Fa0, R &Fa1, R &Pm0, R &Pm1,
-                                              R &Pp0, R &Pp1) {
+                                              R &Pp0, R &Pp1, bool flat = false) {
   const R dzbm = zbm - rf.hr, dzbp = zbp - rf.hr;
-  R dvm0, dvm1, hmo, dvp0, dvp1, hpo;  // own-bathymetry velocities and depths
-  vel_dev<R>(rf, cu4, zm + dzbm, dqm0, dqm1, dvm0, dvm1, hmo);
-  vel_dev<R>(rf, cu4, zp + dzbp, dqp0, dqp1, dvp0, dvp1, hpo);
+  R dvm0, dvm1, hmo, rhm, dvp0, dvp1, hpo, rhp;  // own-bathymetry velocities and depths
+  vel_dev<R>(rf, cu4, zm + dzbm, dqm0, dqm1, dvm0, dvm1, hmo, rhm);
+  vel_dev<R>(rf, cu4, zp + dzbp, dqp0, dqp1, dvp0, dvp1, hpo, rhp);
+  const R urn = rf.ur0 * n0 + rf.ur1 * n1;
+  if (flat) {
+    const R dunm = dvm0 * n0 + dvm1 * n1, dunp = dvp0 * n0 + dvp1 * n1;
+    const R lambda = mx<R>(m_abs(urn + dunp) + m_sqrt(g * hpo), m_abs(urn + dunm) + m_sqrt(g * hmo));
+    const R cm = mx<R>(zm, -zbm), cp = mx<R>(zp, -zbm);
+    F = R(0.5) * ((dqm0 * n0 + dqm1 * n1) + (dqp0 * n0 + dqp1 * n1)) + R(0.5) * lambda * (cm - cp);
+    const R Xm0 = rf.qr0 * dunm + dqm0 * (urn + dunm), Xm1 = rf.qr1 * dunm + dqm1 * (urn + dunm);
+    const R Xp0 = rf.qr0 * dunp + dqp0 * (urn + dunp), Xp1 = rf.qr1 * dunp + dqp1 * (urn + dunp);
+    Fa0 = R(0.5) * (Xm0 + Xp0) + R(0.5) * lambda * (dqm0 - dqp0);
+    Fa1 = R(0.5) * (Xm1 + Xp1) + R(0.5) * lambda * (dqm1 - dqp1);
+    const R sg = g * R(0.25) * (hpo + hmo);
+    const R sm = sg * (cp - cm), sp = sg * (cm - cp);
+    Pm0 = sm * n0; Pm1 = sm * n1;
+    Pp0 = sp * n0; Pp1 = sp * n1;
+    return;
+  }
   const R vm0 = rf.ur0 + dvm0, vm1 = rf.ur1 + dvm1, vp0 = rf.ur0 + dvp0, vp1 = rf.ur1 + dvp1;
   const R lm = m_abs(vm0 * n0 + vm1 * n1) + m_sqrt(g * hmo);
   const R lp = m_abs(vp0 * n0 + vp1 * n1) + m_sqrt(g * hpo);
@@ -180,16 +206,16 @@ __device__ __forceinline__ void face_flux_dev(const RefState<R> &rf, R g, R cu4,
   // reconstructed discharge deviations hu - q_r, hu = h_s u (hydrostatic reconstruction)
   R dhum0, dhum1, dhup0, dhup1;
   const R cu = R(1e-12);
-  if (hmo * hmo * hmo * hmo >= cu4 && hm > cu) {  // u = q / h_own: hu = (h_s / h_own) q
-    const R r = hm / hmo, c = (dzbs - dzbm) / hmo;
+  if (rhm > R(0) && hm > cu) {  // wet: u = q / h_own, hu = (h_s / h_own) q
+    const R r = hm * rhm, c = (dzbs - dzbm) * rhm;
     dhum0 = r * dqm0 + rf.qr0 * c;
     dhum1 = r * dqm1 + rf.qr1 * c;
   } else {
     dhum0 = hm * vm0 - rf.qr0;
     dhum1 = hm * vm1 - rf.qr1;
   }
-  if (hpo * hpo * hpo * hpo >= cu4 && hp > cu) {
-    const R r = hp / hpo, c = (dzbs - dzbp) / hpo;
+  if (rhp > R(0) && hp > cu) {
+    const R r = hp * rhp, c = (dzbs - dzbp) * rhp;
     dhup0 = r * dqp0 + rf.qr0 * c;
     dhup1 = r * dqp1 + rf.qr1 * c;
   } else {
@@ -203,7 +229,6 @@ __device__ __forceinline__ void face_flux_dev(const RefState<R> &rf, R g, R cu4,
   vel_dev<R>(rf, cu4, dhm, dhum0, dhum1, dwm0, dwm1, hh);
   vel_dev<R>(rf, cu4, dhp, dhup0, dhup1, dwp0, dwp1, hh);
   const R dunm = dwm0 * n0 + dwm1 * n1, dunp = dwp0 * n0 + dwp1 * n1;
-  const R urn = rf.ur0 * n0 + rf.ur1 * n1;
   // hu (w.n) - q_r (u_r.n) = q_r (dw.n) + d(hu) ((u_r + dw).n)
   const R Xm0 = rf.qr0 * dunm + dhum0 * (urn + dunm), Xm1 = rf.qr1 * dunm + dhum1 * (urn + dunm);
   const R Xp0 = rf.qr0 * dunp + dhup0 * (urn + dunp), Xp1 = rf.qr1 * dunp + dhup1 * (urn + dunp);
@@ -574,7 +599,7 @@ __device__ __noinline__ void boundary_flux(const StageArgs &a, int bid, int bkin
       dqp1 = dqm1;
     }
     face_flux_dev<R>(rf, g, cu4, zm, dqm0, dqm1, zp, dqp0, dqp1, n0, n1, zbm, zbm, F, Fa0, Fa1,
-                     Pm0, Pm1, Pp0, Pp1);
+                     Pm0, Pm1, Pp0, Pp1, true);
   } else {
     face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbm, F, Fa0, Fa1, Pm0, Pm1,
                  Pp0, Pp1);
@@ -1080,7 +1105,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
             R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
             if constexpr (MIX)
               face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0,
-                               Fa1, Pm0, Pm1, Pp0, Pp1);
+                               Fa1, Pm0, Pm1, Pp0, Pp1, a.sdfe == nullptr);
             else
               face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1,
                            Pm0, Pm1, Pp0, Pp1);
@@ -1121,7 +1146,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
           if constexpr (MIX)
             face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1,
-                             Pm0, Pm1, Pp0, Pp1);
+                             Pm0, Pm1, Pp0, Pp1, a.sdfe == nullptr);
           else
             face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1, Pm0,
                          Pm1, Pp0, Pp1);
