@@ -707,7 +707,6 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   R *X = ZN + NN;             // scratch tiles
   R *FV = X + D::XS;          // 3*FVS face point values
   R *NB = FV + 3 * FVS;       // neighbour traces [slot][var][node]
-  R *QB = RST;                // fast ERK path: discharge partial update (RST is ARK-only)
   auto Dreg = [&](int j) {  // FP64 team region of team j: shared (FP64 form) or global slot
     if constexpr (MIX)
       return a.dscratch + ((int64_t)(blockIdx.x * wpb + warp) * OC_MAXCPW + j) * OC_DSTRIDE;
@@ -754,8 +753,28 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     const int64_t oz = w_off[j] + d, oq = 2 * (int64_t)w_off[j] + d;
     R *Uj = Rreg(j);
     Uj[d] = load_in<RIN, R>(a.rz, oz, zref);
-    Uj[NN + d] = load_in<RIN, R>(a.rq, oq, qref0);
-    Uj[2 * NN + d] = load_in<RIN, R>(a.rq, oq + NN, qref1);
+    const R uq0 = load_in<RIN, R>(a.rq, oq, qref0), uq1 = load_in<RIN, R>(a.rq, oq + NN, qref1);
+    Uj[NN + d] = uq0;
+    Uj[2 * NN + d] = uq1;
+    // fast ERK path: the discharge part of the update known before this stage,
+    // QB = (last stage ? 0 : q^n) + sum_{j<s} f_j k_q[j+1] (RST region, unused by
+    // the explicit stage), loaded with the stage input so that the epilogue loads nothing
+    if (fast && !a.ark && !a.apply_mode) {
+      R qb0 = 0, qb1 = 0;
+#pragma unroll
+      for (int jj = 0; jj < OC_MAXSTAGES; ++jj)
+        if (jj < s) {
+          const KT *kqj = static_cast<const KT *>(a.kq[jj + 1]);
+          qb0 += fR[jj] * (R)kqj[oq];
+          qb1 += fR[jj] * (R)kqj[oq + NN];
+        }
+      if (!a.last) {
+        qb0 += s == 0 ? uq0 : (R)a.un_qf[oq];
+        qb1 += s == 0 ? uq1 : (R)a.un_qf[oq + NN];
+      }
+      Uj[6 * NN + d] = qb0;
+      Uj[7 * NN + d] = qb1;
+    }
     if (!a.apply_mode) {
       R bprev = 0;  // sum_{j<s} f_j kz_j in the reference's order
 #pragma unroll
@@ -769,22 +788,6 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       } else if constexpr (MIX) {
         Uj[9 * NN + d] = (R)(a.un_z[oz] - zref);
       }
-    }
-  }
-  // fast ERK path: the discharge part of the update known before this stage,
-  // QB = (last stage ? 0 : q^n) + sum_{j<s} f_j k_q[j+1], so that the epilogue loads nothing
-  if (fast && !a.ark && !a.apply_mode) {
-    __syncwarp();  // U of every team is written
-#pragma unroll 4
-    for (int e = lane; e < nvalid * 2 * NN; e += 32) {
-      const int j = e / (2 * NN), d = e - j * 2 * NN;
-      const int64_t gq = 2 * (int64_t)w_off[j] + d;
-      R qb = 0;
-#pragma unroll
-      for (int jj = 0; jj < OC_MAXSTAGES; ++jj)
-        if (jj < s) qb += fR[jj] * (R) static_cast<const KT *>(a.kq[jj + 1])[gq];
-      if (!a.last) qb += s == 0 ? Rreg(j)[NN + d] : (R)a.un_qf[gq];
-      Rreg(j)[3 * NN + 3 * NN + d] = qb;  // QB of team j
     }
   }
   __syncwarp();
@@ -1282,9 +1285,25 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   bool need_fp64 = !MIX;
   if (MIX) {
     const R wet_thr = (R)a.wet_threshold;
+    const unsigned team_mask = ((1u << T) - 1u) << (team * T);
+    // Without bathymetry data every Gauss-Lobatto point is wet when the nodal
+    // |zeta - zeta_ref| stay below (zb + zeta_ref - threshold) / Lambda (Lambda: the
+    // Lebesgue constant of the nodal basis at those points, with a margin for the
+    // FP32 evaluation); only warps where that bound fails evaluate the points.
+    const bool flat_zb = a.sd1e == nullptr;
+    const R wet_lim = flat_zb ? (zbe_flat - wet_thr) / tb.lebG * R(0.999) : R(0);
+    auto bound_wet = [&](const R *vals) {  // team-uniform
+      bool ok = flat_zb;
+      if (ok && member && t < N)
+#pragma unroll
+        for (int ix = 0; ix < N; ++ix) ok = ok && m_abs(vals[t * N + ix]) < wet_lim;
+      return (__ballot_sync(OC_FULL, member && !ok) & team_mask) == 0u;
+    };
     // wet check of u^n at the Gauss-Lobatto points (FP32 estimate)
     bool wet = true;
-    if (member && t < N) {
+    const bool sure0 = bound_wet(ZN);
+    const bool exact0 = __any_sync(OC_FULL, member && !sure0);
+    if (exact0 && member && t < N) {
 #pragma unroll
       for (int gx = 0; gx < G; ++gx) {
         R v = 0;
@@ -1295,7 +1314,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     }
     __syncwarp();
     const float *zb1e = a.sd1e ? a.sd1e + a.sdo1[cell] : nullptr;
-    if (member && t < G) {
+    if (exact0 && !sure0 && member && t < G) {
 #pragma unroll
       for (int gy = 0; gy < G; ++gy) {
         R v = 0;
@@ -1347,7 +1366,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     __syncwarp();
     // the closed form is the literal iteration only while every point stays wet:
     // check the result too, else redo the cell with the FP64 literal iteration
-    if (member && t < N) {
+    const bool sure1 = bound_wet(X + 4 * NT);
+    const bool exact1 = __any_sync(OC_FULL, member && !sure1);
+    if (exact1 && member && t < N) {
 #pragma unroll
       for (int gx = 0; gx < G; ++gx) {
         R v = 0;
@@ -1357,7 +1378,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       }
     }
     __syncwarp();
-    if (member && t < G) {
+    if (exact1 && !sure1 && member && t < G) {
 #pragma unroll
       for (int gy = 0; gy < G; ++gy) {
         R v = 0;

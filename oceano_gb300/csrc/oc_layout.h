@@ -22,6 +22,7 @@ struct DegTables {
   R wF[OC_MAXF + 1][OC_MAXF];             // Gauss-Lobatto nf weights
   R lump[OC_MAXN];                        // 1D lumped GL(p+2) mass
   R W1[OC_MAXN][OC_MAXN], W2[OC_MAXN][OC_MAXN], Gk[OC_MAXN][OC_MAXN];  // closed-form sweeps
+  R lebG;  // max over the Gauss-Lobatto (p+2)^2 points of sum_ij |phi_i(x) phi_j(y)|
 };
 
 template <typename R>

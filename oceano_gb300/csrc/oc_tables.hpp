@@ -173,10 +173,17 @@ inline void fill_tables(int p, int max_iter, DegTables<double> &t) {
       t.DQ[q][i] = lag_d(N, xN, i, xQ[q]);
     }
   }
+  double l1 = 0.;
   for (int q = 0; q < G; ++q) {
     t.wG[q] = wG[q];
-    for (int i = 0; i < N; ++i) t.BG[q][i] = lag(N, xN, i, xG[q]);
+    double s = 0.;
+    for (int i = 0; i < N; ++i) {
+      t.BG[q][i] = lag(N, xN, i, xG[q]);
+      s += std::fabs(t.BG[q][i]);
+    }
+    l1 = s > l1 ? s : l1;
   }
+  t.lebG = l1 * l1;  // tensor-product basis: the 2D sum factorises
   double S[OC_MAXN * OC_MAXN], Si[OC_MAXN * OC_MAXN];
   for (int q = 0; q < N; ++q) {
     t.wM[q] = wM[q];
