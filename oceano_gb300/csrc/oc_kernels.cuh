@@ -1059,6 +1059,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   for (int sl = 0; sl < 8; ++sl) {
     const FaceRec r = recs[sl];
     const int kind = member ? r.kind() : 0;
+    // second slots of conforming faces are empty in every team of most warps
+    if (!__any_sync(OC_FULL, kind != 0)) continue;
     const int fo = r.own_face();
     // DoF of node i on face fo: fbase + i * fstride (face_dof)
     const int fbase = fo == 0 ? 0 : fo == 1 ? N - 1 : fo == 2 ? 0 : (N - 1) * N;
