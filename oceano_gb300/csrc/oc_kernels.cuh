@@ -1084,20 +1084,38 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         const int sdo = a.cfsdo ? w_sdo[8 * team + sl] : 0;
         nfo = nf;
         tsel = side ? sub + 1 : 0;
-        if (sub < 0 && pn == P && orient == 0) {  // conforming, same degree: nf == G <= T
+        if (pn == P && orient == 0) {  // same degree: nf == G <= T, point k on both sides
           if (t < G) {
             const int k = t;
+            // trace rows: full face from registers; the coarse side of a hanging
+            // face (own on the plus side, the neighbour's on the minus side) reads
+            // the subface rows
+            const int nsel = side ? 0 : sub + 1;
+            R lo[N], ln[N];
+            if (tsel == 0) {
+#pragma unroll
+              for (int i = 0; i < N; ++i) lo[i] = frow[i];
+            } else {
+#pragma unroll
+              for (int i = 0; i < N; ++i) lo[i] = tb.F[tsel][G][k][i];
+            }
+            if (nsel == 0) {
+#pragma unroll
+              for (int i = 0; i < N; ++i) ln[i] = frow[i];
+            } else {
+#pragma unroll
+              for (int i = 0; i < N; ++i) ln[i] = tb.F[nsel][G][k][i];
+            }
             R zo_ = 0, qo0 = 0, qo1 = 0, zn = 0, qn0 = 0, qn1 = 0;
 #pragma unroll
             for (int i = 0; i < N; ++i) {
               const int d = fbase + i * fstride;
-              const R l = frow[i];
-              zo_ += l * U[d];
-              qo0 += l * U[NN + d];
-              qo1 += l * U[2 * NN + d];
-              zn += l * NB[(sl * 3 + 0) * OC_MAXN + i];
-              qn0 += l * NB[(sl * 3 + 1) * OC_MAXN + i];
-              qn1 += l * NB[(sl * 3 + 2) * OC_MAXN + i];
+              zo_ += lo[i] * U[d];
+              qo0 += lo[i] * U[NN + d];
+              qo1 += lo[i] * U[2 * NN + d];
+              zn += ln[i] * NB[(sl * 3 + 0) * OC_MAXN + i];
+              qn0 += ln[i] * NB[(sl * 3 + 1) * OC_MAXN + i];
+              qn1 += ln[i] * NB[(sl * 3 + 2) * OC_MAXN + i];
             }
             const R zm = side ? zn : zo_, qm0 = side ? qn0 : qo0, qm1 = side ? qn1 : qo1;
             const R zp = side ? zo_ : zn, qp0 = side ? qo0 : qn0, qp1 = side ? qo1 : qn1;
@@ -1134,11 +1152,14 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
             qo1 += l * U[2 * NN + d];
           }
           const int nsel = side ? 0 : sub + 1;
-          for (int i = 0; i < Nn; ++i) {  // neighbour trace
-            const R l = tn.F[nsel][nf][kn][i];
-            zn += l * NB[(sl * 3 + 0) * OC_MAXN + i];
-            qn0 += l * NB[(sl * 3 + 1) * OC_MAXN + i];
-            qn1 += l * NB[(sl * 3 + 2) * OC_MAXN + i];
+#pragma unroll
+          for (int i = 0; i < OC_MAXN; ++i) {  // neighbour trace (Nn <= OC_MAXN nodes)
+            if (i < Nn) {
+              const R l = tn.F[nsel][nf][kn][i];
+              zn += l * NB[(sl * 3 + 0) * OC_MAXN + i];
+              qn0 += l * NB[(sl * 3 + 1) * OC_MAXN + i];
+              qn1 += l * NB[(sl * 3 + 2) * OC_MAXN + i];
+            }
           }
           const R zm = side ? zn : zo_, qm0 = side ? qn0 : qo0, qm1 = side ? qn1 : qo1;
           const R zp = side ? zo_ : zn, qp0 = side ? qo0 : qn0, qp1 = side ? qo1 : qn1;
@@ -1207,12 +1228,23 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           c0 += fcol[k] * FV[FVS + k];
           c1 += fcol[k] * FV[2 * FVS + k];
         }
-      } else {
-        for (int k = 0; k < nfo; ++k) {
-          const R l = tsel < 0 ? tb.BQ[k][t] : tb.F[tsel][nfo][k][t];
+      } else if (tsel > 0 && nfo == G) {  // half of a coarse face, same degree
+#pragma unroll
+        for (int k = 0; k < G; ++k) {
+          const R l = tb.F[tsel][G][k][t];
           cz += l * FV[k];
           c0 += l * FV[FVS + k];
           c1 += l * FV[2 * FVS + k];
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < (Q > OC_MAXF ? Q : OC_MAXF); ++k) {  // nfo <= max(Q, OC_MAXF)
+          if (k < nfo) {
+            const R l = tsel < 0 ? tb.BQ[k][t] : tb.F[tsel][nfo][k][t];
+            cz += l * FV[k];
+            c0 += l * FV[FVS + k];
+            c1 += l * FV[2 * FVS + k];
+          }
         }
       }
       const int d = fbase + t * fstride;
