@@ -1,0 +1,205 @@
+"""Cell partition of one mesh over several ranks with a one-layer ghost halo.
+
+The reference distributes its p4est forest over MPI ranks and refreshes the
+ghost face values once per stage through MatrixFree (`DataAccessOnFaces::values`,
+OceanDG.h:1812-1813).  Here a mesh in Morton order is cut into contiguous cell
+ranges of balanced DoF counts.  Each rank gets a local mesh made of its owned
+cells followed by the ghost cells that share a face with them; faces between a
+ghost and a cell outside the rank are dropped, so the operator computes the
+owned cells exactly (all their faces are local) and garbage it never uses on
+the ghosts.  Before every stage the ghosts' stage input is refreshed from the
+owners (`HaloExchange.exchange`), the only data exchange of the path.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .mesh import Mesh
+
+
+@dataclass
+class Part:
+    rank: int
+    mesh: Mesh                 # owned cells first, then ghosts
+    n_owned: int
+    global_cell: np.ndarray    # [n_local] global cell id of every local cell
+    owner: np.ndarray          # [n_local] owning rank of every local cell
+
+    def dof_index(self, global_mesh: Mesh, var: str = "zeta") -> np.ndarray:
+        """Global DoF index of every local DoF (zeta: n layout; q: 2n layout)."""
+        goff, loff = global_mesh.offsets(), self.mesh.offsets()
+        nd = np.diff(loff)
+        cells = np.repeat(np.arange(self.mesh.n_cells), nd)
+        local = np.arange(int(loff[-1])) - loff[cells]
+        if var == "zeta":
+            return goff[self.global_cell[cells]] + local
+        cells2 = np.repeat(np.arange(self.mesh.n_cells), 2 * nd)
+        local2 = np.arange(2 * int(loff[-1])) - 2 * loff[cells2]
+        return 2 * goff[self.global_cell[cells2]] + local2
+
+
+def owner_ranges(mesh: Mesh, n_parts: int) -> np.ndarray:
+    """Owning rank of every cell: contiguous ranges with balanced DoF counts."""
+    nd = mesh.dofs_per_cell().astype(np.float64)
+    cum = np.cumsum(nd) - 0.5 * nd
+    return np.minimum((cum / nd.sum() * n_parts).astype(np.int64), n_parts - 1)
+
+
+def partition(mesh: Mesh, n_parts: int) -> list:
+    owner = owner_ranges(mesh, n_parts)
+    ni = mesh.n_inner
+    cm, cp = mesh.cell_m[:ni], mesh.cell_p
+    parts = []
+    for r in range(n_parts):
+        owned = np.nonzero(owner == r)[0]
+        touch = (owner[cm] == r) | (owner[cp] == r)
+        nb = np.concatenate([cp[touch & (owner[cm] == r)], cm[touch & (owner[cp] == r)]])
+        ghosts = np.unique(nb[owner[nb] != r])
+        cells = np.concatenate([owned, ghosts])
+        local = np.full(mesh.n_cells, -1, np.int64)
+        local[cells] = np.arange(len(cells))
+        keep = (local[cm] >= 0) & (local[cp] >= 0)  # inner faces between two local cells
+        bm = mesh.cell_m[ni:]
+        keep_b = local[bm] >= 0
+        lm = Mesh(
+            degree=mesh.degree[cells].astype(np.int32),
+            vertices=mesh.vertices[cells],
+            cell_m=np.concatenate([local[cm[keep]], local[bm[keep_b]]]).astype(np.int32),
+            cell_p=local[cp[keep]].astype(np.int32),
+            face_m=np.concatenate([mesh.face_m[:ni][keep], mesh.face_m[ni:][keep_b]]).astype(np.int8),
+            face_p=mesh.face_p[keep].astype(np.int8),
+            subface=mesh.subface[keep].astype(np.int8),
+            orient=mesh.orient[keep].astype(np.int8),
+            bid=mesh.bid[keep_b].astype(np.int32),
+            level=None if mesh.level is None else mesh.level[cells].astype(np.int32),
+            domain=mesh.domain,
+        )
+        parts.append(Part(r, lm, len(owned), cells, owner[cells]))
+    return parts
+
+
+def _dof_idx(mesh: Mesh, cells):
+    """Local DoF indices (zeta layout, q layout) of the given local cells, in order."""
+    off = mesh.offsets()
+    nd = np.diff(off)
+    if len(cells) == 0:
+        return np.zeros(0, np.int64), np.zeros(0, np.int64)
+    z = np.concatenate([off[c] + np.arange(nd[c]) for c in cells])
+    q = np.concatenate([2 * off[c] + np.arange(2 * nd[c]) for c in cells])
+    return z, q
+
+
+def halo_plan(parts: list, rank: int):
+    """(send, recv) of one rank: {other rank: (zeta idx, q idx)} into its local vectors.
+    Every rank derives the same plan from the same partition: the ghosts of rank g
+    owned by rank o travel o -> g in g's ghost order (ascending global cell id)."""
+    me = parts[rank]
+    send, recv = {}, {}
+    for other in parts:
+        if other.rank == rank:
+            continue
+        # my ghosts owned by `other`
+        mine = [i for i in range(me.n_owned, me.mesh.n_cells) if me.owner[i] == other.rank]
+        if mine:
+            recv[other.rank] = _dof_idx(me.mesh, mine)
+        # other's ghosts owned by me, as local indices of my owned cells
+        theirs = other.global_cell[other.n_owned:][other.owner[other.n_owned:] == rank]
+        if len(theirs):
+            pos = {int(c): i for i, c in enumerate(me.global_cell[:me.n_owned])}
+            send[other.rank] = _dof_idx(me.mesh, [pos[int(c)] for c in theirs])
+    return send, recv
+
+
+class HaloExchange:
+    """Refresh the ghost DoFs of one rank's (zeta, q) from their owners: pack the
+    owned DoFs other ranks hold as ghosts, move them, unpack into the ghosts.
+    `transport(send, recv)` moves the buffers ({rank: tensor}); torch_transport
+    uses torch.distributed point-to-point calls (gloo on CPU, NCCL on GPUs)."""
+
+    def __init__(self, parts: list, rank: int, transport=None, device=None):
+        import torch
+        self.rank = rank
+        send, recv = halo_plan(parts, rank)
+        dev = device or "cpu"
+        t = lambda a: torch.as_tensor(a, dtype=torch.int64, device=dev)  # noqa: E731
+        self.send = {r: (t(z), t(q)) for r, (z, q) in send.items()}
+        self.recv = {r: (t(z), t(q)) for r, (z, q) in recv.items()}
+        self.transport = transport or torch_transport
+
+    def exchange(self, zeta, q):
+        import torch
+        sbuf = {r: torch.cat([zeta[iz], q[iq]]) for r, (iz, iq) in self.send.items()}
+        rbuf = {r: torch.empty(len(iz) + len(iq), dtype=zeta.dtype, device=zeta.device)
+                for r, (iz, iq) in self.recv.items()}
+        self.transport(sbuf, rbuf)
+        for r, (iz, iq) in self.recv.items():
+            zeta[iz] = rbuf[r][:len(iz)]
+            q[iq] = rbuf[r][len(iz):]
+
+
+def torch_transport(send: dict, recv: dict):
+    import torch.distributed as dist
+    reqs = [dist.irecv(buf, src=r) for r, buf in recv.items()]
+    reqs += [dist.isend(buf, dst=r) for r, buf in send.items()]
+    for q in reqs:
+        q.wait()
+
+
+def partitioned_erk_step(stage, halo, tableau, t, dt, zeta, q):
+    """One explicit RK step of one rank in Butcher form (ExplicitRungeKuttaIntegrator.h:
+    179-298) with a halo refresh before every stage.  `stage` has the signature of
+    perform_stage_hydro on local vectors: stage(s, n_stages, time, f, rz, rq, kz, kq,
+    solution_z, solution_q, next_z, next_q).  On return the owned DoFs of (zeta, q)
+    hold u^{n+1}; ghosts hold values that the next refresh replaces."""
+    import torch
+    a, b, c = tableau["a"], tableau["b"], tableau["c"]
+    s = len(b)
+    n = zeta.numel()
+    kz = [torch.zeros_like(zeta) for _ in range(s + 1)]
+    kq = [torch.zeros_like(q) for _ in range(s + 1)]
+    nz, nq = torch.zeros_like(zeta), torch.zeros_like(q)
+    halo.exchange(zeta, q)
+    for st in range(s):
+        f = np.asarray(b if st == s - 1 else a[st], np.float64) * dt
+        if st > 0:
+            halo.exchange(nz, nq)
+        rz, rq = (zeta.clone(), q.clone()) if st == 0 else (nz.clone(), nq.clone())
+        stage(st, s, t + c[st] * dt, f, rz, rq, kz, kq, zeta, q, nz, nq)
+    assert zeta.numel() == n
+
+
+def local_exchange(parts: list, zetas, qs, plans=None):
+    """Refresh the ghosts of all parts held by one process (an in-process
+    transport): the same copies HaloExchange makes over the network."""
+    import torch
+    plans = plans or [halo_plan(parts, r) for r in range(len(parts))]
+    for g in range(len(parts)):
+        for o, (rz, rq) in plans[g][1].items():
+            sz, sq = plans[o][0][g]
+            dev = zetas[g].device
+            zetas[g][torch.as_tensor(rz, device=dev)] = zetas[o][torch.as_tensor(sz, device=dev)]
+            qs[g][torch.as_tensor(rq, device=dev)] = qs[o][torch.as_tensor(sq, device=dev)]
+
+
+def local_erk_step(stages, parts, tableau, t, dt, zetas, qs, plans=None):
+    """partitioned_erk_step for all parts of one process in lockstep (stage by
+    stage, ghosts refreshed between stages by local_exchange)."""
+    import torch
+    a, b, c = tableau["a"], tableau["b"], tableau["c"]
+    s = len(b)
+    P = len(parts)
+    plans = plans or [halo_plan(parts, r) for r in range(P)]
+    kz = [[torch.zeros_like(zetas[r]) for _ in range(s + 1)] for r in range(P)]
+    kq = [[torch.zeros_like(qs[r]) for _ in range(s + 1)] for r in range(P)]
+    nz = [torch.zeros_like(zetas[r]) for r in range(P)]
+    nq = [torch.zeros_like(qs[r]) for r in range(P)]
+    local_exchange(parts, zetas, qs, plans)
+    for st in range(s):
+        f = np.asarray(b if st == s - 1 else a[st], np.float64) * dt
+        if st > 0:
+            local_exchange(parts, nz, nq, plans)
+        for r in range(P):
+            rz, rq = (zetas[r].clone(), qs[r].clone()) if st == 0 else (nz[r].clone(), nq[r].clone())
+            stages[r](st, s, t + c[st] * dt, f, rz, rq, kz[r], kq[r], zetas[r], qs[r], nz[r], nq[r])
