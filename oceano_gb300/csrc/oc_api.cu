@@ -121,6 +121,8 @@ struct oc_op {
   double *d_geo = nullptr, *d_fnrm = nullptr, *d_flen = nullptr;
   float *d_geof = nullptr;
   double *d_dscratch = nullptr;  // mixed form: FP64 zeta work area per (warp, team) slot
+  DegTables<double> *d_tabd = nullptr;  // table copies in global memory (divergent reads)
+  DegTables<float> *d_tabf = nullptr;
   double *d_sd[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   float *d_sde[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   // degree groups
@@ -476,6 +478,8 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   OC_TRY(upload_tables_p2(td.data(), tf.data()));
   OC_TRY(upload_tables_p3(td.data(), tf.data()));
   OC_TRY(upload_tables_p4(td.data(), tf.data()));
+  OC_TRY(upload(op, &op->d_tabd, td.data(), td.size()));
+  OC_TRY(upload(op, &op->d_tabf, tf.data(), tf.size()));
   OC_TRY(upload_tables_hp_v0(td.data(), tf.data()));
   OC_TRY(upload_tables_hp_v1(td.data(), tf.data()));
   OC_TRY(upload_tables_hp_v2(td.data(), tf.data()));
@@ -626,6 +630,8 @@ static void fill_common(oc_op *op, StageArgs &a) {
   a.ref.rr0 = std::fmaf(-a.ref.ur0, a.ref.hr, a.ref.qr0);  // exact residual (IEEE fma)
   a.ref.rr1 = std::fmaf(-a.ref.ur1, a.ref.hr, a.ref.qr1);
   a.dscratch = op->d_dscratch;
+  a.gtabd = op->d_tabd;
+  a.gtabf = op->d_tabf;
   a.cfsdo = (op->d_sd[3] || op->d_sd[4]) ? op->d_cfsdo : nullptr;
   const double cu = op->prm.threshold_wetdry;
   a.g = op->prm.g; a.cu4 = cu * cu * cu * cu; a.nu = op->prm.horizontal_viscosity;

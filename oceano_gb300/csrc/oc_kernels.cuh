@@ -1055,6 +1055,12 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     for (int k = 0; k < G; ++k) fcol[k] = tb.F[0][G][k][tt];
     fw = tb.wF[G][kk];
   }
+  // lane-dependent table entries of the hanging / degree-jump face paths come
+  // from the global copy (L1), where divergent addresses cost a few wavefronts
+  // instead of one constant-bank replay per distinct address
+  const DegTables<R> *gt = reinterpret_cast<const DegTables<R> *>(
+      sizeof(R) == 4 ? (const void *)a.gtabf : (const void *)a.gtabd);
+  const DegTables<R> &tbg = gt[P - 1];
 #pragma unroll 1
   for (int sl = 0; sl < 8; ++sl) {
     const FaceRec r = recs[sl];
@@ -1078,7 +1084,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       if (kind == 1) {
         const int side = r.side(), sub = r.sub(), orient = r.orient(), nf = r.nf();
         const int pn = r.nb_deg(), Nn = pn + 1;
-        const DegTables<R> &tn = tab<R>(pn);
+        const DegTables<R> &tn = gt[pn - 1];
         if (side == 1 && sub >= 0) len *= R(0.5);  // coarse side: the fine half-face
         const R n0 = side ? -on0 : on0, n1 = side ? -on1 : on1;  // minus normal
         const int sdo = a.cfsdo ? w_sdo[8 * team + sl] : 0;
@@ -1097,14 +1103,14 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
               for (int i = 0; i < N; ++i) lo[i] = frow[i];
             } else {
 #pragma unroll
-              for (int i = 0; i < N; ++i) lo[i] = tb.F[tsel][G][k][i];
+              for (int i = 0; i < N; ++i) lo[i] = __ldg(&tbg.F[tsel][G][k][i]);
             }
             if (nsel == 0) {
 #pragma unroll
               for (int i = 0; i < N; ++i) ln[i] = frow[i];
             } else {
 #pragma unroll
-              for (int i = 0; i < N; ++i) ln[i] = tb.F[nsel][G][k][i];
+              for (int i = 0; i < N; ++i) ln[i] = __ldg(&tbg.F[nsel][G][k][i]);
             }
             R zo_ = 0, qo0 = 0, qo1 = 0, zn = 0, qn0 = 0, qn1 = 0;
 #pragma unroll
@@ -1146,7 +1152,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
           for (int i = 0; i < N; ++i) {  // own trace
             const int d = face_dof(N, fo, i);
-            const R l = tb.F[tsel][nf][ko][i];
+            const R l = __ldg(&tbg.F[tsel][nf][ko][i]);
             zo_ += l * U[d];
             qo0 += l * U[NN + d];
             qo1 += l * U[2 * NN + d];
@@ -1155,7 +1161,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
           for (int i = 0; i < OC_MAXN; ++i) {  // neighbour trace (Nn <= OC_MAXN nodes)
             if (i < Nn) {
-              const R l = tn.F[nsel][nf][kn][i];
+              const R l = __ldg(&tn.F[nsel][nf][kn][i]);
               zn += l * NB[(sl * 3 + 0) * OC_MAXN + i];
               qn0 += l * NB[(sl * 3 + 1) * OC_MAXN + i];
               qn1 += l * NB[(sl * 3 + 2) * OC_MAXN + i];
@@ -1176,7 +1182,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           else
             face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1, Pm0,
                          Pm1, Pp0, Pp1);
-          const R jxw = tb.wF[nf][k] * len;
+          const R jxw = __ldg(&tbg.wF[nf][k]) * len;
           if (side == 0) {
             FV[ko] = -F * jxw;
             FV[FVS + ko] = (-Fa0 - Pm0) * jxw;
@@ -1231,7 +1237,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       } else if (tsel > 0 && nfo == G) {  // half of a coarse face, same degree
 #pragma unroll
         for (int k = 0; k < G; ++k) {
-          const R l = tb.F[tsel][G][k][t];
+          const R l = __ldg(&tbg.F[tsel][G][k][t]);
           cz += l * FV[k];
           c0 += l * FV[FVS + k];
           c1 += l * FV[2 * FVS + k];
@@ -1240,7 +1246,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
         for (int k = 0; k < (Q > OC_MAXF ? Q : OC_MAXF); ++k) {  // nfo <= max(Q, OC_MAXF)
           if (k < nfo) {
-            const R l = tsel < 0 ? tb.BQ[k][t] : tb.F[tsel][nfo][k][t];
+            const R l = tsel < 0 ? tb.BQ[k][t] : __ldg(&tbg.F[tsel][nfo][k][t]);
             cz += l * FV[k];
             c0 += l * FV[FVS + k];
             c1 += l * FV[2 * FVS + k];

@@ -90,6 +90,10 @@ struct StageArgs {
   // per (launch-wide warp, team) slot, OC_MAXCPW slots per warp (only cells that
   // are not fully wet touch it)
   double *dscratch;
+  // global-memory copies of the per-degree tables (index p - 1), read through
+  // the L1 cache where lanes need different entries (hanging and degree-jump faces)
+  const DegTables<double> *gtabd;
+  const DegTables<float> *gtabf;
   // mixed form: reference state (depth h_ref, discharge q_ref); the FP32 discharge
   // is q - q_ref and the fluxes are evaluated minus their reference value
   double h_ref, q_ref[2];
