@@ -47,35 +47,77 @@ def owner_ranges(mesh: Mesh, n_parts: int) -> np.ndarray:
     return np.minimum((cum / nd.sum() * n_parts).astype(np.int64), n_parts - 1)
 
 
+GHOST_BID = 15  # boundary id of the cut faces of ghost cells (any condition: ghosts are discarded)
+
+
+def with_ghost_boundary(bcs: dict) -> dict:
+    """Boundary conditions of a local mesh: those of the global mesh plus a wall on
+    the cut faces of the ghost cells (their residual is never used)."""
+    out = dict(bcs)
+    out[GHOST_BID] = ("wall",)
+    return out
+
+
 def partition(mesh: Mesh, n_parts: int) -> list:
+    """Local meshes of the ranks.  Ghosts = the cells sharing a face with an owned
+    cell; when a ghost is the coarse side of a hanging face whose second half is
+    local, its first half's fine cell joins as a ghost too (the operator wants
+    subface 0 of a split face).  Ghost faces with no local cell on the other side
+    become boundary faces with id GHOST_BID."""
     owner = owner_ranges(mesh, n_parts)
     ni = mesh.n_inner
-    cm, cp = mesh.cell_m[:ni], mesh.cell_p
+    cm, cp, sub = mesh.cell_m[:ni], mesh.cell_p, mesh.subface
+    bm = mesh.cell_m[ni:]
     parts = []
     for r in range(n_parts):
         owned = np.nonzero(owner == r)[0]
-        touch = (owner[cm] == r) | (owner[cp] == r)
-        nb = np.concatenate([cp[touch & (owner[cm] == r)], cm[touch & (owner[cp] == r)]])
-        ghosts = np.unique(nb[owner[nb] != r])
+        is_local = owner == r
+        nb = np.concatenate([cp[is_local[cm]], cm[is_local[cp]]])
+        is_local = is_local.copy()
+        is_local[nb] = True
+        while True:  # subface closure of coarse ghost faces
+            half = (sub == 1) & is_local[cm] & is_local[cp]  # second half local
+            need = np.zeros(mesh.n_cells, bool)
+            for f in np.nonzero(half)[0]:
+                # first half of the same coarse face: same plus cell and face number
+                g = np.nonzero((cp == cp[f]) & (mesh.face_p == mesh.face_p[f]) & (sub == 0))[0]
+                need[cm[g][~is_local[cm[g]]]] = True
+            if not need.any():
+                break
+            is_local |= need
+        ghosts = np.nonzero(is_local & (owner != r))[0]
         cells = np.concatenate([owned, ghosts])
         local = np.full(mesh.n_cells, -1, np.int64)
         local[cells] = np.arange(len(cells))
         keep = (local[cm] >= 0) & (local[cp] >= 0)  # inner faces between two local cells
-        bm = mesh.cell_m[ni:]
         keep_b = local[bm] >= 0
+        # cut faces: a local (ghost) cell whose neighbour across a face is not local
+        cut_m = (local[cm] >= 0) & (local[cp] < 0)
+        cut_p = (local[cp] >= 0) & (local[cm] < 0) & (sub < 0)  # full plus-side faces only
+        cut_cells = np.concatenate([local[cm[cut_m]], local[cp[cut_p]]])
+        cut_faces = np.concatenate([mesh.face_m[:ni][cut_m], mesh.face_p[cut_p]])
+        # a coarse ghost face cut on both halves: one boundary face
+        both = (local[cp] >= 0) & (local[cm] < 0) & (sub == 0)
+        for f in np.nonzero(both)[0]:
+            g = np.nonzero((cp == cp[f]) & (mesh.face_p == mesh.face_p[f]) & (sub == 1))[0]
+            if len(g) and local[cm[g[0]]] < 0:
+                cut_cells = np.append(cut_cells, local[cp[f]])
+                cut_faces = np.append(cut_faces, mesh.face_p[f])
         lm = Mesh(
             degree=mesh.degree[cells].astype(np.int32),
             vertices=mesh.vertices[cells],
-            cell_m=np.concatenate([local[cm[keep]], local[bm[keep_b]]]).astype(np.int32),
+            cell_m=np.concatenate([local[cm[keep]], local[bm[keep_b]], cut_cells]).astype(np.int32),
             cell_p=local[cp[keep]].astype(np.int32),
-            face_m=np.concatenate([mesh.face_m[:ni][keep], mesh.face_m[ni:][keep_b]]).astype(np.int8),
+            face_m=np.concatenate([mesh.face_m[:ni][keep], mesh.face_m[ni:][keep_b],
+                                   cut_faces]).astype(np.int8),
             face_p=mesh.face_p[keep].astype(np.int8),
             subface=mesh.subface[keep].astype(np.int8),
             orient=mesh.orient[keep].astype(np.int8),
-            bid=mesh.bid[keep_b].astype(np.int32),
+            bid=np.concatenate([mesh.bid[keep_b], np.full(len(cut_cells), GHOST_BID)]).astype(np.int32),
             level=None if mesh.level is None else mesh.level[cells].astype(np.int32),
             domain=mesh.domain,
         )
+        assert not (local[cells[:len(owned)]] < 0).any()
         parts.append(Part(r, lm, len(owned), cells, owner[cells]))
     return parts
 

@@ -56,7 +56,8 @@ def _halo_worker(rank, world, port, out, case):
                       WORLD_SIZE=str(world))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     from cases import CASES, VORTEX, static_arrays
-    from oceano_gb300.partition import HaloExchange, partition, partitioned_erk_step
+    from oceano_gb300.partition import (HaloExchange, partition, partitioned_erk_step,
+                                        with_ghost_boundary)
     from oracle import oracle as O
     mesh_f, bcs, pdata, friction = CASES[case]
     mesh = mesh_f()
@@ -67,7 +68,8 @@ def _halo_worker(rank, world, port, out, case):
     dt = 0.05 / full.transport_speed(z0, q0)
     parts = partition(mesh, world)
     part = parts[rank]
-    orc = O.Oracle(part.mesh, friction=friction, bcs=bcs, vortex=VORTEX + [0, 0])
+    orc = O.Oracle(part.mesh, friction=friction, bcs=with_ghost_boundary(bcs),
+                     vortex=VORTEX + [0, 0])
     if pdata is not None:
         orc.set_static(*static_arrays(orc, pdata))
     iz, iq = part.dof_index(mesh, "zeta"), part.dof_index(mesh, "q")

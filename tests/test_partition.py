@@ -41,12 +41,13 @@ def test_partition_covers_every_cell_once():
 @pytest.mark.parametrize("case", ["hanging_p2", "mixed_degree"])
 def test_local_lockstep_matches_single_mesh(case):
     import torch
-    from oceano_gb300.partition import local_erk_step
+    from oceano_gb300.partition import local_erk_step, with_ghost_boundary
     mesh, full, z0, q0, dt, parts = setup(case, 3)
     mesh_f, bcs, pdata, friction = CASES[case]
     stages, zs, qs = [], [], []
     for p in parts:
-        orc = O.Oracle(p.mesh, friction=friction, bcs=bcs, vortex=VORTEX + [0, 0])
+        orc = O.Oracle(p.mesh, friction=friction, bcs=with_ghost_boundary(bcs),
+                       vortex=VORTEX + [0, 0])
 
         def stage(st, s, t, f, rz, rq, kz, kq, sz, sq, nz, nq, orc=orc):
             orc.stage_erk(st, s, t, f, rz.numpy(), rq.numpy(), [k.numpy() for k in kz],
@@ -72,14 +73,14 @@ def test_gpu_partitioned_matches_single_mesh(gpu_lib, case):
     halo copies between stages), against the unpartitioned GPU run (FP64, 1e-12)."""
     import torch
     from oceano_gb300.operator import OceanoOperator
-    from oceano_gb300.partition import local_erk_step
+    from oceano_gb300.partition import local_erk_step, with_ghost_boundary
     from oceano_gb300.workloads import apply_bcs
     mesh, full, z0, q0, dt, parts = setup(case, 3)
     mesh_f, bcs, pdata, friction = CASES[case]
 
     def make(m):
         op = OceanoOperator(m, friction=["none", "linear", "manning"][friction])
-        apply_bcs(op, bcs)
+        apply_bcs(op, with_ghost_boundary(bcs))
         op.set_vortex(*VORTEX)
         if pdata is not None:
             op.initialize_data_at_quadrature(pdata)
