@@ -637,6 +637,8 @@ static void fill_common(oc_op *op, StageArgs &a) {
   a.g = op->prm.g; a.cu4 = cu * cu * cu * cu; a.nu = op->prm.horizontal_viscosity;
   a.zeta_ref = op->prm.precision == OC_PREC_MIXED ? op->prm.zeta_reference : 0.0;
   a.wet_threshold = 1e-3;
+  a.gf = (float)a.g; a.cu4f = (float)a.cu4; a.wet_thrf = (float)a.wet_threshold;
+  a.zreff = (float)a.zeta_ref;
   a.friction = op->prm.friction_model; a.max_iter = op->prm.max_iteration_height;
   a.batch = op->prm.batch_width;
   for (int b = 0; b < OC_MAXBID; ++b) {
@@ -741,6 +743,7 @@ extern "C" oc_status oc_perform_stage_hydro(oc_op *op, uint32_t stage, uint32_t 
   for (uint32_t j = 0; j <= stage; ++j) { dy.f[j] = fr[j]; dy.ft[j] = ark ? ftr[j] : 0.0; }
   dy.fm = fmat;
   dy.time = time;
+  stage_dyn_round(dy);
   a.dyn = op->d_dyn;
   a.stage = (int)stage; a.n_stages = (int)n_stages; a.ark = ark; a.last = last;
   a.write_kq_last = 1;
@@ -1007,6 +1010,7 @@ extern "C" oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time
     }
     d.fm = sc.ark && s < 2 ? sc.dt[s] * dt : 0.0;
     d.time = time + sc.c[s] * dt;
+    stage_dyn_round(d);
   }
   OC_TRY(cudaMemcpyAsync(op->d_dyn, op->h_dyn, sizeof(StageDyn) * sc.s, cudaMemcpyHostToDevice,
                          op->stream));
@@ -1099,6 +1103,7 @@ extern "C" oc_status oc_apply(oc_op *op, double time, const double *sz, const do
   StageDyn &dy = op->h_dyn[OC_MAXSTAGES];
   std::memset(&dy, 0, sizeof(dy));
   dy.time = time;
+  stage_dyn_round(dy);
   OC_TRY(cudaMemcpyAsync(op->d_dyn + OC_MAXSTAGES, &dy, sizeof(dy), cudaMemcpyHostToDevice, op->stream));
   a.dyn = op->d_dyn + OC_MAXSTAGES;
   a.apply_mode = 1; a.n_stages = 1;

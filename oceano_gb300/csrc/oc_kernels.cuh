@@ -534,7 +534,7 @@ __device__ __noinline__ void boundary_flux(const StageArgs &a, int bid, int bkin
                                            double sx, const double *geo, double zref, int sdk,
                                            R g, R cu4, R zm, R qm0, R qm1, R n0, R n1, R &F,
                                            R &Fa0, R &Fa1) {
-  R zbm = MIX ? (R)zref : R(0);
+  R zbm = MIX ? (R)a.zreff : R(0);
   if (MIX && a.sdbe) zbm = (R)a.sdbe[sdk];
   else if (!MIX && a.sdb) zbm = (R)a.sdb[sdk];
   const double e0 = fo == 0 ? 0. : fo == 1 ? 1. : sx;
@@ -638,6 +638,21 @@ struct FaceRec {
   __device__ __forceinline__ int bid() const { return (pk >> 16) & 15; }
 };
 
+// Stage coefficients in the compute type: the FP32 copies for the FP32 bulk (one
+// 16-byte read-only load, no FP64 conversion), the FP64 values otherwise.
+template <typename R>
+__device__ __forceinline__ void load_coefs(const float *ff, const double *fd,
+                                           R (&o)[OC_MAXSTAGES]) {
+  static_assert(OC_MAXSTAGES == 4, "one float4 of coefficients");
+  if constexpr (sizeof(R) == 4) {
+    const float4 f4 = __ldg(reinterpret_cast<const float4 *>(ff));
+    o[0] = f4.x; o[1] = f4.y; o[2] = f4.z; o[3] = f4.w;
+  } else {
+#pragma unroll
+    for (int j = 0; j < OC_MAXSTAGES; ++j) o[j] = (R)__ldg(&fd[j]);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // The fused stage kernel.
 //   MIX = false: FP64 plain form (R = KT = double).
@@ -676,10 +691,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   const int nvalid = max(0, min(cpw, n_group - gi0));  // cells of this warp
   const bool valid = member && team < nvalid;
   const int s = a.stage;
-  const StageDyn dy = *a.dyn;
-  R fR[OC_MAXSTAGES];  // coefficients in the compute type, converted once
-#pragma unroll
-  for (int j = 0; j < OC_MAXSTAGES; ++j) fR[j] = (R)dy.f[j];
+  R fR[OC_MAXSTAGES];  // coefficients in the compute type (mixed form: the FP32 copies)
+  load_coefs<R>(a.dyn->ff, a.dyn->f, fR);
   R fRs = fR[0];  // f_s
 #pragma unroll
   for (int j = 1; j < OC_MAXSTAGES; ++j)
@@ -687,8 +700,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   // the mixed time-step path (FP32 registers) forms internal stage inputs in FP32
   constexpr bool fast = MIX && sizeof(KT) == 4;
   const double zref = MIX ? a.zeta_ref : 0.0;
-  const R g = (R)a.g, cu4 = (R)a.cu4;
-  const R zbe_flat = (R)zref;  // zb + zeta_ref where no bathymetry is given
+  const R g = MIX ? (R)a.gf : (R)a.g, cu4 = MIX ? (R)a.cu4f : (R)a.cu4;
+  const R zbe_flat = MIX ? (R)a.zreff : R(0);  // zb + zeta_ref where no bathymetry is given
   // mixed form: discharge stored as q - q_r (reference state (h_r, q_r))
   const RefStateF &rf = a.ref;
   const double qref0 = MIX ? a.q_ref[0] : 0.0, qref1 = MIX ? a.q_ref[1] : 0.0;
@@ -1324,7 +1337,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   __syncwarp();
   bool need_fp64 = !MIX;
   if (MIX) {
-    const R wet_thr = (R)a.wet_threshold;
+    const R wet_thr = (R)a.wet_thrf;
     const unsigned team_mask = ((1u << T) - 1u) << (team * T);
     // Without bathymetry data every Gauss-Lobatto point is wet when the nodal
     // |zeta - zeta_ref| stay below (zb + zeta_ref - threshold) / Lambda (Lambda: the
@@ -1466,10 +1479,39 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   }
   __syncwarp();
 
+  // last stage of the mixed time step: u^n of the FP64 accumulation, loaded here
+  // so that the loads overlap the discharge passes (lane element e = lane + 32 i)
+  constexpr int EZ = (CPWMAX * NN + 31) / 32, EQ = (2 * CPWMAX * NN + 31) / 32;
+  double unz[fast ? EZ : 1], unq[fast ? EQ : 1];
+  if constexpr (fast) {
+    if (a.out_z) {
+#pragma unroll
+      for (int i = 0; i < EZ; ++i) {
+        const int e = lane + 32 * i;
+        if (e < nvalid * NN) {
+          const int j = e / NN, d = e - j * NN;
+          unz[i] = a.un_z[w_off[j] + d];
+        }
+      }
+    }
+    if (!a.ark && a.out_q) {
+#pragma unroll
+      for (int i = 0; i < EQ; ++i) {
+        const int e = lane + 32 * i;
+        if (e < nvalid * 2 * NN) {
+          const int j = e / (2 * NN), d = e - j * 2 * NN;
+          unq[i] = a.un_q[2 * (int64_t)w_off[j] + d];
+        }
+      }
+    }
+  }
+
   // ---- 4. discharge: local_apply_inverse_mass_matrix_discharge (OceanDG.h:1532-1571);
   //         ARK: cell_mass_discharge + inverse_modified_mass (:1573-1645, :2086-2116) ----
   if (split) {
     // b = sum_j (f_j kex_j + ft_j kim_j); stores kex_s, kim_s
+    R ftR[OC_MAXSTAGES];
+    load_coefs<R>(a.dyn->fft, a.dyn->ft, ftR);
     if (member && t < N) {
 #pragma unroll
       for (int e = 0; e < 2; ++e)
@@ -1482,15 +1524,15 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
             static_cast<KT *>(a.kq[2 * s + 1])[gidx] = (KT)kex;
             static_cast<KT *>(a.kq[2 * s + 2])[gidx] = (KT)kim;
           }
-          R bsum = s == 0 ? (R)dy.f[0] * kex + (R)dy.ft[0] * kim
-                          : (R)dy.f[0] * (R) static_cast<const KT *>(a.kq[1])[gidx] +
-                                (R)dy.ft[0] * (R) static_cast<const KT *>(a.kq[2])[gidx];
+          R bsum = s == 0 ? fR[0] * kex + ftR[0] * kim
+                          : fR[0] * (R) static_cast<const KT *>(a.kq[1])[gidx] +
+                                ftR[0] * (R) static_cast<const KT *>(a.kq[2])[gidx];
 #pragma unroll
           for (int j = 1; j < OC_MAXSTAGES; ++j) {
             if (j > s) break;
             const R ke = j == s ? kex : (R) static_cast<const KT *>(a.kq[2 * j + 1])[gidx];
             const R ki = j == s ? kim : (R) static_cast<const KT *>(a.kq[2 * j + 2])[gidx];
-            bsum += (R)dy.f[j] * ke + (R)dy.ft[j] * ki;
+            bsum += fR[j] * ke + ftR[j] * ki;
           }
           RES[(1 + e) * NN + d] = bsum;
         }
@@ -1506,13 +1548,13 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           const int64_t gidx = qo + e * NN + d;
           const R kex = RES[(1 + e) * NN + d];
           if (valid) static_cast<KT *>(a.kq[2 * s + 1])[gidx] = (KT)kex;
-          R bsum = (R)dy.f[0] * (s == 0 ? kex : (R) static_cast<const KT *>(a.kq[1])[gidx]);
+          R bsum = fR[0] * (s == 0 ? kex : (R) static_cast<const KT *>(a.kq[1])[gidx]);
 #pragma unroll
           for (int j = 1; j < OC_MAXSTAGES; ++j) {
             if (j > s) break;
             const R ke = j == s ? kex : (R) static_cast<const KT *>(a.kq[2 * j + 1])[gidx];
             const R ki = (R) static_cast<const KT *>(a.kq[2 * j])[gidx];
-            bsum += (R)dy.f[j] * ke + (R)dy.f[j - 1] * ki;
+            bsum += fR[j] * ke + fR[j - 1] * ki;
           }
           RES[(1 + e) * NN + d] = bsum;
         }
@@ -1551,6 +1593,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       }
     }
     __syncwarp();
+    const R fmR = sizeof(R) == 4 ? (R)__ldg(&a.dyn->ffm) : (R)__ldg(&a.dyn->fm);
     R m0[N], m1[N];  // MIX: y-integrated correction; FP64: y-integrated M q^n
 #pragma unroll
     for (int i = 0; i < N; ++i) m0[i] = m1[i] = 0;
@@ -1579,8 +1622,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         const R jf = friction_jac<R>(a.friction, g, u0, u1, cf, depth<R>(vz, zb));
         const R jxw = tb.wM[t] * tb.wM[qy] * det;
         coef[qy] = R(1) / jxw;
-        coef[qy] *= R(1) / (R(1) + (R)dy.fm * jf);
-        const R wq = MIX ? jxw * (R)dy.fm * jf : jxw;  // MIX: correction; FP64: mass of q^n
+        coef[qy] *= R(1) / (R(1) + fmR * jf);
+        const R wq = MIX ? jxw * fmR * jf : jxw;  // MIX: correction; FP64: mass of q^n
 #pragma unroll
         for (int iy = 0; iy < N; ++iy) {
           m0[iy] += tb.BM[qy][iy] * (wq * n0);
@@ -1683,11 +1726,13 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       if (a.out_rz) a.out_rz[gz] = (float)(Rj[9 * NN + d] + Rj[8 * NN + d]);
     }
     if (a.out_z) {
-#pragma unroll 2
-      for (int e = lane; e < nvalid * NN; e += 32) {
-        const int j = e / NN, d = e - j * NN;
-        const int64_t gz = w_off[j] + d;
-        a.out_z[gz] = a.un_z[gz] + (double)Rreg(j)[8 * NN + d];
+#pragma unroll
+      for (int i = 0; i < EZ; ++i) {
+        const int e = lane + 32 * i;
+        if (e < nvalid * NN) {
+          const int j = e / NN, d = e - j * NN;
+          a.out_z[w_off[j] + d] = unz[i] + (double)Rreg(j)[8 * NN + d];
+        }
       }
     }
     if (anyflag) {  // cells that took the FP64 literal iteration (rare)
@@ -1735,11 +1780,13 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       Rj[4 * NN + d] = up;  // last stage: delta for the FP64 accumulation
     }
     if (a.out_q) {
-#pragma unroll 2
-      for (int e = lane; e < nvalid * 2 * NN; e += 32) {
-        const int j = e / (2 * NN), d = e - j * 2 * NN;
-        const int64_t gq = 2 * (int64_t)w_off[j] + d;
-        a.out_q[gq] = a.un_q[gq] + (double)Rreg(j)[4 * NN + d];
+#pragma unroll
+      for (int i = 0; i < EQ; ++i) {
+        const int e = lane + 32 * i;
+        if (e < nvalid * 2 * NN) {
+          const int j = e / (2 * NN), d = e - j * 2 * NN;
+          a.out_q[2 * (int64_t)w_off[j] + d] = unq[i] + (double)Rreg(j)[4 * NN + d];
+        }
       }
     }
     return;
@@ -1754,10 +1801,11 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       // ERK: k_q[s+1] = M^-1 L_h q; next = q^n + sum_j f_j k_q[j+1]
       const double kc = (double)(KT)v;
       if (wkq) static_cast<KT *>(a.kq[s + 1])[gq] = (KT)v;
-      double acc = a.un_q[gq] + dy.f[0] * (s == 0 ? kc : (double)static_cast<const KT *>(a.kq[1])[gq]);
+      const double *fd = a.dyn->f;
+      double acc = a.un_q[gq] + fd[0] * (s == 0 ? kc : (double)static_cast<const KT *>(a.kq[1])[gq]);
 #pragma unroll
       for (int jj = 1; jj < OC_MAXSTAGES; ++jj)
-        if (jj <= s) acc += dy.f[jj] * (jj == s ? kc : (double)static_cast<const KT *>(a.kq[jj + 1])[gq]);
+        if (jj <= s) acc += fd[jj] * (jj == s ? kc : (double)static_cast<const KT *>(a.kq[jj + 1])[gq]);
       nxt = acc;
     } else if (!a.last) {
       nxt = MIX ? a.un_q[gq] + (double)v : (double)v;

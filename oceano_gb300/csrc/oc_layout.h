@@ -34,10 +34,18 @@ inline void cast_tables(const DegTables<double> &a, DegTables<R> &b) {
 
 // Per-call coefficients, read by the kernels from device memory so that a
 // captured CUDA graph stays valid when dt or the time change.
-struct StageDyn {
+struct alignas(16) StageDyn {
+  float ff[OC_MAXSTAGES], fft[OC_MAXSTAGES];  // FP32 copies of f, ft (mixed form: one 16-byte load each)
   double f[OC_MAXSTAGES], ft[OC_MAXSTAGES];
   double fm, time;
+  float ffm, pad_[3];
 };
+
+// Fill the FP32 copies of a coefficient block from its FP64 values.
+inline void stage_dyn_round(StageDyn &d) {
+  for (int j = 0; j < OC_MAXSTAGES; ++j) { d.ff[j] = (float)d.f[j]; d.fft[j] = (float)d.ft[j]; }
+  d.ffm = (float)d.fm;
+}
 
 // FP32 reference state of the mixed form: depth, discharge, velocity q/h and the
 // residual q - u h of the rounded pair (computed with one fused multiply-add).
@@ -98,6 +106,8 @@ struct StageArgs {
   // is q - q_ref and the fluxes are evaluated minus their reference value
   double h_ref, q_ref[2];
   RefStateF ref;  // the same state in FP32 with u_ref = q_ref / h_ref (read from the parameter bank)
+  // FP32 copies of g, cu4, the wet threshold and zeta_ref (no conversions in the kernels)
+  float gf, cu4f, wet_thrf, zreff;
   // one-launch hp stage (stage_kernel_hp): per degree p the first block, the
   // number of blocks, the cells and the cell list of the group
   int hp_first_block[OC_MAXDEG + 1], hp_blocks[OC_MAXDEG + 1], hp_n[OC_MAXDEG + 1];
