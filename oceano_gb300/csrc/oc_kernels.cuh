@@ -296,17 +296,6 @@ __device__ __forceinline__ R load_r(const void *p, int64_t i, int is_float, doub
 
 // stage-input load with the input precision fixed at compile time (a runtime
 // switch would let the compiler evaluate both branches)
-// Asynchronous 4-byte global -> shared copy (cp.async, completes without a wait
-// loop of ours; cp_async_wait_all() + __syncwarp() before the data is read).
-__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
 template <typename RIN, typename R>
 __device__ __forceinline__ R load_in(const void *p, int64_t i, double ref) {
   if constexpr (sizeof(RIN) == 4) {
@@ -325,17 +314,15 @@ struct Dims {
   static constexpr int T = Q > G ? Q : G;
   static constexpr int NN = N * N, NT = N * T;
   static constexpr int CPW = 32 / T;
-  // scratch tiles of the sum factorisation
+  // scratch tiles of the sum factorisation (also hold the 8 x 3 x OC_MAXN neighbour traces)
   static constexpr int XS = 6 * NT > 8 * 3 * OC_MAXN ? 6 * NT : 8 * 3 * OC_MAXN;
-  // neighbour traces of the 8 face slots (3 variables x up to 5 nodes each)
-  static constexpr int NBS = 8 * 3 * OC_MAXN;
   // per-cell shared memory: compute-type region and FP64 region (elements)
-  static constexpr int SZR = 10 * NN + XS + 3 * FVS + NBS;  // U 3, RES 3, RST 2, BZ 1, ZN 1; X; FV; NB
+  static constexpr int SZR = 10 * NN + XS + 3 * FVS;  // U 3, RES 3, RST 2, BZ 1, ZN 1; X; FV
   static constexpr int SZD = NN + 3 * NT + T + 2;
   // Team strides: padded so that the 32/T teams of a warp start on different
   // shared-memory banks (stride mod 32 chosen per degree and element size to
   // keep row, column and node-row accesses at most 2-way conflicted).
-  static constexpr int pad_f = P == 1 ? 5 : P == 2 ? 5 : P == 3 ? 3 : 8;
+  static constexpr int pad_f = P == 1 ? 29 : P == 2 ? 29 : P == 3 ? 3 : 0;
   static constexpr int pad_d = P == 1 ? 5 : P == 2 ? 2 : P == 3 ? 3 : 4;
   template <typename R>
   static constexpr int bytes_r() {
@@ -719,7 +706,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   R *ZN = BZ + NN;            // NN mixed form: zeta^n - zeta_ref
   R *X = ZN + NN;             // scratch tiles
   R *FV = X + D::XS;          // 3*FVS face point values
-  R *NB = FV + 3 * FVS;       // neighbour traces [slot][var][node]
+  R *NB = X;                  // neighbour traces [slot][var][node] (face phase)
   auto Dreg = [&](int j) {  // FP64 team region of team j: shared (FP64 form) or global slot
     if constexpr (MIX)
       return a.dscratch + ((int64_t)(blockIdx.x * wpb + warp) * OC_MAXCPW + j) * OC_DSTRIDE;
@@ -804,27 +791,6 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     }
   }
   __syncwarp();
-  // neighbour traces: FP32 stage inputs are copied asynchronously (cp.async) and
-  // land while the cell integrals run; other inputs are loaded before the faces
-  constexpr bool async_nb = sizeof(RIN) == 4;
-  if constexpr (async_nb) {
-    if (member) {
-      for (int e = t; e < 8 * OC_MAXN; e += T) {
-        const int sl = e / OC_MAXN, i = e - sl * OC_MAXN;
-        const FaceRec r = reinterpret_cast<const FaceRec *>(w_rec + 16 * team)[sl];
-        const int Nn = r.nb_deg() + 1;
-        if (r.kind() == 1 && i < Nn) {
-          const int d = face_dof(Nn, r.nb_face(), i);
-          const int64_t oz = r.other, oq = 2 * (int64_t)r.other;
-          cp_async4(&NB[(sl * 3 + 0) * OC_MAXN + i], static_cast<const float *>(a.rz) + oz + d);
-          cp_async4(&NB[(sl * 3 + 1) * OC_MAXN + i], static_cast<const float *>(a.rq) + oq + d);
-          cp_async4(&NB[(sl * 3 + 2) * OC_MAXN + i],
-                    static_cast<const float *>(a.rq) + oq + Nn * Nn + d);
-        }
-      }
-    }
-    cp_async_commit();
-  }
   const R Ji00 = gR[6], Ji01 = gR[7], Ji10 = gR[8], Ji11 = gR[9];
   const R det = gR[10];
 
@@ -1036,9 +1002,10 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   // ---- 2. faces: local_apply_face_* (OceanDG.h:936-1050) and
   //         local_apply_boundary_face_* (:1105-1339) ----------------------------
   const FaceRec *recs = reinterpret_cast<const FaceRec *>(w_rec + 16 * team);
-  // 2a. neighbour traces of every inner slot: [slot][var][node]
-  if constexpr (async_nb) cp_async_wait_all();
-  if (!async_nb && member) {
+  // 2a. neighbour traces of every inner slot: [slot][var][node], in the scratch
+  // tiles (free between the cell integrals and the zeta solve); a smaller team
+  // region leaves more of the SM's shared memory / L1 to the L1 cache
+  if (member) {
     for (int e = t; e < 8 * OC_MAXN; e += T) {
       const int sl = e / OC_MAXN, i = e - sl * OC_MAXN;
       const FaceRec r = recs[sl];
