@@ -1047,6 +1047,12 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     const int kind = member ? r.kind() : 0;
     // second slots of conforming faces are empty in every team of most warps
     if (!__any_sync(OC_FULL, kind != 0)) continue;
+    // Warp-uniform choice of the inner-face path: the register-row path when every
+    // inner face of the warp in this slot joins two cells of this degree in standard
+    // orientation, else the table path for all of them (one path per warp: on hp
+    // meshes the teams of a warp meet different neighbour degrees, and two paths
+    // would run one after the other)
+    const bool reg_path = __all_sync(OC_FULL, kind != 1 || (r.nb_deg() == P && r.orient() == 0));
     const int fo = r.own_face();
     // DoF of node i on face fo: fbase + i * fstride (face_dof)
     const int fbase = fo == 0 ? 0 : fo == 1 ? N - 1 : fo == 2 ? 0 : (N - 1) * N;
@@ -1070,7 +1076,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         const int sdo = a.cfsdo ? w_sdo[8 * team + sl] : 0;
         nfo = nf;
         tsel = side ? sub + 1 : 0;
-        if (pn == P && orient == 0) {  // same degree: nf == G <= T, point k on both sides
+        if (reg_path) {  // same degree: nf == G <= T, point k on both sides
           if (t < G) {
             const int k = t;
             // trace rows: full face from registers; the coarse side of a hanging
@@ -1205,28 +1211,25 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       }
     }
     __syncwarp();
+    // integration rows: registers when every face of the warp in this slot is a full
+    // face of this degree's point set, else the global table copy (boundary faces:
+    // Gauss rows; inner faces: the trace rows of the own side)
+    const bool reg_cols = __all_sync(OC_FULL, nfo == 0 || (tsel == 0 && nfo == G));
     if (nfo > 0 && t < N) {  // integrate the own-side values against the own basis
       R cz = 0, c0 = 0, c1 = 0;
-      if (tsel == 0 && nfo == G) {  // full face of this degree's point set
+      if (reg_cols) {
 #pragma unroll
         for (int k = 0; k < G; ++k) {
           cz += fcol[k] * FV[k];
           c0 += fcol[k] * FV[FVS + k];
           c1 += fcol[k] * FV[2 * FVS + k];
         }
-      } else if (tsel > 0 && nfo == G) {  // half of a coarse face, same degree
-#pragma unroll
-        for (int k = 0; k < G; ++k) {
-          const R l = __ldg(&tbg.F[tsel][G][k][t]);
-          cz += l * FV[k];
-          c0 += l * FV[FVS + k];
-          c1 += l * FV[2 * FVS + k];
-        }
       } else {
+        const R *col = tsel < 0 ? &tbg.BQ[0][t] : &tbg.F[tsel][nfo][0][t];  // stride OC_MAXN
 #pragma unroll
         for (int k = 0; k < (Q > OC_MAXF ? Q : OC_MAXF); ++k) {  // nfo <= max(Q, OC_MAXF)
           if (k < nfo) {
-            const R l = tsel < 0 ? tb.BQ[k][t] : __ldg(&tbg.F[tsel][nfo][k][t]);
+            const R l = __ldg(col + k * OC_MAXN);
             cz += l * FV[k];
             c0 += l * FV[FVS + k];
             c1 += l * FV[2 * FVS + k];
