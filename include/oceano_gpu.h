@@ -277,9 +277,10 @@ oc_status oc_conservative_coarsening(oc_op *op, const uint8_t *mark, double *hei
  *                          on a coarse face with two fine neighbours, either),
  *   cell_info[6c + 4]    = refinement level, cell_info[6c + 5] = member index
  *                          (< n_members; the vorticity maximum is taken per member),
- * writes features[12c + 0..11] = cell means of zeta, hu, hv; vorticity w/max;
- *   d/dx, d/dy of w/max from the face neighbours; the four neighbours' w/max;
- *   level; degree.  The vorticity is the reference indicator (max over QGauss(p_max)
+ * writes features[12c + 0..11] = cell means of zeta, hu, hv; L = log10(|w/max| + 1e-12);
+ *   (L(face 1) - L(face 0)) / 2, (L(face 3) - L(face 2)) / 2 from the face neighbours;
+ *   the four neighbours' L; level; degree (the threshold lies decades below the bulk
+ *   of w/max, hence the log scale).  The vorticity is the reference indicator (max over QGauss(p_max)
  *   points of |dv/dx - du/dy|).  flags (may be NULL): 1 where w/max > threshold.
  *   vorticity (may be NULL): w/max per cell. */
 oc_status oc_indicator_features(oc_op *op, const double *zeta, const double *q,

@@ -358,15 +358,16 @@ __global__ void features_kernel(const AuxArgs a, const double *z, const double *
   const float mx = (m >= 0 && m < n_members) ? __uint_as_float(vmax[m]) : 0.f;
   const float inv = mx > 0.f ? 1.f / mx : 0.f;
   const float w0 = w[c] * inv;
+  // vorticity magnitudes relative to the member maximum on a log10 scale: the
+  // refinement threshold (1e-5 of the maximum) sits many decades below the bulk
+  // of the values, where a linear feature is lost in the BF16 inputs
   float nb[4];
-  for (int f = 0; f < 4; ++f) nb[f] = inf[f] >= 0 ? w[inf[f]] * inv : w0;
-  const double *J = a.geo + 11 * (int64_t)c;
-  const float hx = (float)sqrt(J[2] * J[2] + J[4] * J[4]);
-  const float hy = (float)sqrt(J[3] * J[3] + J[5] * J[5]);
+  for (int f = 0; f < 4; ++f) nb[f] = log10f(fabsf(inf[f] >= 0 ? w[inf[f]] * inv : w0) + 1e-12f);
   float *o = feat + 12 * (int64_t)c;
-  o[0] = (float)zm; o[1] = (float)q0; o[2] = (float)q1; o[3] = w0;
-  o[4] = (nb[1] - nb[0]) / (2.f * hx);
-  o[5] = (nb[3] - nb[2]) / (2.f * hy);
+  o[0] = (float)zm; o[1] = (float)q0; o[2] = (float)q1;
+  o[3] = log10f(fabsf(w0) + 1e-12f);
+  o[4] = 0.5f * (nb[1] - nb[0]);  // differences across the cell (faces 1-0, 3-2)
+  o[5] = 0.5f * (nb[3] - nb[2]);
   o[6] = nb[0]; o[7] = nb[1]; o[8] = nb[2]; o[9] = nb[3];
   o[10] = (float)inf[4]; o[11] = (float)p;
   if (flags) flags[c] = w0 > thr ? 1.f : 0.f;

@@ -678,12 +678,10 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   const int nvalid = max(0, min(cpw, n_group - gi0));  // cells of this warp
   const bool valid = member && team < nvalid;
   const int s = a.stage;
-  R fR[OC_MAXSTAGES];  // coefficients in the compute type (mixed form: the FP32 copies)
-  load_coefs<R>(a.dyn->ff, a.dyn->f, fR);
-  R fRs = fR[0];  // f_s
-#pragma unroll
-  for (int j = 1; j < OC_MAXSTAGES; ++j)
-    if (j == a.stage) fRs = fR[j];
+  // programmatic dependent launch: the next launch in the stream may be scheduled
+  // now; it waits (griddepcontrol.wait) for this grid to complete before it reads
+  // what this one writes
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   // the mixed time-step path (FP32 registers) forms internal stage inputs in FP32
   constexpr bool fast = MIX && sizeof(KT) == 4;
   const double zref = MIX ? a.zeta_ref : 0.0;
@@ -747,6 +745,17 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   if (a.cfsdo)
     for (int e = lane; e < nvalid * 8; e += 32)
       w_sdo[e] = a.cfsdo[8 * (int64_t)w_cell[e >> 3] + (e & 7)];
+  // Everything above reads only the mesh (written before the stream's first stage
+  // launch); from here on the kernel reads the previous launch's results and
+  // writes buffers it may still read, so it waits for that launch to complete.
+  // Without a programmatic launch the wait returns at once.
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  R fR[OC_MAXSTAGES];  // coefficients in the compute type (mixed form: the FP32 copies)
+  load_coefs<R>(a.dyn->ff, a.dyn->f, fR);
+  R fRs = fR[0];  // f_s
+#pragma unroll
+  for (int j = 1; j < OC_MAXSTAGES; ++j)
+    if (j == a.stage) fRs = fR[j];
 #pragma unroll 4
   for (int e = lane; e < nvalid * NN; e += 32) {
     const int j = e / NN, d = e - j * NN;
@@ -1786,6 +1795,27 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     if (a.out_q) a.out_q[gq] = nxt;
     if (MIX && a.out_rq) a.out_rq[gq] = (float)(nxt - (d < NN ? qref0 : qref1));
   }
+}
+
+// Launch of a stage kernel with programmatic stream serialization: its blocks may
+// be scheduled while the previous kernel of the stream drains (that kernel lets
+// them with griddepcontrol.launch_dependents); the kernel reads only mesh data
+// before its griddepcontrol.wait.  Valid inside stream capture (the graph keeps
+// a programmatic edge).
+template <typename K>
+static cudaError_t launch_programmatic(K kernel, int grid, int threads, int smem,
+                                       cudaStream_t st, const StageArgs &a) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, a);
 }
 
 // One degree group per launch.

@@ -45,8 +45,8 @@ cudaError_t OC_CAT(configure_stage_hp_v, OC_HP_VARIANT)() {
 cudaError_t OC_CAT(launch_stage_hp_v, OC_HP_VARIANT)(const StageArgs &a, int grid, int wpb,
                                                      cudaStream_t st) {
   if (wpb > kMaxWarpsPerBlock) return cudaErrorInvalidValue;
-  stage_kernel_hp<HpR, HpKT, kHpMix, HpRIN><<<grid, wpb * 32, wpb * hp_warp_bytes(), st>>>(a);
-  return cudaGetLastError();
+  return launch_programmatic(stage_kernel_hp<HpR, HpKT, kHpMix, HpRIN>, grid, wpb * 32,
+                             wpb * hp_warp_bytes(), st, a);
 }
 
 cudaError_t OC_CAT(upload_tables_hp_v, OC_HP_VARIANT)(const DegTables<double> *td,

@@ -26,8 +26,7 @@ static cudaError_t launch_one(const StageArgs &a, int grid, int wpb, cudaStream_
   constexpr int P = OC_DEGREE;
   if (wpb > kMaxWarpsPerBlock) return cudaErrorInvalidValue;
   const int smem = wpb * Dims<P>::template warp_bytes<R>();
-  stage_kernel<P, R, KT, MIX, RIN><<<grid, wpb * 32, smem, st>>>(a);
-  return cudaGetLastError();
+  return launch_programmatic(stage_kernel<P, R, KT, MIX, RIN>, grid, wpb * 32, smem, st, a);
 }
 
 // dynamic shared-memory opt-in, done once at set-up (outside any stream capture)

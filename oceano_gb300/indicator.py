@@ -197,15 +197,18 @@ def training_pairs(records, horizon):
 
 
 def evaluate(model, records, horizon, members, n_members, threshold=0.5):
-    """Precision / recall of the predicted flags `horizon` records ahead and the
-    remesh counts of the vorticity indicator and of the learned indicator."""
+    """Precision / recall of the predicted flags `horizon` records ahead, the
+    remesh counts of the vorticity indicator and of the learned indicator, and
+    the mean size of the learned refinement set (flags or predicted) over the
+    flagged set."""
     import torch
     tp = fp = fn = 0
-    preds, flags = [], []
+    preds, flags, ratio = [], [], []
     for k, (f, fl) in enumerate(records):
         p = model.predict(f, threshold)
         preds.append(p.cpu().numpy())
         flags.append(fl.cpu().numpy() > 0.5)
+        ratio.append((preds[-1] | flags[-1]).sum() / max(flags[-1].sum(), 1))
         if k + horizon < len(records):
             y = records[k + horizon][1] > 0.5
             tp += int((p & y).sum())
@@ -214,4 +217,5 @@ def evaluate(model, records, horizon, members, n_members, threshold=0.5):
     base = remesh_count(flags, None, members, n_members)
     learned = remesh_count(flags, preds, members, n_members)
     return {"precision": tp / max(tp + fp, 1), "recall": tp / max(tp + fn, 1),
-            "remesh_vorticity": base, "remesh_learned": learned}
+            "remesh_vorticity": base, "remesh_learned": learned,
+            "refined_over_flagged": float(np.mean(ratio))}

@@ -110,6 +110,11 @@ def lobatto_weights(n):
     return 0.5 * w
 
 
+def _log_mag(x):
+    """log10(|x| + 1e-12) of FP32 relative vorticities, in FP32."""
+    return np.log10(np.abs(np.asarray(x, f32)) + f32(1e-12)).astype(f32)
+
+
 def features(orc, mesh, z, q, info, n_members, threshold):
     """The 12 features, flags and normalised vorticity of every cell."""
     u = orc.velocity_field(z, q)
@@ -133,13 +138,10 @@ def features(orc, mesh, z, q, info, n_members, threshold):
         feat[c, 1] = W @ q[2 * a:2 * a + n]
         feat[c, 2] = W @ q[2 * a + n:2 * a + 2 * n]
         nb = [w[info[c, f]] * inv[c] if info[c, f] >= 0 else w0[c] for f in range(4)]
-        nb = np.asarray(nb, f32)
-        v = mesh.vertices[c]
-        hx = np.hypot(v[2] - v[0], v[3] - v[1])
-        hy = np.hypot(v[4] - v[0], v[5] - v[1])
-        feat[c, 3] = w0[c]
-        feat[c, 4] = (nb[1] - nb[0]) / (2 * hx)
-        feat[c, 5] = (nb[3] - nb[2]) / (2 * hy)
+        nb = _log_mag(np.asarray(nb, f32))
+        feat[c, 3] = _log_mag(w0[c])
+        feat[c, 4] = 0.5 * (nb[1] - nb[0])
+        feat[c, 5] = 0.5 * (nb[3] - nb[2])
         feat[c, 6:10] = nb
         feat[c, 10] = info[c, 4]
         feat[c, 11] = p
