@@ -183,7 +183,10 @@ oc_status oc_perform_stage_hydro(oc_op *op, uint32_t stage, uint32_t n_stages, d
  * (ExplicitRungeKuttaIntegrator.h:179-298) or AdditiveRungeKuttaIntegrator::
  * perform_time_step (AdditiveRungeKuttaIntegrator.h:206-339), with all stage
  * registers owned by the handle and the stage sequence replayed as a CUDA graph.
- * height/discharge are updated in place.
+ * height/discharge are updated in place.  With OC_MEM_HOST they are copied in;
+ * when both are page-locked (cudaHostAlloc / cudaHostRegister) the last stage
+ * writes u^{n+1} into them directly, overlapping the transfer with the stage,
+ * else they are copied out.  The call returns when the host vectors hold u^{n+1}.
  */
 oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time, double dt,
                                double *height, double *discharge, int32_t memory);

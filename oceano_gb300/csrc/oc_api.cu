@@ -170,6 +170,7 @@ struct oc_op {
   cudaGraphExec_t graph = nullptr;
   int graph_scheme = -1;
   const void *graph_z = nullptr, *graph_q = nullptr;
+  const void *graph_oz = nullptr, *graph_oq = nullptr;  // last-stage outputs of the graph
 };
 
 #define OC_TRY(call)                                                              \
@@ -842,7 +843,7 @@ static oc_status ensure_ts(oc_op *op, const Scheme &sc) {
 
 // arguments of stage st of a time step on the solution (z, q)
 static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, double *q,
-                            StageArgs &a) {
+                            StageArgs &a, double *oz = nullptr, double *oq = nullptr) {
   const bool mixed = op->prm.precision == OC_PREC_MIXED;
   fill_common(op, a);
   {
@@ -863,8 +864,8 @@ static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, doub
     a.out_unqf = (mixed && st == 0) ? op->ts_unqf : nullptr;
     for (int j = 0; j <= sc.s; ++j) a.kz[j] = op->ts_kz[j];
     for (int j = 0; j < 2 * OC_MAXSTAGES; ++j) a.kq[j] = op->ts_kq[j];
-    if (last) {
-      a.out_z = z; a.out_q = q; a.out_rz = nullptr; a.out_rq = nullptr;
+    if (last) {  // u^{n+1} in place, or into (oz, oq) when given
+      a.out_z = oz ? oz : z; a.out_q = oq ? oq : q; a.out_rz = nullptr; a.out_rq = nullptr;
       a.aux_q = sc.ark ? op->ts_aux : nullptr;
     } else if (mixed) {
       a.out_z = nullptr; a.out_q = nullptr;
@@ -878,11 +879,12 @@ static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, doub
 }
 
 // enqueue the stages of one time step on op->stream (capturable)
-static oc_status enqueue_step(oc_op *op, const Scheme &sc, double *z, double *q) {
+static oc_status enqueue_step(oc_op *op, const Scheme &sc, double *z, double *q,
+                              double *oz = nullptr, double *oq = nullptr) {
   const bool mixed = op->prm.precision == OC_PREC_MIXED;
   for (int st = 0; st < sc.s; ++st) {
     StageArgs a;
-    step_stage_args(op, sc, st, z, q, a);
+    step_stage_args(op, sc, st, z, q, a, oz, oq);
     oc_status s = launch_groups(op, a, mixed ? 1 : 0);
     if (s != OC_OK) return s;
   }
@@ -982,6 +984,18 @@ static oc_status autotune(oc_op *op, const Scheme &sc, const double *z, const do
   return read_error(op);
 }
 
+// Device address of a page-locked host buffer (cudaHostAlloc / cudaHostRegister),
+// or NULL for pageable memory.
+static double *mapped_host(double *p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();  // pageable memory may report an error on older drivers
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+  return static_cast<double *>(at.devicePointer);
+}
+
 extern "C" oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time, double dt,
                                           double *z, double *q, int32_t memory) {
   if (!op || !z || !q) return OC_ERR_INVALID_ARG;
@@ -993,11 +1007,17 @@ extern "C" oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time
   if (st != OC_OK) return st;
   const size_t nz = op->n_dofs, nq = 2 * nz;
   double *dz = z, *dq = q;
+  // host vectors: copied in; the last stage writes u^{n+1} straight into them when
+  // both are page-locked host memory the GPU can address (over NVLink-C2C on
+  // Grace-Blackwell, overlapping the transfer with the stage), else copied out
+  double *oz = nullptr, *oq = nullptr;
   if (memory == OC_MEM_HOST) {
     if (ensure(op, &op->ts_z, nz) || ensure(op, &op->ts_q, nq)) return OC_ERR_CUDA;
     OC_TRY(cudaMemcpyAsync(op->ts_z, z, nz * 8, cudaMemcpyHostToDevice, op->stream));
     OC_TRY(cudaMemcpyAsync(op->ts_q, q, nq * 8, cudaMemcpyHostToDevice, op->stream));
     dz = op->ts_z; dq = op->ts_q;
+    oz = mapped_host(z); oq = mapped_host(q);
+    if (!oz || !oq) oz = oq = nullptr;
   }
   // coefficients: rows a_i[stage] (b_i at the last stage) times dt
   for (int s = 0; s < sc.s; ++s) {
@@ -1018,12 +1038,13 @@ extern "C" oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time
     st = autotune(op, sc, dz, dq);
     if (st != OC_OK) return st;
   }
-  if (!op->graph || op->graph_scheme != scheme || op->graph_z != dz || op->graph_q != dq) {
+  if (!op->graph || op->graph_scheme != scheme || op->graph_z != dz || op->graph_q != dq ||
+      op->graph_oz != oz || op->graph_oq != oq) {
     if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
     cudaGraph_t g;
     OC_TRY(cudaStreamBeginCapture(op->stream, cudaStreamCaptureModeThreadLocal));
     const int64_t before = op->launches;
-    st = enqueue_step(op, sc, dz, dq);
+    st = enqueue_step(op, sc, dz, dq, oz, oq);
     cudaError_t ce = cudaStreamEndCapture(op->stream, &g);
     op->graph_launches = op->launches - before;
     op->launches = before;
@@ -1032,12 +1053,15 @@ extern "C" oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time
     OC_TRY(cudaGraphInstantiate(&op->graph, g, 0));
     cudaGraphDestroy(g);
     op->graph_scheme = scheme; op->graph_z = dz; op->graph_q = dq;
+    op->graph_oz = oz; op->graph_oq = oq;
   }
   OC_TRY(cudaGraphLaunch(op->graph, op->stream));
   op->launches += op->graph_launches;
   if (memory == OC_MEM_HOST) {
-    OC_TRY(cudaMemcpyAsync(z, op->ts_z, nz * 8, cudaMemcpyDeviceToHost, op->stream));
-    OC_TRY(cudaMemcpyAsync(q, op->ts_q, nq * 8, cudaMemcpyDeviceToHost, op->stream));
+    if (!oz) {
+      OC_TRY(cudaMemcpyAsync(z, op->ts_z, nz * 8, cudaMemcpyDeviceToHost, op->stream));
+      OC_TRY(cudaMemcpyAsync(q, op->ts_q, nq * 8, cudaMemcpyDeviceToHost, op->stream));
+    }
     return read_error(op);
   }
   return OC_OK;

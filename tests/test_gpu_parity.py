@@ -247,6 +247,48 @@ def test_time_step_matches_stages(gpu_lib):
 TAB = O.TABLEAUX["ssp33"]
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_time_step_host_buffers(gpu_lib, precision):
+    """oc_perform_time_step on host vectors: page-locked buffers (the last stage
+    writes u^{n+1} into them directly) and pageable ones (copied back) give the
+    bits of the device-vector run, over several steps and a change of buffers."""
+    import ctypes as C
+    import torch
+    from oceano_gb300 import _lib
+    kw = dict(precision="mixed", zeta_reference=1.0) if precision == "mixed" else {}
+    mesh, orc, op = setup("mixed_degree", **kw)
+    z, q = perturbed_state(orc, 3)
+    dt = 0.05 / orc.transport_speed(z, q)
+    zd, qd = torch.from_numpy(z.copy()).cuda(), torch.from_numpy(q.copy()).cuda()
+    pinned = [(torch.from_numpy(z.copy()).pin_memory(), torch.from_numpy(q.copy()).pin_memory())
+              for _ in range(2)]
+    zp, qp = z.copy(), q.copy()
+
+    def host_step(t, zh, qh):
+        _lib.check(_lib.lib().oc_perform_time_step(op.h, _lib.SCHEME["ssp33"], t, dt,
+                                                   C.c_void_p(zh.data_ptr()),
+                                                   C.c_void_p(qh.data_ptr()), _lib.OC_MEM_HOST),
+                   op.h)
+
+    for it in range(4):
+        t = it * dt
+        op.perform_time_step("ssp33", t, dt, zd, qd)
+        a, b = pinned[it % 2]
+        host_step(t, a, b)
+        if it % 2 == 0:  # the other pair follows with a copy of the state
+            pinned[1][0].copy_(a)
+            pinned[1][1].copy_(b)
+        else:
+            pinned[0][0].copy_(a)
+            pinned[0][1].copy_(b)
+        op.perform_time_step("ssp33", t, dt, zp, qp)
+    torch.cuda.synchronize()
+    zr, qr = zd.cpu().numpy(), qd.cpu().numpy()
+    a, b = pinned[1]
+    assert np.array_equal(a.numpy(), zr) and np.array_equal(b.numpy(), qr)
+    assert np.array_equal(zp, zr) and np.array_equal(qp, qr)
+
+
 def test_unknown_boundary_id(gpu_lib):
     from oceano_gb300._lib import OceanoError
     from oceano_gb300.operator import OceanoOperator
