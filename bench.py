@@ -63,45 +63,79 @@ class Workload:
     """Operators (mixed, FP64), initial state, dt and scheme of one workload,
     and a factory of the matching FP64 oracle for the CPU baseline."""
 
-    def __init__(self, name):
+    def __init__(self, name, gpu=True):
+        """gpu=False builds the mesh, initial state and dt on the host only (the
+        reference arm: no GPU operator, the state projected by the oracle)."""
         from oceano_gb300 import workloads as W
         self.name = name
         self.scheme = "ssp33"
+        self.op_m = self.op_d = None
+        z0 = q0 = None
         if name == "vortex":
             mesh, vx = workload()
-            self.op_m, self.op_d = make_op(mesh, vx, "mixed"), make_op(mesh, vx, "fp64")
-            n = self.op_d.n_dofs
-            self.z0, self.q0 = np.zeros(n), np.zeros(2 * n)
-            self.op_d.project_vortex(0.0, self.z0, self.q0)
+            if gpu:
+                self.op_m, self.op_d = make_op(mesh, vx, "mixed"), make_op(mesh, vx, "fp64")
+                n = self.op_d.n_dofs
+                z0, q0 = np.zeros(n), np.zeros(2 * n)
+                self.op_d.project_vortex(0.0, z0, q0)
             self.desc = "vortex p=3, 320x160 cells (51200), 2457600 DoFs, SSP-RK3 step"
             self.oracle_kw = dict(bcs={0: ("wall",)}, vortex=list(vx) + [0, 0])
         elif name == "hp":
-            self.op_m, self.z0, self.q0 = W.hp_vortex("mixed")
-            self.op_d, _, _ = W.hp_vortex("fp64")
-            self.desc = (f"vortex on the seeded random hp mesh ({self.op_d.mesh.n_cells} cells, "
+            if gpu:
+                self.op_m, z0, q0 = W.hp_vortex("mixed")
+                self.op_d, _, _ = W.hp_vortex("fp64")
+                mesh = self.op_d.mesh
+            else:
+                from oceano_gb300 import random_hp_mesh
+                mesh = random_hp_mesh(seed=20261203, target=60000)
+            self.desc = (f"vortex on the seeded random hp mesh ({mesh.n_cells} cells, "
                          f"p=1..4, hanging faces), SSP-RK3 step")
             self.oracle_kw = dict(bcs={0: ("wall",)}, vortex=list(W.vortex_params()) + [0, 0])
         elif name == "channel":
-            self.op_m, self.z0, self.q0 = W.channel("mixed")
-            self.op_d, _, _ = W.channel("fp64")
+            if gpu:
+                self.op_m, z0, q0 = W.channel("mixed")
+                self.op_d, _, _ = W.channel("fp64")
+                mesh = self.op_d.mesh
+            else:
+                from oceano_gb300.mesh import channel_mesh
+                mesh = channel_mesh(2, 250, 10)
+                z0, q0 = W.uniform_state(mesh, 0.0, (W.CHANNEL_Q_IN, 0.0))
             self.scheme = "ark_stage3_order2"
             self.desc = ("channel 250x10 cells p=2, bump, implicit Manning n=0.03, "
                          "ARK stage_3_order_2 step")
             self.oracle_kw = dict(friction=2, bcs=W.CHANNEL_BCS)
         elif name == "ensemble":
-            self.op_m, self.z0, self.q0, members, meshes = W.ensemble(64, "mixed")
-            self.op_d = W.vortex_operator(self.op_m.mesh, "fp64", members[0]["vortex"])
-            self.desc = (f"64-member vortex ensemble, {self.op_d.mesh.n_cells} cells "
+            if gpu:
+                self.op_m, z0, q0, members, meshes = W.ensemble(64, "mixed")
+                self.op_d = W.vortex_operator(self.op_m.mesh, "fp64", members[0]["vortex"])
+                mesh = self.op_d.mesh
+            else:
+                from oceano_gb300.mesh import concatenate_meshes
+                members = W.ensemble_members(64, 1000)
+                meshes = [W.member_mesh(m) for m in members]
+                mesh = concatenate_meshes(meshes)
+                zs, qs = zip(*[W.vortex_nodal_state(m, mm["vortex"]) for m, mm in zip(meshes, members)])
+                z0, q0 = np.concatenate(zs), np.concatenate(qs)
+            self.desc = (f"64-member vortex ensemble, {mesh.n_cells} cells "
                          f"(5k-40k per member, p=1,2), one operator, SSP-RK3 step")
             self.oracle_kw = dict(bcs={0: ("wall",)})
         else:
             raise ValueError(name)
-        self.mesh = self.op_d.mesh
-        self.n = self.op_d.n_dofs
+        self.mesh = mesh
         # degree-4 cells at the finest level of the hp mesh need a smaller Courant
         # number (CFL 0.075 diverges there within 20 steps, in the oracle as well)
         self.cfl = {"vortex": CFL_VORTEX, "hp": CFL_HP}.get(name, CFL)
-        self.dt = self.cfl / self.op_d.compute_cell_transport_speed(self.z0, self.q0)
+        if gpu:
+            self.n = self.op_d.n_dofs
+            self.z0, self.q0 = z0, q0
+            self.dt = self.cfl / self.op_d.compute_cell_transport_speed(self.z0, self.q0)
+        else:
+            orc = self.oracle()
+            if z0 is None:
+                z0, q0 = orc.project_vortex(0.0)
+            self.n = orc.n
+            self.z0, self.q0 = z0, q0
+            self.dt = self.cfl / orc.transport_speed(self.z0, self.q0)
 
     def oracle(self):
         from oracle import oracle as O
@@ -327,7 +361,7 @@ def run_reference(args, rank, world):
     """CPU restatement timed on the host cores (rank 0 only)."""
     if rank != 0:
         return
-    wl = Workload(args.workload)
+    wl = Workload(args.workload, gpu=False)
     orc = wl.oracle()
     z, q = wl.z0.copy(), wl.q0.copy()
     for i in range(args.warmup):
