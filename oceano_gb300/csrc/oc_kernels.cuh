@@ -295,14 +295,23 @@ __device__ __forceinline__ R load_r(const void *p, int64_t i, int is_float, doub
 }
 
 // stage-input load with the input precision fixed at compile time (a runtime
-// switch would let the compiler evaluate both branches)
+// switch would let the compiler evaluate both branches).  Read-only loads
+// (ld.global.nc): the stage inputs are not written during the launch, and the
+// compiler may then issue the loads of several elements ahead of the shared-memory
+// stores of the earlier ones (one memory round trip instead of one per element).
 template <typename RIN, typename R>
 __device__ __forceinline__ R load_in(const void *p, int64_t i, double ref) {
   if constexpr (sizeof(RIN) == 4) {
-    return (R)(static_cast<const float *>(p)[i]);
+    return (R)__ldg(static_cast<const float *>(p) + i);
   } else {
-    return (R)(static_cast<const double *>(p)[i] - ref);
+    return (R)(__ldg(static_cast<const double *>(p) + i) - ref);
   }
+}
+
+// read-only load of a stage register (FP32 or FP64)
+template <typename KT>
+__device__ __forceinline__ KT ldro(const void *p, int64_t i) {
+  return __ldg(static_cast<const KT *>(p) + i);
 }
 
 // stride of the per-variable face point values (>= OC_MAXF and OC_MAXQ)
@@ -731,12 +740,16 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   R gR[11];  // geometry in the compute type (FP32 copy in the mixed form); loads issued early
 #pragma unroll
   for (int k = 0; k < 11; ++k) {
-    if constexpr (MIX) gR[k] = (R)a.geof[11 * (int64_t)cell + k];
-    else gR[k] = (R)geo[k];
+    if constexpr (MIX) gR[k] = (R)__ldg(a.geof + 11 * (int64_t)cell + k);
+    else gR[k] = (R)__ldg(geo + k);
   }
-  for (int e = lane; e < nvalid * 16; e += 32) {  // face records (invalid teams: empty)
-    const int j = e >> 4, k = e & 15;
-    w_rec[j * 16 + k] = a.cfrec[16 * (int64_t)w_cell[j] + k];
+#pragma unroll
+  for (int i = 0; i < (CPWMAX * 16 + 31) / 32; ++i) {  // face records (invalid teams: empty)
+    const int e = lane + 32 * i;
+    if (e < nvalid * 16) {
+      const int j = e >> 4, k = e & 15;
+      w_rec[j * 16 + k] = __ldg(a.cfrec + 16 * (int64_t)w_cell[j] + k);
+    }
   }
   for (int e = lane; e < (CPWMAX - nvalid) * 16; e += 32) {
     const int j = nvalid + (e >> 4);
@@ -756,8 +769,12 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
   for (int j = 1; j < OC_MAXSTAGES; ++j)
     if (j == a.stage) fRs = fR[j];
-#pragma unroll 4
-  for (int e = lane; e < nvalid * NN; e += 32) {
+  // stage input: element e = lane + 32 i of the warp's cells (compile-time trip
+  // count, so that the loads of all elements are issued before the stores)
+#pragma unroll
+  for (int i = 0; i < (CPWMAX * NN + 31) / 32; ++i) {
+    const int e = lane + 32 * i;
+    if (e >= nvalid * NN) break;
     const int j = e / NN, d = e - j * NN;
     const int64_t oz = w_off[j] + d, oq = 2 * (int64_t)w_off[j] + d;
     R *Uj = Rreg(j);
@@ -773,13 +790,12 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
       for (int jj = 0; jj < OC_MAXSTAGES; ++jj)
         if (jj < s) {
-          const KT *kqj = static_cast<const KT *>(a.kq[jj + 1]);
-          qb0 += fR[jj] * (R)kqj[oq];
-          qb1 += fR[jj] * (R)kqj[oq + NN];
+          qb0 += fR[jj] * (R)ldro<KT>(a.kq[jj + 1], oq);
+          qb1 += fR[jj] * (R)ldro<KT>(a.kq[jj + 1], oq + NN);
         }
       if (!a.last) {
-        qb0 += s == 0 ? uq0 : (R)a.un_qf[oq];
-        qb1 += s == 0 ? uq1 : (R)a.un_qf[oq + NN];
+        qb0 += s == 0 ? uq0 : (R)__ldg(a.un_qf + oq);
+        qb1 += s == 0 ? uq1 : (R)__ldg(a.un_qf + oq + NN);
       }
       Uj[6 * NN + d] = qb0;
       Uj[7 * NN + d] = qb1;
@@ -789,13 +805,13 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
       for (int jj = 0; jj < OC_MAXSTAGES; ++jj)  // compile-time indices: fR stays in registers
         if (jj < s)
-          bprev = jj == 0 ? fR[0] * (R) static_cast<const KT *>(a.kz[1])[oz]
-                          : bprev + fR[jj] * (R) static_cast<const KT *>(a.kz[jj + 1])[oz];
+          bprev = jj == 0 ? fR[0] * (R)ldro<KT>(a.kz[1], oz)
+                          : bprev + fR[jj] * (R)ldro<KT>(a.kz[jj + 1], oz);
       Uj[8 * NN + d] = bprev;
       if constexpr (fast) {
-        Uj[9 * NN + d] = s == 0 ? Uj[d] : (R)a.un_zf[oz];
+        Uj[9 * NN + d] = s == 0 ? Uj[d] : (R)__ldg(a.un_zf + oz);
       } else if constexpr (MIX) {
-        Uj[9 * NN + d] = (R)(a.un_z[oz] - zref);
+        Uj[9 * NN + d] = (R)(__ldg(a.un_z + oz) - zref);
       }
     }
   }
@@ -1015,7 +1031,10 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   // tiles (free between the cell integrals and the zeta solve); a smaller team
   // region leaves more of the SM's shared memory / L1 to the L1 cache
   if (member) {
-    for (int e = t; e < 8 * OC_MAXN; e += T) {
+#pragma unroll
+    for (int ii = 0; ii < (8 * OC_MAXN + T - 1) / T; ++ii) {
+      const int e = t + ii * T;
+      if (e >= 8 * OC_MAXN) break;
       const int sl = e / OC_MAXN, i = e - sl * OC_MAXN;
       const FaceRec r = recs[sl];
       const int Nn = r.nb_deg() + 1;
