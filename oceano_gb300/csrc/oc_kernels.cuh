@@ -654,10 +654,10 @@ __device__ __forceinline__ void load_coefs(const float *ff, const double *fd,
 //   MIX = false: FP64 plain form (R = KT = double).
 //   MIX = true : mixed form; R = float bulk, KT = type of the k registers.
 // Memory flow: warp-cooperative prologue (stage input, face records, partial
-// zeta right-hand side), neighbour traces of all face slots prefetched into
-// shared memory, team-local compute, warp-cooperative epilogue (RK update and
-// stores).  Global accesses of the prologue/epilogue are lane-contiguous over
-// the warp's cells.
+// zeta right-hand side), team-local cell integrals, neighbour traces of all face
+// slots loaded into the scratch tiles for the face phase, team-local zeta and
+// discharge solves, warp-cooperative epilogue (RK update and stores).  Global
+// accesses of the prologue/epilogue are lane-contiguous over the warp's cells.
 // ---------------------------------------------------------------------------
 // resident 4-warp blocks per SM the mixed kernels are compiled for (register cap)
 #ifndef OC_MIXED_MIN_BLOCKS
