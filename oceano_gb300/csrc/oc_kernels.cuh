@@ -854,7 +854,10 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     if (member && t < Q) {  // y-pass, pointwise model, y-integration on column qx = t
       const double *sd0 = a.sd0 ? a.sd0 + a.sdo0[cell] : nullptr;
       const float *sd0e = a.sd0e ? a.sd0e + a.sdo0[cell] : nullptr;
-#pragma unroll
+      // not unrolled: the point loop is the largest block of the kernel, and a
+      // smaller instruction footprint leaves fewer warps waiting on instruction
+      // fetch (the shape coefficients become uniform constant loads)
+#pragma unroll 1
       for (int qy = 0; qy < Q; ++qy) {
         R z = 0, zx = 0, zy = 0, q0 = 0, q1 = 0;
 #pragma unroll
@@ -1660,7 +1663,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   }
   // S^-1 diag(coef) S^-T applied to the two discharge components of RES (in place)
   if (member && t < N) {  // x-pass: A[iy][qx] = sum_ix Sinv[ix][qx] in[iy][ix]
-#pragma unroll
+#pragma unroll 1  // component loop kept rolled (instruction footprint)
     for (int e = 0; e < 2; ++e)
 #pragma unroll
       for (int qx = 0; qx < N; ++qx) {
@@ -1672,7 +1675,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   }
   __syncwarp();
   if (member && t < N) {  // y on column qx = t: scale, back-transform in y
-#pragma unroll
+#pragma unroll 1  // component loop kept rolled (instruction footprint)
     for (int e = 0; e < 2; ++e) {
       R bq[N];
 #pragma unroll
@@ -1693,7 +1696,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   }
   __syncwarp();
   if (member && t < N) {  // x back-transform into RES_q
-#pragma unroll
+#pragma unroll 1  // component loop kept rolled (instruction footprint)
     for (int e = 0; e < 2; ++e)
 #pragma unroll
       for (int ix = 0; ix < N; ++ix) {
