@@ -12,8 +12,15 @@ value    : mixed form (FP32 bulk, FP64 accumulation), inputs resident in HBM,
 fp64     : the plain FP64 form on the same GPU.
 e2e      : mixed form through the public C ABI with pinned host buffers, copies
            in and out inside the timed region.
-roofline : dominant kernel = the fused stage kernel; algorithmic bytes per
-           DoF-stage as documented in DESIGN.md; peak from MEASURED_PEAKS.json.
+e2e_stage_abi: the literal drop-in call, three oc_perform_stage_hydro calls
+           per step on host vectors with host-side registers (every stage
+           copies its inputs in and its outputs out), mixed form.
+roofline : dominant kernel = the fused stage kernel; algorithmic bytes per step
+           = per scalar DoF and stage the stage input, u^n and the stage output
+           at their stored precision, plus 5 doubles of geometry per cell;
+           peak from MEASURED_PEAKS.json.  `traffic` (DRAM bytes per launch)
+           comes from an ncu capture of the same kernel (`traffic_source`
+           names it); a bench run does not run under ncu.
 cpu_baseline / --impl reference: the FP64 C oracle (CPU restatement; the
            reference itself needs deal.II + MPI) with OpenMP on all host cores.
 
@@ -181,14 +188,21 @@ def algorithmic_bytes(n_dofs_var, n_cells, mixed, static_bytes=0):
     return n * per_dof + 3 * n_cells * 5 * 8 + 3 * static_bytes
 
 
-def measured_traffic():
-    """DRAM bytes per stage launch from the committed ncu summary, or None."""
-    p = os.path.join(ROOT, "profiles", "stage_kernel_p3_mixed_vortex320x160_traffic.md")
+TRAFFIC_PROFILE = os.path.join("profiles", "stage_kernel_p3_mixed_vortex320x160_traffic.md")
+
+
+def profiled_traffic():
+    """DRAM bytes per stage launch and warp instructions per launch from the ncu
+    summary of the stage kernel (profiles/), or None: these counters exist only
+    under ncu, which never runs inside a timed bench."""
+    p = os.path.join(ROOT, TRAFFIC_PROFILE)
+    out = {}
     if os.path.exists(p):
         for line in open(p):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":")[1])
-    return None
+            for key in ("traffic_bytes_per_launch", "warp_instructions_per_launch"):
+                if line.startswith(key + ":"):
+                    out[key] = float(line.split(":")[1])
+    return out
 
 
 def peaks():
@@ -306,6 +320,49 @@ def _host_step(op, t, dt, zh, qh, scheme="ssp33"):
                                                C.c_void_p(zh.data_ptr()),
                                                C.c_void_p(qh.data_ptr()), _lib.OC_MEM_HOST),
                op.h)
+
+
+def time_e2e_stage_abi(op, z0, q0, steps, warmup, dt):
+    """The drop-in call of the reference's integrator loop: per step three
+    oc_perform_stage_hydro calls (SSP-RK3, ExplicitRungeKuttaIntegrator.h:179-298)
+    on pinned host vectors with host-side registers, so that every stage copies
+    its inputs in and its outputs out.  Returns ms per step and the bytes moved
+    each way per step."""
+    import torch
+    a = [[1.0], [0.25, 0.25]]  # SSP-RK3 Butcher rows (time_stepping.h:170-192)
+    b = [1 / 6, 1 / 6, 2 / 3]
+    c = [0.0, 1.0, 0.5]
+    n = z0.size
+
+    def pinned(x):  # NumPy view of page-locked host memory
+        return torch.from_numpy(np.ascontiguousarray(x)).pin_memory().numpy()
+
+    z, q = pinned(z0.copy()), pinned(q0.copy())
+    kz = [pinned(np.zeros(n)) for _ in range(4)]
+    kq = [pinned(np.zeros(2 * n)) for _ in range(4)]
+    nz, nq = pinned(np.zeros(n)), pinned(np.zeros(2 * n))
+    rz, rq = pinned(np.zeros(n)), pinned(np.zeros(2 * n))
+
+    def step(t):
+        for st in range(3):
+            f = np.array(b if st == 2 else a[st], np.float64) * dt
+            if st == 0:
+                rz[:] = z; rq[:] = q
+            else:
+                rz[:] = nz; rq[:] = nq
+            op.perform_stage_hydro(st, 3, t + c[st] * dt, f, [rz, rq], kz, kq, z, q, nz, nq)
+
+    for i in range(warmup):
+        step(i * dt)
+    t0 = time.perf_counter()
+    for i in range(steps):
+        step((warmup + i) * dt)
+    el = time.perf_counter() - t0
+    nb = 8 * n
+    # per stage s: in r, u^n (3 vectors' worth each) and k_1..k_s; out k_{s+1} and next/solution
+    h2d = sum(3 * nb * (2 + s) for s in range(3))
+    d2h = 3 * 3 * nb * 2
+    return 1e3 * el / steps, h2d, d2h
 
 
 def cpu_baseline(wl, steps):
@@ -481,13 +538,16 @@ def main():
     barrier(world)
     legs = set(args.legs.split(","))
     with Clocks() as clk:  # samples over both timed loops (the mixed one alone is ~30 ms)
-        ms_m, zm, qm, launches = time_device(wl.op_m, mesh, z0, q0, args.steps, args.warmup, dt,
-                                             flush, wl.scheme)
+        if "mixed" in legs:
+            ms_m, zm, qm, launches = time_device(wl.op_m, mesh, z0, q0, args.steps, args.warmup,
+                                                 dt, flush, wl.scheme)
         if "fp64" in legs:
-            ms_d, zd, qd, _ = time_device(wl.op_d, mesh, z0, q0, args.steps, args.warmup, dt,
-                                          flush, wl.scheme)
+            ms_d, zd, qd, launches_d = time_device(wl.op_d, mesh, z0, q0, args.steps,
+                                                   args.warmup, dt, flush, wl.scheme)
         else:
             ms_d, zd, qd = [float("nan")], zm, qm
+        if "mixed" not in legs:  # FP64-only run (profiling of the FP64 kernel)
+            ms_m, zm, qm, launches = ms_d, zd, qd, launches_d
     t_m = max_over_ranks(sum(ms_m) / 1e3, world)
     t_d = max_over_ranks(sum(ms_d) / 1e3, world)
     ndof = 3 * n
@@ -499,6 +559,14 @@ def main():
         if "e2e" in legs else (float("nan"), 0)
     e2e_ms = max_over_ranks(e2e_ms, world)
     e2e_value = ndof * stages * world / (e2e_ms / 1e3)
+    stage_abi = None
+    if "e2e" in legs and wl.scheme == "ssp33":
+        sa_ms, sa_in, sa_out = time_e2e_stage_abi(wl.op_m, z0, q0, max(2, args.steps // 10), 1, dt)
+        sa_ms = max_over_ranks(sa_ms, world)
+        stage_abi = {"value": ndof * stages * world / (sa_ms / 1e3), "unit": "DoF-stage/s",
+                     "ms_per_step": sa_ms, "h2d_bytes_per_step": sa_in,
+                     "d2h_bytes_per_step": sa_out,
+                     "call": "3 x oc_perform_stage_hydro(OC_MEM_HOST) per step, host registers"}
     peak, peak_kind = peaks()
     static_bytes = 4 * sum(wl.op_m.static_data_size(k) for k in range(5)) \
         if wl.name == "channel" else 0
@@ -508,6 +576,17 @@ def main():
     achieved = bytes_step / per_step_launches / (step_s / per_step_launches) / 1e9
     clocks = clk.summary()
     err_z, err_q = rel(zm, zd), rel(qm, qd)
+    vortex = args.workload == "vortex"
+    prof = profiled_traffic() if vortex else {}
+    issue = None
+    if prof.get("warp_instructions_per_launch") and clocks.get("sm_mhz"):
+        # issue-rate roofline: 4 warp schedulers per SM, one instruction per clock each
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        launch_s = step_s / per_step_launches
+        peak_issue = 4 * sms * clocks["sm_mhz"] * 1e6
+        ach = prof["warp_instructions_per_launch"] / launch_s
+        issue = {"achieved": ach / 1e9, "peak": peak_issue / 1e9, "unit": "G warp-inst/s",
+                 "frac": ach / peak_issue, "source": "instructions: ncu capture, " + TRAFFIC_PROFILE}
     out = {
         "metric": METRIC, "value": value, "unit": "DoF-stage/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_m / args.steps,
@@ -523,12 +602,15 @@ def main():
         "l2_error_vs_fp64": {"zeta": err_z, "hu_hv": err_q, "after_steps": args.warmup + args.steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
-                     "traffic": measured_traffic() if args.workload == "vortex" else None,
+                     "traffic": prof.get("traffic_bytes_per_launch") if vortex else None,
+                     "traffic_source": ("ncu capture, " + TRAFFIC_PROFILE) if vortex else None,
                      "peak_source": peak_kind,
                      "kernel": "oc::stage_kernel (mixed, FP32 stage input)",
                      "algorithmic_bytes_per_step": bytes_step},
         "e2e": {"value": e2e_value, "unit": "DoF-stage/s", "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes},
+        "e2e_stage_abi": stage_abi,
+        "issue_roofline": issue,
         "gpu_launches": launches,
         "clocks": clocks,
     }

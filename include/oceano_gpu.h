@@ -186,7 +186,9 @@ oc_status oc_perform_stage_hydro(oc_op *op, uint32_t stage, uint32_t n_stages, d
  * height/discharge are updated in place.  With OC_MEM_HOST they are copied in;
  * when both are page-locked (cudaHostAlloc / cudaHostRegister) the last stage
  * writes u^{n+1} into them directly, overlapping the transfer with the stage,
- * else they are copied out.  The call returns when the host vectors hold u^{n+1}.
+ * else they are copied out.  The call returns when the host vectors hold u^{n+1}
+ * (and reports device-side errors); with OC_MEM_DEVICE it returns once the step
+ * is enqueued, and oc_synchronize reports its device-side errors.
  */
 oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time, double dt,
                                double *height, double *discharge, int32_t memory);
@@ -219,15 +221,19 @@ oc_status oc_project_vortex(oc_op *op, double time, double *height, double *disc
 
 /*
  * Transport-speed maximum without any device allocation.  No counterpart in
- * the reference: it serves callers that cannot call cudaMalloc when they need
- * dt (code running during CUDA-graph stream capture, hosts whose device memory
- * belongs to a pool or arena, allocation-free real-time loops).  height and
- * discharge are device vectors, speed is one device double written on the
- * handle's stream (NaN if the state holds a non-finite value); the call does
- * not synchronise.  Scratch is a fixed device array inside the library: at most
- * 524,288 cells (else OC_ERR_UNSUPPORTED); calls that overlap on the GPU share
- * it and race; the first call on a device sets it up and must come before any
- * stream capture.
+ * the reference: it serves callers that may not call cudaMalloc when they need
+ * dt (hosts whose device memory belongs to a pool or arena they must not
+ * bypass, real-time loops that forbid allocation after start-up, embedding
+ * frameworks that account for every device byte).  height and discharge are
+ * device vectors, speed is one device double written on the handle's stream
+ * (NaN if a point speed is not finite, where oc_transport_speed returns
+ * OC_ERR_NONFINITE); the call does not synchronise.  Scratch is a fixed device
+ * array inside the library: at most 524,288 cells (else OC_ERR_UNSUPPORTED,
+ * before any launch); calls that overlap on the GPU share it and race.  The
+ * first call on a device sets it up (once per device, thread-safe) and should
+ * come before any stream capture; a device reset after that call is not
+ * supported.  Failures set oc_last_error; a CUDA error pending from earlier
+ * work is reported (OC_ERR_CUDA) and not cleared.
  */
 oc_status oc_transport_speed_noalloc(oc_op *op, const double *height, const double *discharge,
                                      double *speed);
@@ -317,8 +323,13 @@ oc_status oc_mlp_gradient(oc_mlp *m, const float *features, const float *labels,
 /* one Adam step (beta 0.9, 0.999, eps 1e-8) with the handle's gradient */
 oc_status oc_mlp_adam_step(oc_mlp *m, float lr);
 
-/* device synchronisation and the stream the handle launches on */
+/* Waits for the handle's stream, then reports and clears the device-side error
+ * flags raised since the last check: OC_ERR_UNKNOWN_BOUNDARY_ID from a face
+ * kernel, OC_ERR_NONFINITE when a time step or a last stage wrote a non-finite
+ * u^{n+1}.  Calls on device vectors (OC_MEM_DEVICE) return without waiting, so
+ * their device-side errors surface here (or at the next call on host vectors). */
 oc_status oc_synchronize(oc_op *op);
+/* the stream the handle launches on */
 void *oc_stream(oc_op *op);
 /* kernels launched by this handle since creation (launch accounting) */
 int64_t oc_launch_count(const oc_op *op);

@@ -57,6 +57,6 @@ def load(path) -> Checkpoint:
         extra = {k[6:]: d[k] for k in d.files if k.startswith("extra_")}
         ck = Checkpoint(mesh, d["height"].copy(), d["discharge"].copy(), float(d["time"]),
                         int(d["step"]), extra)
-    if ck.height.size != mesh.n_dofs():
+    if ck.height.size != mesh.n_dofs() or ck.discharge.size != 2 * mesh.n_dofs():
         raise ValueError(f"{path}: state size does not match the mesh")
     return ck

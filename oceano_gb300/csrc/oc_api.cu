@@ -146,6 +146,7 @@ struct oc_op {
   void *ts_kz[OC_MAXSTAGES + 1] = {nullptr}, *ts_kq[2 * OC_MAXSTAGES] = {nullptr};
   void *ts_rz[2] = {nullptr, nullptr}, *ts_rq[2] = {nullptr, nullptr};
   double *ts_z = nullptr, *ts_q = nullptr;  // solution when the caller passes host memory
+  double *ts_z0 = nullptr, *ts_q0 = nullptr;  // one-stage schemes: copy of u^n (stage input)
   double *ts_aux = nullptr;
   float *ts_unzf = nullptr, *ts_unqf = nullptr;  // FP32 copies of u^n (mixed time step)
   // mixed form reference state (FP32-representable values)
@@ -235,6 +236,8 @@ static cudaError_t launch_stage_hp(int hv, const StageArgs &a, int grid, int wpb
   }
 }
 
+static oc_status read_error(oc_op *op);
+
 extern "C" {
 
 const char *oc_last_error(const oc_op *op) { return op ? op->err.c_str() : "null handle"; }
@@ -273,8 +276,7 @@ oc_status oc_launch_config(const oc_op *op, int32_t *out) {
 
 oc_status oc_synchronize(oc_op *op) {
   if (!op) return OC_ERR_INVALID_ARG;
-  OC_TRY(cudaStreamSynchronize(op->stream));
-  return OC_OK;
+  return read_error(op);  // waits for the stream, reports and clears the device flags
 }
 
 void oc_destroy(oc_op *op) {
@@ -834,6 +836,10 @@ static oc_status ensure_ts(oc_op *op, const Scheme &sc) {
     if (!op->ts_rq[j]) OC_TRY(alloc(op, &op->ts_rq[j], nq * rs));
   }
   if (sc.ark && !op->ts_aux) OC_TRY(alloc(op, (void **)&op->ts_aux, nq * 8));
+  if (sc.s == 1 && !op->ts_z0) {  // the single stage writes u^{n+1} over u^n
+    OC_TRY(alloc(op, (void **)&op->ts_z0, nz * 8));
+    OC_TRY(alloc(op, (void **)&op->ts_q0, nq * 8));
+  }
   if (mixed && !op->ts_unzf) {
     OC_TRY(alloc(op, (void **)&op->ts_unzf, nz * 4));
     OC_TRY(alloc(op, (void **)&op->ts_unqf, nq * 4));
@@ -851,7 +857,10 @@ static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, doub
     a.dyn = op->d_dyn + st;
     a.stage = st; a.n_stages = sc.s; a.ark = sc.ark; a.last = last; a.write_kq_last = 0;
     if (st == 0) {
-      a.rz = z; a.rq = q; a.r_is_float = 0;
+      // a one-stage scheme overwrites u^n in place: its stage input is a copy
+      // (neighbour traces must not see outputs of other blocks)
+      a.rz = sc.s == 1 ? op->ts_z0 : z; a.rq = sc.s == 1 ? op->ts_q0 : q;
+      a.r_is_float = 0;
     } else {
       a.rz = op->ts_rz[(st - 1) & 1]; a.rq = op->ts_rq[(st - 1) & 1];
       a.r_is_float = mixed ? 1 : 0;
@@ -882,6 +891,11 @@ static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, doub
 static oc_status enqueue_step(oc_op *op, const Scheme &sc, double *z, double *q,
                               double *oz = nullptr, double *oq = nullptr) {
   const bool mixed = op->prm.precision == OC_PREC_MIXED;
+  if (sc.s == 1) {
+    const size_t nz = op->n_dofs;
+    OC_TRY(cudaMemcpyAsync(op->ts_z0, z, nz * 8, cudaMemcpyDeviceToDevice, op->stream));
+    OC_TRY(cudaMemcpyAsync(op->ts_q0, q, 2 * nz * 8, cudaMemcpyDeviceToDevice, op->stream));
+  }
   for (int st = 0; st < sc.s; ++st) {
     StageArgs a;
     step_stage_args(op, sc, st, z, q, a, oz, oq);
@@ -932,6 +946,10 @@ static oc_status autotune(oc_op *op, const Scheme &sc, const double *z, const do
   oc_status st = OC_OK;
   cudaError_t ce = cudaMemcpyAsync(tz, z, nz * 8, cudaMemcpyDeviceToDevice, op->stream);
   if (ce == cudaSuccess) ce = cudaMemcpyAsync(tq, q, nq * 8, cudaMemcpyDeviceToDevice, op->stream);
+  if (ce == cudaSuccess && sc.s == 1)  // stage input of one-stage schemes
+    ce = cudaMemcpyAsync(op->ts_z0, z, nz * 8, cudaMemcpyDeviceToDevice, op->stream);
+  if (ce == cudaSuccess && sc.s == 1)
+    ce = cudaMemcpyAsync(op->ts_q0, q, nq * 8, cudaMemcpyDeviceToDevice, op->stream);
   if (ce != cudaSuccess) st = fail(op, OC_ERR_CUDA, cudaGetErrorString(ce));
   const int64_t launches = op->launches;
   const int reps = 5;
@@ -1333,5 +1351,8 @@ bool noalloc_aux_args(const oc_op *op, AuxArgs *a, cudaStream_t *stream) {
   *a = aux_args(const_cast<oc_op *>(op));
   *stream = op->stream;
   return true;
+}
+void noalloc_set_error(oc_op *op, const std::string &msg) {
+  if (op) op->err = msg;
 }
 }  // namespace oc

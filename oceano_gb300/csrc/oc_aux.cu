@@ -48,6 +48,7 @@ __global__ void transport_speed_kernel(const AuxArgs a, const double *z, const d
                                        unsigned long long *out) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   double local = 0;
+  bool nonfinite = false;
   if (c < a.n_cells) {
     const int p = a.deg[c], N = p + 1, G = p + 2, n = N * N;
     const DegTables<double> &tb = tab<double>(p);
@@ -84,9 +85,12 @@ __global__ void transport_speed_kernel(const AuxArgs a, const double *z, const d
       }
       const double j0 = J[6] * e0 + J[7] * e1, j1 = J[8] * e0 + J[9] * e1;
       const double mev = sqrt((j0 * j0 + j1 * j1) / (e0 * e0 + e1 * e1));
-      local = mx<double>(local, mev * sos + conv);
+      const double sp = mev * sos + conv;
+      // std::max keeps the running maximum when sp is NaN: check every point
+      if (!isfinite(sp)) nonfinite = true;
+      local = mx<double>(local, sp);
     }
-    if (!isfinite(local)) {
+    if (nonfinite || !isfinite(local)) {
       atomicOr(a.err, ERR_NONFINITE);
       local = 0;
     }

@@ -649,6 +649,12 @@ __device__ __forceinline__ void load_coefs(const float *ff, const double *fd,
   }
 }
 
+// One flag word per warp: OC_ERR_NONFINITE when any lane stored a non-finite
+// u^{n+1} (read by the host at its next synchronising call).
+__device__ __forceinline__ void report_nonfinite(const StageArgs &a, bool bad) {
+  if (__any_sync(OC_FULL, bad) && (threadIdx.x & 31) == 0) atomicOr(a.err, ERR_NONFINITE);
+}
+
 // ---------------------------------------------------------------------------
 // The fused stage kernel.
 //   MIX = false: FP64 plain form (R = KT = double).
@@ -1713,6 +1719,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   // Mixed time step (fast): delta = sum_j f_j k_j in FP32; internal stages store
   // u^n_f32 + delta (FP32), the last stage accumulates u^n + delta in FP64.
   KT *kz_out = static_cast<KT *>(a.kz[s + 1]);
+  bool nonfinite = false;  // a non-finite value in u^{n+1} (last stage)
   if constexpr (fast) {
     // FP32 stage input u^n_f32 + delta; FP64 result only at the last stage (its
     // own loop, so that no FP64 work is issued at the internal stages)
@@ -1732,7 +1739,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         const int e = lane + 32 * i;
         if (e < nvalid * NN) {
           const int j = e / NN, d = e - j * NN;
-          a.out_z[w_off[j] + d] = unz[i] + (double)Rreg(j)[8 * NN + d];
+          const double v = unz[i] + (double)Rreg(j)[8 * NN + d];
+          a.out_z[w_off[j] + d] = v;
+          nonfinite |= !isfinite(v);
         }
       }
     }
@@ -1744,6 +1753,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         const double *DZj = Dreg(j);
         if (a.out_z) a.out_z[gz] = DZj[d];
         if (a.out_rz) a.out_rz[gz] = (float)(DZj[d] - zref);
+        nonfinite |= a.last && !isfinite(DZj[d]);
       }
     }
   } else {
@@ -1761,6 +1771,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         zn = a.un_z[gz] + (double)Rj[8 * NN + d];
       }
       if (a.out_z) a.out_z[gz] = zn;
+      nonfinite |= a.last && !isfinite(zn);
       if (MIX && a.out_rz) a.out_rz[gz] = (float)(zn - zref);
     }
   }
@@ -1786,10 +1797,13 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         const int e = lane + 32 * i;
         if (e < nvalid * 2 * NN) {
           const int j = e / (2 * NN), d = e - j * 2 * NN;
-          a.out_q[2 * (int64_t)w_off[j] + d] = unq[i] + (double)Rreg(j)[4 * NN + d];
+          const double v = unq[i] + (double)Rreg(j)[4 * NN + d];
+          a.out_q[2 * (int64_t)w_off[j] + d] = v;
+          nonfinite |= !isfinite(v);
         }
       }
     }
+    report_nonfinite(a, nonfinite);
     return;
   }
 #pragma unroll 2
@@ -1815,8 +1829,10 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       nxt = a.un_q[gq] + (double)v;
     }
     if (a.out_q) a.out_q[gq] = nxt;
+    nonfinite |= a.last && !isfinite(nxt);
     if (MIX && a.out_rq) a.out_rq[gq] = (float)(nxt - (d < NN ? qref0 : qref1));
   }
+  report_nonfinite(a, nonfinite);
 }
 
 // Launch of a stage kernel with programmatic stream serialization: its blocks may

@@ -1,18 +1,18 @@
 // Transport-speed maximum for callers that cannot allocate device memory.
 //
-// Some callers cannot call cudaMalloc at the point where they need dt: code
-// running while a CUDA stream is being captured into a graph, hosts whose
-// device memory is owned by a pool or arena they must not bypass, and
-// real-time loops that forbid allocation after start-up.  For them this file
-// provides oc_transport_speed_noalloc, which computes the same value as
-// oc_transport_speed with no allocation at all: its scratch is a fixed
-// file-scope device array that exists from library load until process exit
-// on every GPU that loads the library.
+// Some callers of this library may not call cudaMalloc at the point where
+// they need dt: hosts whose device memory is owned by a pool or arena they
+// must not bypass, real-time loops that forbid allocation after start-up, and
+// embedding frameworks that account for every device byte themselves.  For
+// them this file provides oc_transport_speed_noalloc, which computes the same
+// value as oc_transport_speed with no allocation at all: its scratch is a
+// fixed file-scope device array that exists from library load until process
+// exit on every GPU that loads the library.
 //
 // Limits and sharing:
 //  * the scratch holds one partial maximum per 128-cell block, so a mesh may
 //    have at most OC_NOALLOC_MAX_CELLS = 4096 * 128 = 524,288 cells; larger
-//    meshes are rejected with OC_ERR_UNSUPPORTED;
+//    meshes are rejected with OC_ERR_UNSUPPORTED before anything is launched;
 //  * every call, from any handle, uses the same array; two calls whose kernels
 //    overlap on the GPU (different streams, or different host threads) race on
 //    it.  Calls on one stream are ordered and safe;
@@ -21,10 +21,18 @@
 //    read.
 // Set-up: the first call on a device (made with that device current) resolves
 // the scratch address with cudaGetSymbolAddress and uploads this file's shape
-// tables; make that first call before starting any stream capture.
+// tables, once per device and process, under a lock (host threads may make
+// first calls concurrently); make that first call before starting any stream
+// capture.  A device reset (cudaDeviceReset) after the first call is not
+// supported: it discards the uploaded tables, which are not uploaded again.
+// Errors: failures set the handle's message (oc_last_error); a CUDA error left
+// pending by earlier work of the calling thread is reported and not cleared.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstring>
+#include <mutex>
+#include <string>
 
 #include "oc_kernels.cuh"
 #include "oc_tables.hpp"
@@ -38,14 +46,19 @@ constexpr int kNoallocMaxBlocks = 4096;
 // block partial maxima (bit patterns of non-negative doubles, or NaN)
 static __device__ __align__(256) double g_speed_partials[kNoallocMaxBlocks];
 
+constexpr int kNoallocMaxDevices = 64;
 struct NoallocDevice {
-  bool ready = false;
-  double *partials = nullptr;  // device address of g_speed_partials
+  std::atomic<bool> ready{false};
+  double *partials = nullptr;  // device address of g_speed_partials (written before ready)
 };
-static NoallocDevice g_noalloc_dev[64];
+static NoallocDevice g_noalloc_dev[kNoallocMaxDevices];
+static std::mutex g_noalloc_setup;  // serialises the per-device set-up
+
+static __device__ __forceinline__ double quiet_nan() { return __longlong_as_double(0x7ff8000000000000ll); }
 
 // per-cell maximum of sigma_max(J^-1) sqrt(g h) + |J^-1 u|_inf over the
-// Gauss-Lobatto p+2 points (OceanDG.h:2505-2580); a non-finite value poisons
+// Gauss-Lobatto p+2 points (OceanDG.h:2505-2580); a non-finite point speed
+// (NaN or infinity, where oc_transport_speed reports OC_ERR_NONFINITE) poisons
 // the block result with NaN
 __global__ void noalloc_speed_partials(const AuxArgs a, const double *z, const double *q,
                                        double *partials) {
@@ -90,8 +103,8 @@ __global__ void noalloc_speed_partials(const AuxArgs a, const double *z, const d
         const double j0 = J[6] * e0 + J[7] * e1, j1 = J[8] * e0 + J[9] * e1;
         const double mev = sqrt((j0 * j0 + j1 * j1) / (e0 * e0 + e1 * e1));
         const double sp = mev * sos + conv;
-        local = isfinite(sp) ? mx<double>(local, sp) : sp;
-        if (!isfinite(local)) break;
+        local = isfinite(sp) ? mx<double>(local, sp) : quiet_nan();
+        if (isnan(local)) break;
       }
   }
   __shared__ double red[kNoallocBlock / 32];
@@ -130,8 +143,44 @@ __global__ void noalloc_speed_final(const double *partials, int nblocks, double 
   }
 }
 
-// Fill AuxArgs from the handle (defined with the handle in oc_api.cu).
+// Fill AuxArgs from the handle, and set its error message (defined with the
+// handle in oc_api.cu).
 bool noalloc_aux_args(const oc_op *op, AuxArgs *a, cudaStream_t *stream);
+void noalloc_set_error(oc_op *op, const std::string &msg);
+
+// Once per device (that device current): scratch address and this unit's shape
+// tables.  Returns the scratch address, or nullptr with `why` set.
+static double *noalloc_setup(int dev, std::string &why) {
+  NoallocDevice &d = g_noalloc_dev[dev];
+  if (d.ready.load(std::memory_order_acquire)) return d.partials;
+  std::lock_guard<std::mutex> lock(g_noalloc_setup);
+  if (d.ready.load(std::memory_order_relaxed)) return d.partials;
+  void *ptr = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&ptr, g_speed_partials);
+  if (e != cudaSuccess || !ptr) {
+    why = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+    return nullptr;
+  }
+  static DegTables<double> td[OC_MAXDEG];  // filled once, under the lock
+  static DegTables<float> tf[OC_MAXDEG];
+  static bool filled = false;
+  if (!filled) {
+    for (int p = 1; p <= OC_MAXDEG; ++p) {
+      fill_tables(p, 15, td[p - 1]);
+      cast_tables(td[p - 1], tf[p - 1]);
+    }
+    filled = true;
+  }
+  e = cudaMemcpyToSymbol(c_tabd, td, sizeof(td));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_tabf, tf, sizeof(tf));
+  if (e != cudaSuccess) {
+    why = std::string("shape tables: ") + cudaGetErrorString(e);
+    return nullptr;
+  }
+  d.partials = static_cast<double *>(ptr);
+  d.ready.store(true, std::memory_order_release);
+  return d.partials;
+}
 
 }  // namespace oc
 
@@ -139,32 +188,51 @@ using namespace oc;
 
 extern "C" oc_status oc_transport_speed_noalloc(oc_op *op, const double *height,
                                                const double *discharge, double *speed) {
-  if (!op || !height || !discharge || !speed) return OC_ERR_INVALID_ARG;
+  if (!op) return OC_ERR_INVALID_ARG;
+  if (!height || !discharge || !speed) {
+    noalloc_set_error(op, "oc_transport_speed_noalloc: null vector");
+    return OC_ERR_INVALID_ARG;
+  }
   AuxArgs a;
   cudaStream_t stream = nullptr;
-  if (!noalloc_aux_args(op, &a, &stream)) return OC_ERR_INVALID_ARG;
-  const int nblocks = (a.n_cells + kNoallocBlock - 1) / kNoallocBlock;
-  if (nblocks > kNoallocMaxBlocks) return OC_ERR_UNSUPPORTED;  // > 524,288 cells
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return OC_ERR_CUDA;
-  NoallocDevice &d = g_noalloc_dev[dev];
-  if (!d.ready) {  // once per device: scratch address and this unit's shape tables
-    void *ptr = nullptr;
-    if (cudaGetSymbolAddress(&ptr, g_speed_partials) != cudaSuccess || !ptr) return OC_ERR_CUDA;
-    static DegTables<double> td[OC_MAXDEG];
-    static DegTables<float> tf[OC_MAXDEG];
-    for (int p = 1; p <= OC_MAXDEG; ++p) {
-      fill_tables(p, 15, td[p - 1]);
-      cast_tables(td[p - 1], tf[p - 1]);
-    }
-    if (cudaMemcpyToSymbol(c_tabd, td, sizeof(td)) != cudaSuccess) return OC_ERR_CUDA;
-    if (cudaMemcpyToSymbol(c_tabf, tf, sizeof(tf)) != cudaSuccess) return OC_ERR_CUDA;
-    d.partials = static_cast<double *>(ptr);
-    d.ready = true;
+  if (!noalloc_aux_args(op, &a, &stream)) {
+    noalloc_set_error(op, "oc_transport_speed_noalloc: handle without a mesh");
+    return OC_ERR_INVALID_ARG;
   }
-  noalloc_speed_partials<<<nblocks, kNoallocBlock, 0, stream>>>(a, height, discharge, d.partials);
-  if (cudaGetLastError() != cudaSuccess) return OC_ERR_CUDA;
-  noalloc_speed_final<<<1, 256, 0, stream>>>(d.partials, nblocks, speed);
-  if (cudaGetLastError() != cudaSuccess) return OC_ERR_CUDA;
+  const int nblocks = (a.n_cells + kNoallocBlock - 1) / kNoallocBlock;
+  if (nblocks > kNoallocMaxBlocks) {
+    noalloc_set_error(op, "oc_transport_speed_noalloc: " + std::to_string(a.n_cells) +
+                              " cells exceed the fixed scratch (at most " +
+                              std::to_string(kNoallocMaxBlocks * kNoallocBlock) + " cells)");
+    return OC_ERR_UNSUPPORTED;
+  }
+  // a pending error of earlier work would be indistinguishable from a launch
+  // failure of this call: report it and leave it for the caller
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess) {
+    noalloc_set_error(op, std::string("oc_transport_speed_noalloc: pending CUDA error: ") +
+                              cudaGetErrorString(e));
+    return OC_ERR_CUDA;
+  }
+  int dev = 0;
+  e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kNoallocMaxDevices) {
+    noalloc_set_error(op, "oc_transport_speed_noalloc: no usable current device");
+    return OC_ERR_CUDA;
+  }
+  std::string why;
+  double *partials = noalloc_setup(dev, why);
+  if (!partials) {
+    noalloc_set_error(op, "oc_transport_speed_noalloc: set-up failed: " + why);
+    return OC_ERR_CUDA;
+  }
+  noalloc_speed_partials<<<nblocks, kNoallocBlock, 0, stream>>>(a, height, discharge, partials);
+  noalloc_speed_final<<<1, 256, 0, stream>>>(partials, nblocks, speed);
+  e = cudaPeekAtLastError();  // launch errors of this call (left for the caller too)
+  if (e != cudaSuccess) {
+    noalloc_set_error(op, std::string("oc_transport_speed_noalloc: launch: ") +
+                              cudaGetErrorString(e));
+    return OC_ERR_CUDA;
+  }
   return OC_OK;
 }

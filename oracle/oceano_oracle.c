@@ -1113,6 +1113,37 @@ static void inv_mass_cell(const oracle_t *o, int c, const double *coef, const do
   }
 }
 
+/* OceanoOperator::apply with its documented semantics (OceanDG.h:1658-1691;
+ * the reference's own body, :1692-1727, calls functions that do not exist):
+ * dst = M^-1 L_h(t, src) for zeta and q, M^-1 the exact cell inverse on Gauss
+ * p+1 (CellwiseInverseMassMatrix, as for the discharge at OceanDG.h:1532-1571)
+ * for all three variables.  Returns -1 on an unknown boundary id. */
+int oc_oracle_apply(void *h, double t, const double *sz, const double *sq, double *dz,
+                    double *dq)
+{
+  oracle_t *o = (oracle_t *)h;
+  const int64_t nd = o->n_dofs;
+  double *lz = (double *)malloc(sizeof(double) * nd);
+  double *lq = (double *)malloc(sizeof(double) * 2 * nd);
+  int r = apply_Lh(o, t, sz, sq, NULL, lz, lq, 0);
+  if (r == 0) {
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < o->n_cells; ++c) {
+      const shape_t *s = &o->sh[o->deg[c]];
+      const int N = s->N, n = N * N;
+      const double *J = o->jac + 11 * c;
+      double tz[MAXN * MAXN];
+      apply2d_sq(N, s->BMinv, 1, lz + o->off[c], tz);
+      for (int k = 0; k < n; ++k) tz[k] *= 1. / (s->wM[k % N] * s->wM[k / N] * J[10]);
+      apply2d_sq(N, s->BMinv, 0, tz, dz + o->off[c]);
+      inv_mass_cell(o, c, NULL, lq + 2 * o->off[c], dq + 2 * o->off[c]);
+    }
+  }
+  free(lz);
+  free(lq);
+  return r;
+}
+
 /* ------------------------------------------------------------------ */
 /* Stages                                                              */
 /* ------------------------------------------------------------------ */

@@ -61,6 +61,8 @@ def lib():
         L.oc_oracle_stage_ark.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, _dp, _dp,
                                           C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, pp,
                                           pp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oc_oracle_apply.restype = C.c_int
+        L.oc_oracle_apply.argtypes = [C.c_void_p, C.c_double, _dp, _dp, _dp, _dp]
         L.oc_oracle_transport_speed.restype = C.c_double
         L.oc_oracle_transport_speed.argtypes = [C.c_void_p, _dp, _dp]
         L.oc_oracle_project_vortex.argtypes = [C.c_void_p, C.c_double, _dp, _dp]
@@ -150,6 +152,14 @@ class Oracle:
                                       _ptr(next_z), _ptr(next_q))
         if r:
             raise RuntimeError("oracle: unknown boundary id")
+
+    def apply(self, t, z, q):
+        """dst = M^-1 L_h(t, src), exact Gauss p+1 cell inverse for all variables."""
+        dz, dq = np.zeros(self.n), np.zeros(2 * self.n)
+        if lib().oc_oracle_apply(self.h, t, np.ascontiguousarray(z, np.float64),
+                                 np.ascontiguousarray(q, np.float64), dz, dq):
+            raise RuntimeError("oracle: unknown boundary id")
+        return dz, dq
 
     def transport_speed(self, z, q):
         return float(lib().oc_oracle_transport_speed(self.h, z, q))

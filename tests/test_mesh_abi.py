@@ -11,7 +11,6 @@ from cases import hanging_mesh
 from oceano_gb300 import QuadForest, random_hp_mesh, uniform_mesh, vortex_mesh
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_MSH = "/root/reference/tests/shallowWaterVortex/shallowWaterVortex_20x10cells.msh"
 
 
 def face_slots(mesh):
@@ -69,44 +68,32 @@ def test_random_hp_mesh_is_seeded():
     assert set(np.unique(a.degree)) <= {1, 2, 3, 4} and a.n_hanging > 0
 
 
-def read_msh4_quads(path):
-    """Quads and their physical tags from a Gmsh 4.1 ASCII file (test helper)."""
-    lines = open(path).read().split("\n")
-    i = lines.index("$Nodes")
-    nb, nn = map(int, lines[i + 1].split()[:2])
-    coords = {}
-    k = i + 2
-    for _ in range(nb):
-        _, _, _, cnt = map(int, lines[k].split())
-        tags = [int(lines[k + 1 + j]) for j in range(cnt)]
-        for j in range(cnt):
-            coords[tags[j]] = tuple(map(float, lines[k + 1 + cnt + j].split()))
-        k += 1 + 2 * cnt
-    i = lines.index("$Elements")
-    nb = int(lines[i + 1].split()[0])
-    k = i + 2
-    quads, lines_tagged = [], []
-    for _ in range(nb):
-        dim, ent, etype, cnt = map(int, lines[k].split())
-        for j in range(cnt):
-            f = list(map(int, lines[k + 1 + j].split()))
-            if etype == 3:
-                quads.append([coords[n] for n in f[1:]])
-            elif etype == 1:
-                lines_tagged.append((ent, [coords[n] for n in f[1:]]))
-        k += 1 + cnt
-    return quads, lines_tagged
-
-
-@pytest.mark.skipif(not os.path.exists(REF_MSH), reason="reference mesh not mounted")
 def test_matches_reference_vortex_mesh():
-    """The 20x10 coarse grid equals the reference's Gmsh vortex mesh cell set."""
-    quads, _ = read_msh4_quads(REF_MSH)
-    assert len(quads) == 200
-    ref = sorted((round(min(p[0] for p in q), 9), round(min(p[1] for p in q), 9)) for q in quads)
+    """The 20x10 coarse grid equals the reference's Gmsh vortex mesh
+    (tests/shallowWaterVortex/shallowWaterVortex_20x10cells.msh, stored as the
+    fixture tests/golden/vortex_coarse_mesh.npz by make_mesh_fixture.py): the
+    same cells, and boundary faces with the same ids (walls 0, inflow 1 at
+    x = 0, outflow 2 at x = 2)."""
+    d = np.load(os.path.join(ROOT, "tests", "golden", "vortex_coarse_mesh.npz"))
+    quads = d["quads"]
+    assert quads.shape == (200, 4, 2)
+    ref = sorted((round(q[:, 0].min(), 9), round(q[:, 1].min(), 9)) for q in quads)
     m = uniform_mesh(20, 10, (0.0, 2.0, 0.0, 1.0), False, 1)
     ours = sorted((round(v[0], 9), round(v[1], 9)) for v in m.vertices)
     assert ref == ours
+
+    def key(a, b):
+        return tuple(sorted([(round(a[0], 9), round(a[1], 9)), (round(b[0], 9), round(b[1], 9))]))
+
+    ref_faces = {key(*ln): int(t) for ln, t in zip(d["lines"], d["line_physical"])}
+    corner = {0: (0, 2), 1: (1, 3), 2: (0, 1), 3: (2, 3)}  # face -> local vertices
+    our_faces = {}
+    for b in range(m.n_bnd):
+        f = m.n_inner + b
+        v = m.vertices[m.cell_m[f]].reshape(4, 2)
+        i0, i1 = corner[int(m.face_m[f])]
+        our_faces[key(v[i0], v[i1])] = int(m.bid[b])
+    assert our_faces == ref_faces
 
 
 def test_closed_form_sweeps_match_literal_iteration():

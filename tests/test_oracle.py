@@ -171,3 +171,33 @@ def test_transport_speed_uniform():
     h = 0.1
     expect = np.sqrt(9.81) / h + 1.0 / h  # sigma_max(J^-1) c + |J^-1 u|
     assert abs(orc.transport_speed(z, q) - expect) < 1e-12 * expect
+
+
+@pytest.mark.parametrize("mesh_f", [lambda: vortex_mesh(0, 2), lambda: mixed_degree(hanging_mesh(2))])
+def test_apply_is_inverse_mass_of_the_residual(mesh_f):
+    """apply(): M dst = L_h(src) with the exact cell mass matrix (Gauss p+1 on
+    affine cells): zeta against the ERK stage's L_h zeta register, discharge
+    against its M^-1 L_h q register (the same inverse)."""
+    from cases import perturbed_state
+    from oceano_gb300.basis import gauss, lagrange_matrix, lobatto
+    mesh = mesh_f()
+    orc = O.Oracle(mesh, bcs={0: ("wall",)}, vortex=VORTEX + [0, 0])
+    z, q = perturbed_state(orc, 3)
+    n = orc.n
+    kz = [np.zeros(n) for _ in range(4)]
+    kq = [np.zeros(2 * n) for _ in range(4)]
+    orc.stage_erk(0, 3, 0.01, np.array([1e-3]), z, q, kz, kq, z.copy(), q.copy(), np.zeros(n),
+                  np.zeros(2 * n))
+    dz, dq = orc.apply(0.01, z, q)
+    assert np.array_equal(dq, kq[1])
+    off = mesh.offsets()
+    for c in range(mesh.n_cells):
+        N = int(mesh.degree[c]) + 1
+        xg, wg = gauss(N)
+        B = lagrange_matrix(lobatto(N)[0], xg)
+        M1 = B.T @ np.diag(wg) @ B
+        v = mesh.vertices[c].reshape(4, 2)
+        det = abs((v[1, 0] - v[0, 0]) * (v[2, 1] - v[0, 1]) - (v[2, 0] - v[0, 0]) * (v[1, 1] - v[0, 1]))
+        Mc = det * np.kron(M1, M1)
+        r = Mc @ dz[off[c]:off[c + 1]] - kz[1][off[c]:off[c + 1]]
+        assert np.abs(r).max() <= 1e-12 * max(1.0, np.abs(kz[1][off[c]:off[c + 1]]).max())
