@@ -205,6 +205,15 @@ def profiled_traffic():
     return out
 
 
+def bf16_peak():
+    """Dense BF16 TFLOP/s (burst) of MEASURED_PEAKS.json, else the fallback."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["bf16_tflops"])
+    return 1900.0
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -485,11 +494,20 @@ def run_indicator(args):
     for _ in range(3):
         model.forward(f)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    # forward kernel alone: CUDA events on the model's stream around `reps` launches
+    import ctypes as C
+    from oceano_gb300._lib import lib as oclib
+    stream = torch.cuda.ExternalStream(int(oclib().oc_mlp_stream(model.h) or 0))
+    out = torch.empty(f.shape[0], dtype=torch.float32, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     reps = 20
+    e0.record(stream)
     for _ in range(reps):
-        model.forward(f)
-    t_fwd = (time.perf_counter() - t0) / reps
+        oclib().oc_mlp_forward(model.h, C.c_void_p(f.data_ptr()), f.shape[0],
+                               C.c_void_p(out.data_ptr()))
+    e1.record(stream)
+    e1.synchronize()
+    t_fwd = e0.elapsed_time(e1) / 1e3 / reps
     flops_fwd = 2 * (12 * 64 + 64 * 64 + 64)
     out = {
         "metric": "learned refinement indicator: BF16 MLP forward cells/s",
@@ -501,6 +519,11 @@ def run_indicator(args):
                    "train_samples": int(X.shape[0]), "eval_cells": int(f.shape[0]),
                    "epochs": INDICATOR_EPOCHS},
         "forward_tflops": f.shape[0] * flops_fwd / t_fwd / 1e12,
+        "forward_roofline": {"bound": "tensor", "achieved": f.shape[0] * flops_fwd / t_fwd / 1e12,
+                             "peak": bf16_peak(), "unit": "TFLOP/s",
+                             "frac": f.shape[0] * flops_fwd / t_fwd / 1e12 / bf16_peak(),
+                             "kernel": "mlp_forward_mma_kernel (mma.sync m16n8k16 bf16)",
+                             "flop_per_cell": flops_fwd},
         "train_samples_per_s": X.shape[0] * INDICATOR_EPOCHS / t_train,
         "loss_first_last": [losses[0], losses[-1]],
         "eval": res,

@@ -74,27 +74,115 @@ __device__ __forceinline__ float layer2_row(const SmemWeights &s, const float *h
   return bf(fmaxf(a, 0.f));
 }
 
-__global__ void __launch_bounds__(kThreads) mlp_forward_kernel(const float *w, const float *norm,
-                                                               const float *feat, int64_t n,
-                                                               float *logit) {
-  __shared__ SmemWeights s;
-  load_weights(s, w, norm);
-  __syncthreads();
-  // block-uniform tile loop; the barrier keeps the shared weight reads inside it
-  const int64_t tiles = (n + kThreads - 1) / kThreads;
-  for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    const int64_t c = tile * kThreads + threadIdx.x;
-    if (c < n) {
-      float x[NF], xh[NF], h1[NH];
+// ---------------------------------------------------------------------------
+// Forward pass on the BF16 tensor cores (mma.sync m16n8k16, FP32 accumulation).
+// One warp evaluates 16 samples per MMA row block: layer 1 is X [16 x 16] (12
+// features, zero-padded) times W1^T [16 x 64] (8 MMAs), layer 2 is
+// H1 [16 x 64] times W2^T [64 x 64] (4 k-steps x 8 n-tiles = 32 MMAs), layer 3
+// a dot product with w3 reduced over the quad of lanes that share a row.  The
+// accumulator fragment of layer 1 (rows g, g+8; columns 8j + 2t, +1 of n-tile
+// j) is exactly the A fragment of layer 2 for k-tile j/2, so the activations
+// never leave registers; the weights are held as B fragments in registers for
+// the whole kernel.  Biases enter as the accumulators' initial values.
+// (g = lane / 4, t = lane % 4, PTX ISA fragment layout of mma.m16n8k16.)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);  // .x (low half) = lo
+  return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2,
+                                         uint32_t a3, uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+constexpr int kMmaWarps = 4;
+
+__global__ void __launch_bounds__(32 * kMmaWarps) mlp_forward_mma_kernel(
+    const float *w, const float *norm, const float *feat, int64_t n, float *logit) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  // B fragments: layer 1 n-tile j: k = 2t, 2t+1 | 2t+8, 2t+9 (k >= 12: padding),
+  // column n = 8j + g; layer 2 k-tile kk, n-tile j: k = 16kk + 2t (+1 | +8, +9)
+  uint32_t B1[8][2], B2[4][8][2];
+  float bias1[8][2], bias2[8][2], w3v[8][2];
 #pragma unroll
-      for (int i = 0; i < NF; ++i) x[i] = feat[c * NF + i];
-      layer1(s, x, xh, h1);
-      float z = s.b3;
-#pragma unroll 1
-      for (int j = 0; j < NH; ++j) z = fmaf(s.w3[j], layer2_row(s, h1, j), z);
-      logit[c] = z;
+  for (int j = 0; j < 8; ++j) {
+    const float *r1 = w + OW1 + (8 * j + g) * NF;
+    B1[j][0] = pack_bf16(r1[2 * t], r1[2 * t + 1]);
+    B1[j][1] = t < 2 ? pack_bf16(r1[2 * t + 8], r1[2 * t + 9]) : 0u;
+    const float *r2 = w + OW2 + (8 * j + g) * NH;
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+      B2[kk][j][0] = pack_bf16(r2[16 * kk + 2 * t], r2[16 * kk + 2 * t + 1]);
+      B2[kk][j][1] = pack_bf16(r2[16 * kk + 2 * t + 8], r2[16 * kk + 2 * t + 9]);
     }
-    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int col = 8 * j + 2 * t + e;
+      bias1[j][e] = w[OB1 + col];
+      bias2[j][e] = w[OB2 + col];
+      w3v[j][e] = bf(w[OW3 + col]);
+    }
+  }
+  const float b3 = w[OB3];
+  // normalisation of the four feature columns this lane holds
+  const int fc[4] = {2 * t, 2 * t + 1, 2 * t + 8, 2 * t + 9};
+  float mu[4], is[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    mu[e] = fc[e] < NF ? norm[fc[e]] : 0.f;
+    is[e] = fc[e] < NF ? norm[NF + fc[e]] : 0.f;
+  }
+  const int64_t tiles = (n + 15) / 16;
+  const int64_t warp0 = (int64_t)blockIdx.x * kMmaWarps + (threadIdx.x >> 5);
+  const int64_t nwarps = (int64_t)gridDim.x * kMmaWarps;
+  for (int64_t tile = warp0; tile < tiles; tile += nwarps) {
+    const int64_t r0 = 16 * tile + g, r1 = r0 + 8;
+    float x0[4], x1[4];  // rows r0, r1 at columns fc[]
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const bool col = fc[e] < NF;
+      x0[e] = (col && r0 < n) ? bf((feat[r0 * NF + fc[e]] - mu[e]) * is[e]) : 0.f;
+      x1[e] = (col && r1 < n) ? bf((feat[r1 * NF + fc[e]] - mu[e]) * is[e]) : 0.f;
+    }
+    const uint32_t a0 = pack_bf16(x0[0], x0[1]), a1 = pack_bf16(x1[0], x1[1]);
+    const uint32_t a2 = pack_bf16(x0[2], x0[3]), a3 = pack_bf16(x1[2], x1[3]);
+    // layer 1 -> A fragments of layer 2
+    uint32_t H[4][4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float c[4] = {bias1[j][0], bias1[j][1], bias1[j][0], bias1[j][1]};
+      mma_bf16(c, a0, a1, a2, a3, B1[j][0], B1[j][1]);
+      const uint32_t lo = pack_bf16(fmaxf(c[0], 0.f), fmaxf(c[1], 0.f));  // row g
+      const uint32_t hi = pack_bf16(fmaxf(c[2], 0.f), fmaxf(c[3], 0.f));  // row g + 8
+      H[j >> 1][(j & 1) * 2 + 0] = lo;
+      H[j >> 1][(j & 1) * 2 + 1] = hi;
+    }
+    // layer 2 and the layer-3 dot products of rows g and g + 8
+    float z0 = 0.f, z1 = 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float c[4] = {bias2[j][0], bias2[j][1], bias2[j][0], bias2[j][1]};
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk)
+        mma_bf16(c, H[kk][0], H[kk][1], H[kk][2], H[kk][3], B2[kk][j][0], B2[kk][j][1]);
+      z0 = fmaf(w3v[j][0], bf(fmaxf(c[0], 0.f)), z0);
+      z0 = fmaf(w3v[j][1], bf(fmaxf(c[1], 0.f)), z0);
+      z1 = fmaf(w3v[j][0], bf(fmaxf(c[2], 0.f)), z1);
+      z1 = fmaf(w3v[j][1], bf(fmaxf(c[3], 0.f)), z1);
+    }
+    z0 += __shfl_xor_sync(0xffffffffu, z0, 1);
+    z0 += __shfl_xor_sync(0xffffffffu, z0, 2);
+    z1 += __shfl_xor_sync(0xffffffffu, z1, 1);
+    z1 += __shfl_xor_sync(0xffffffffu, z1, 2);
+    if (t == 0) {
+      if (r0 < n) logit[r0] = b3 + z0;
+      if (r1 < n) logit[r1] = b3 + z1;
+    }
   }
 }
 
@@ -394,8 +482,13 @@ oc_status oc_mlp_fit_normalization(oc_mlp *m, const float *features, int64_t n) 
 oc_status oc_mlp_forward(oc_mlp *m, const float *features, int64_t n, float *logits) {
   if (!m || !features || !logits || n < 0) return OC_ERR_INVALID_ARG;
   if (n == 0) return OC_OK;
-  const int grid = (int)std::min<int64_t>(152 * 8, (n + kThreads - 1) / kThreads);
-  mlp_forward_kernel<<<grid, kThreads, 0, m->stream>>>(m->d_w, m->d_norm, features, n, logits);
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t tiles = (n + 15) / 16;
+  const int grid = (int)std::min<int64_t>((int64_t)sms * 8, (tiles + kMmaWarps - 1) / kMmaWarps);
+  mlp_forward_mma_kernel<<<grid, 32 * kMmaWarps, 0, m->stream>>>(m->d_w, m->d_norm, features, n,
+                                                                  logits);
   MLP_TRY(cudaGetLastError());
   return OC_OK;
 }

@@ -12,6 +12,8 @@ product path.
   multiply-adds in the GPU's order (an FP32 product is exact in FP64, so
   fp32(fp64(a*b) + c) is the fused result except for double-rounding ties).
   exact=True: the same network in FP64 without roundings (for finite differences).
+* forward_tensor_core(): the roundings of the tensor-core forward kernel, with
+  the samples whose result depends on the hardware's summation order marked.
 * loss_and_grad(): weighted BCE-with-logits loss and its analytic gradient,
   treating the roundings as identities, accumulated in FP64.
 """
@@ -73,6 +75,45 @@ def forward(params, norm, X, exact=False):
         h2[:, j] = bf16(np.maximum(a, f32(0)))
         z = fma32(w3b[j], h2[:, j], z)
     return z, (xh, h1, h2)
+
+
+def _bf16_boundary_distance(v):
+    """Distance of FP64 values to the nearest BF16 rounding boundary (the
+    midpoint between two adjacent BF16 numbers), for v > 0."""
+    v = np.asarray(v, f64)
+    b = bf16(v.astype(f32)).astype(f64)
+    e = np.floor(np.log2(np.maximum(np.abs(v), 1e-300)))
+    ulp = np.exp2(e - 7)
+    return 0.5 * ulp - np.abs(v - b)
+
+
+def forward_tensor_core(params, norm, X, margin=1e-6):
+    """The forward pass of the tensor-core kernel: BF16 weights, inputs and
+    activations as forward(), each layer's sum of exact BF16 products formed
+    at FP32 precision or better (here exactly, in FP64) before the BF16
+    rounding.  Returns (logits, flip_prone): flip_prone marks the samples with
+    a hidden activation whose exact value lies within `margin` x (sum of
+    |terms|) of a BF16 rounding boundary, where a different summation order of
+    the hardware may round the activation to the neighbouring BF16 value."""
+    W1, b1, W2, b2, w3, b3 = unpack(params)
+    mean, istd = np.asarray(norm[:NF]), np.asarray(norm[NF:])
+    W1b, W2b, w3b = (bf16(a).astype(f64) for a in (W1, W2, w3))
+    X = np.asarray(X, f32)
+    xh = bf16((X - mean.astype(f32)).astype(f32) * istd.astype(f32)).astype(f64)
+    prone = np.zeros(X.shape[0], bool)
+
+    def layer(a_in, W, b):
+        a = a_in @ W.T + np.asarray(b, f64)
+        mag = np.abs(a_in) @ np.abs(W).T + np.abs(np.asarray(b, f64))
+        pos = a > 0
+        near = pos & (_bf16_boundary_distance(np.where(pos, a, 1.0)) < margin * mag)
+        near |= np.abs(a) < margin * mag  # sign of a cancellation
+        return bf16(np.maximum(a, 0.0).astype(f32)).astype(f64), near.any(axis=1)
+
+    h1, p1 = layer(xh, W1b, b1)
+    h2, p2 = layer(h1, W2b, b2)
+    z = h2 @ w3b + f64(b3)
+    return z, p1 | p2
 
 
 def loss_and_grad(params, norm, X, y, pos_weight, exact=False):

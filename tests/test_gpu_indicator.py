@@ -68,13 +68,23 @@ def test_features_match_oracle(gpu_lib):
     assert np.array_equal(fl[sure], flo[sure])
 
 
-def test_mlp_forward_matches_oracle(gpu_lib):
+@pytest.mark.parametrize("n", [3000, 70001])
+def test_mlp_forward_matches_oracle(gpu_lib, n):
+    """Tensor-core forward (BF16 MMA, FP32 accumulation) against the oracle's
+    emulation: 1e-5 wherever no hidden activation lies within the hardware's
+    summation-order uncertainty of a BF16 rounding boundary.  Where one does,
+    the activation may round to the neighbouring BF16 value (one BF16 step,
+    2^-8 relative): fewer than 1% of the samples differ by more than 1e-5,
+    none by more than 1e-3 of the logit scale."""
     import torch
-    p, norm, X, _ = random_net(1, 3000)
+    p, norm, X, _ = random_net(1, n)
     m = model_with(p, norm)
-    z = m.forward(torch.from_numpy(X).cuda()).cpu().numpy()
-    zo, _ = IO.forward(p, norm, X)
-    assert np.abs(z - zo).max() <= 1e-5 * (1 + np.abs(zo).max())
+    z = m.forward(torch.from_numpy(X).cuda()).cpu().numpy().astype(np.float64)
+    zo, prone = IO.forward_tensor_core(p, norm, X)
+    scale = 1 + np.abs(zo).max()
+    d = np.abs(z - zo)
+    assert d[~prone].max() <= 1e-5 * scale
+    assert (d > 1e-5 * scale).mean() < 0.01 and d.max() <= 1e-3 * scale
 
 
 @pytest.mark.parametrize("n", [100, 1000, 70000])
