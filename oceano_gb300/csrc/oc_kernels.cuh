@@ -240,6 +240,72 @@ __device__ __forceinline__ void face_flux_dev(const RefState<R> &rf, R g, R cu4,
   Pp0 = sp * n0; Pp1 = sp * n1;
 }
 
+// face_flux_dev with bathymetry (zb- != zb+): the well-balanced differences of
+// the hydrostatic reconstruction (LaxFriedrichsModified.h:161-192) and of the
+// pressure jump (NumericalFluxBase.h:103-126) in FP64 -- the depths at the own
+// and the reconstructed bathymetry zb* = min(zb-, zb+), the ratios h*/h and
+// (zb* - zb)/h of the reconstructed discharge, max(zeta, -zb*) of both sides
+// and the pressure term g/4 (h+ + h-) (c+ - c-) -- from FP64 bathymetry
+// (absolute zb) and the FP32 free-surface deviations zm, zp (zeta - zeta_ref);
+// velocities, wave speeds and fluxes stay FP32.
+template <typename R>
+__device__ __forceinline__ void face_flux_dev_wb(const RefState<R> &rf, R g, double g64, R cu4,
+                                                 double zref, R zm, R dqm0, R dqm1, R zp, R dqp0,
+                                                 R dqp1, R n0, R n1, double zbm, double zbp,
+                                                 R &F, R &Fa0, R &Fa1, R &Pm0, R &Pm1, R &Pp0,
+                                                 R &Pp1) {
+  const double hr = (double)rf.hr;
+  const double zma = (double)zm + zref, zpa = (double)zp + zref;  // absolute free surface
+  // own-bathymetry depths (velocities and wave speeds)
+  R dvm0, dvm1, hmo, rhm, dvp0, dvp1, hpo, rhp;
+  vel_dev<R>(rf, cu4, (R)(zma + zbm - hr), dqm0, dqm1, dvm0, dvm1, hmo, rhm);
+  vel_dev<R>(rf, cu4, (R)(zpa + zbp - hr), dqp0, dqp1, dvp0, dvp1, hpo, rhp);
+  const R vm0 = rf.ur0 + dvm0, vm1 = rf.ur1 + dvm1, vp0 = rf.ur0 + dvp0, vp1 = rf.ur1 + dvp1;
+  const R lm = m_abs(vm0 * n0 + vm1 * n1) + m_sqrt(g * hmo);
+  const R lp = m_abs(vp0 * n0 + vp1 * n1) + m_sqrt(g * hpo);
+  const R lambda = mx<R>(lp, lm);
+  const R urn = rf.ur0 * n0 + rf.ur1 * n1;
+  const double zbs = fmin(zbm, zbp);
+  const double hm64 = fmax(zma + zbs, 1e-12), hp64 = fmax(zpa + zbs, 1e-12);
+  const double hmo64 = fmax(zma + zbm, 1e-12), hpo64 = fmax(zpa + zbp, 1e-12);
+  // reconstructed discharge deviations hu - q_r, hu = h* u
+  R dhum0, dhum1, dhup0, dhup1;
+  const R cu = R(1e-12);
+  if (rhm > R(0) && hm64 > 1e-12) {  // wet: u = q / h_own, hu = (h*/h_own) q
+    const R r = (R)(hm64 / hmo64), c = (R)((zbs - zbm) / hmo64);
+    dhum0 = r * dqm0 + rf.qr0 * c;
+    dhum1 = r * dqm1 + rf.qr1 * c;
+  } else {
+    dhum0 = (R)hm64 * vm0 - rf.qr0;
+    dhum1 = (R)hm64 * vm1 - rf.qr1;
+  }
+  if (rhp > R(0) && hp64 > 1e-12) {
+    const R r = (R)(hp64 / hpo64), c = (R)((zbs - zbp) / hpo64);
+    dhup0 = r * dqp0 + rf.qr0 * c;
+    dhup1 = r * dqp1 + rf.qr1 * c;
+  } else {
+    dhup0 = (R)hp64 * vp0 - rf.qr0;
+    dhup1 = (R)hp64 * vp1 - rf.qr1;
+  }
+  (void)cu;
+  const double cm = fmax(zma, -zbs), cp = fmax(zpa, -zbs);
+  const R dc = (R)(cm - cp);
+  F = R(0.5) * ((dhum0 * n0 + dhum1 * n1) + (dhup0 * n0 + dhup1 * n1)) + R(0.5) * lambda * dc;
+  // advective flux: velocity recomputed from hu at the reconstructed depth
+  R dwm0, dwm1, dwp0, dwp1, hh;
+  vel_dev<R>(rf, cu4, (R)(hm64 - hr), dhum0, dhum1, dwm0, dwm1, hh);
+  vel_dev<R>(rf, cu4, (R)(hp64 - hr), dhup0, dhup1, dwp0, dwp1, hh);
+  const R dunm = dwm0 * n0 + dwm1 * n1, dunp = dwp0 * n0 + dwp1 * n1;
+  const R Xm0 = rf.qr0 * dunm + dhum0 * (urn + dunm), Xm1 = rf.qr1 * dunm + dhum1 * (urn + dunm);
+  const R Xp0 = rf.qr0 * dunp + dhup0 * (urn + dunp), Xp1 = rf.qr1 * dunp + dhup1 * (urn + dunp);
+  Fa0 = R(0.5) * (Xm0 + Xp0) + R(0.5) * lambda * (dhum0 - dhup0);
+  Fa1 = R(0.5) * (Xm1 + Xp1) + R(0.5) * lambda * (dhum1 - dhup1);
+  const double sg = 0.25 * g64 * (hp64 + hm64) * (cp - cm);  // minus-side call; plus: -sg
+  const R sm = (R)sg;
+  Pm0 = sm * n0; Pm1 = sm * n1;
+  Pp0 = -sm * n0; Pp1 = -sm * n1;
+}
+
 // Icbc_ShallowWaterVortex.h:139-226 (regularity p=2), FP64
 __host__ __device__ inline double vortex_H(double x) {
   const double cosx = cos(x), cos2x = cos(2. * x), sin2x = sin(2. * x), sinx = sin(x);
@@ -904,8 +970,18 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         const R dz0 = Ji00 * zx + Ji10 * zy, dz1 = Ji01 * zx + Ji11 * zy;
         R fr0 = 0, fr1 = 0;
         if (a.friction && !split) friction<R>(a.friction, g, v0, v1, cf, h, fr0, fr1);
-        const R s0 = -g * h * dz0 - fr0 + w0 + fc * qa1;
-        const R s1 = -g * h * dz1 - fr1 + w1 - fc * qa0;
+        // -g h grad(zeta) (ShallowWater.h:405-432); with bathymetry the mixed form
+        // forms h = zeta + zb and the product in FP64 (well-balanced source)
+        R pg0 = -g * h * dz0, pg1 = -g * h * dz1;
+        if constexpr (MIX) {
+          if (sd0) {
+            const double h64 = fmax((double)z + zref + sd0[5 * k], 1e-12);
+            pg0 = (R)(-a.g * h64 * (double)dz0);
+            pg1 = (R)(-a.g * h64 * (double)dz1);
+          }
+        }
+        const R s0 = pg0 - fr0 + w0 + fc * qa1;
+        const R s1 = pg1 - fr1 + w1 - fc * qa0;
         const R g00 = (Ji00 * F00 + Ji01 * F01) * w, g01 = (Ji10 * F00 + Ji11 * F01) * w;
         const R g10 = (Ji00 * F10 + Ji01 * F11) * w, g11 = (Ji10 * F10 + Ji11 * F11) * w;
         const R sv0 = s0 * w, sv1 = s1 * w;
@@ -1149,16 +1225,19 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
             const R zm = side ? zn : zo_, qm0 = side ? qn0 : qo0, qm1 = side ? qn1 : qo1;
             const R zp = side ? zo_ : zn, qp0 = side ? qo0 : qn0, qp1 = side ? qo1 : qn1;
             R zbm = MIX ? zbe_flat : R(0), zbp = zbm;
-            if (MIX && a.sdfe) {
-              zbm = (R)a.sdfe[sdo + 2 * k]; zbp = (R)a.sdfe[sdo + 2 * k + 1];
-            } else if (!MIX && a.sdf) {
+            if (!MIX && a.sdf) {
               zbm = (R)a.sdf[sdo + 2 * k]; zbp = (R)a.sdf[sdo + 2 * k + 1];
             }
             R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
-            if constexpr (MIX)
-              face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0,
-                               Fa1, Pm0, Pm1, Pp0, Pp1, a.sdfe == nullptr);
-            else
+            if constexpr (MIX) {
+              if (a.sdf)  // bathymetry: well-balanced differences in FP64
+                face_flux_dev_wb<R>(rf, g, a.g, cu4, zref, zm, qm0, qm1, zp, qp0, qp1, n0, n1,
+                                    a.sdf[sdo + 2 * k], a.sdf[sdo + 2 * k + 1], F, Fa0, Fa1, Pm0,
+                                    Pm1, Pp0, Pp1);
+              else
+                face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F,
+                                 Fa0, Fa1, Pm0, Pm1, Pp0, Pp1, true);
+            } else
               face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1,
                            Pm0, Pm1, Pp0, Pp1);
             const R jxw = fw * len;
@@ -1193,16 +1272,19 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           const R zm = side ? zn : zo_, qm0 = side ? qn0 : qo0, qm1 = side ? qn1 : qo1;
           const R zp = side ? zo_ : zn, qp0 = side ? qo0 : qn0, qp1 = side ? qo1 : qn1;
           R zbm = MIX ? zbe_flat : R(0), zbp = zbm;
-          if (MIX && a.sdfe) {
-            zbm = (R)a.sdfe[sdo + 2 * k]; zbp = (R)a.sdfe[sdo + 2 * k + 1];
-          } else if (!MIX && a.sdf) {
+          if (!MIX && a.sdf) {
             zbm = (R)a.sdf[sdo + 2 * k]; zbp = (R)a.sdf[sdo + 2 * k + 1];
           }
           R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
-          if constexpr (MIX)
-            face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1,
-                             Pm0, Pm1, Pp0, Pp1, a.sdfe == nullptr);
-          else
+          if constexpr (MIX) {
+            if (a.sdf)  // bathymetry: well-balanced differences in FP64
+              face_flux_dev_wb<R>(rf, g, a.g, cu4, zref, zm, qm0, qm1, zp, qp0, qp1, n0, n1,
+                                  a.sdf[sdo + 2 * k], a.sdf[sdo + 2 * k + 1], F, Fa0, Fa1, Pm0,
+                                  Pm1, Pp0, Pp1);
+            else
+              face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0,
+                               Fa1, Pm0, Pm1, Pp0, Pp1, true);
+          } else
             face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1, Pm0,
                          Pm1, Pp0, Pp1);
           const R jxw = __ldg(&tbg.wF[nf][k]) * len;
