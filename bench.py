@@ -489,7 +489,7 @@ def run_indicator(args):
     t_train = time.perf_counter() - t0
     ev_op, z2, q2, info2, dt2, members = setup(64, 1000)
     recs2 = run_and_record(ev_op, z2, q2, info2, 64, dt2, 60, every=1)
-    res = evaluate(model, recs2, horizon, members, 64)
+    res = evaluate(model, recs2, horizon, members, 64, info=info2.cpu().numpy())
     f = recs2[0][0]
     for _ in range(3):
         model.forward(f)
@@ -509,6 +509,16 @@ def run_indicator(args):
     e1.synchronize()
     t_fwd = e0.elapsed_time(e1) / 1e3 / reps
     flops_fwd = 2 * (12 * 64 + 64 * 64 + 64)
+    # remeshing runs: 16 independent members (own mesh, operator and time step),
+    # p-adaptive degree map (1 outside / 2 inside the refined set) with state
+    # transfer, 40 steps, under the three policies
+    from oceano_gb300.adapt import remesh_experiment
+    rm_members = W.ensemble_members(16, 1000)
+    remesh = {"members": 16, "steps": 40, "degrees": "1 outside, 2 inside the refined set"}
+    for name, kw in (("vorticity", {}), ("dilated_1", {"layers": 1}),
+                     ("learned", {"model": model})):
+        policy = name.split("_")[0]
+        remesh[name] = remesh_experiment(rm_members, policy, 40, **kw)
     out = {
         "metric": "learned refinement indicator: BF16 MLP forward cells/s",
         "value": f.shape[0] / t_fwd, "unit": "cells/s", "n_gpus": 1, "steps": args.steps,
@@ -527,6 +537,7 @@ def run_indicator(args):
         "train_samples_per_s": X.shape[0] * INDICATOR_EPOCHS / t_train,
         "loss_first_last": [losses[0], losses[-1]],
         "eval": res,
+        "remesh_runs": remesh,
     }
     print(json.dumps(out))
 

@@ -242,66 +242,66 @@ __device__ __forceinline__ void face_flux_dev(const RefState<R> &rf, R g, R cu4,
 
 // face_flux_dev with bathymetry (zb- != zb+): the well-balanced differences of
 // the hydrostatic reconstruction (LaxFriedrichsModified.h:161-192) and of the
-// pressure jump (NumericalFluxBase.h:103-126) in FP64 -- the depths at the own
-// and the reconstructed bathymetry zb* = min(zb-, zb+), the ratios h*/h and
-// (zb* - zb)/h of the reconstructed discharge, max(zeta, -zb*) of both sides
-// and the pressure term g/4 (h+ + h-) (c+ - c-) -- from FP64 bathymetry
-// (absolute zb) and the FP32 free-surface deviations zm, zp (zeta - zeta_ref);
-// velocities, wave speeds and fluxes stay FP32.
+// pressure jump (NumericalFluxBase.h:103-126) in FP64 -- zb* = min(zb-, zb+),
+// the reconstructed depths h* = zeta + zb*, the bathymetry differences
+// zb* - zb of the reconstructed discharge, max(zeta, -zb*) of both sides and
+// the depth sum of the pressure term -- from the FP64 bathymetry (absolute zb)
+// and the FP32 free-surface deviations zm, zp (zeta - zeta_ref).  Velocities,
+// wave speeds, fluxes and the remaining products stay FP32.  (GB300 runs FP64
+// at 1/64 of the FP32 rate: no FP64 division or product is needed here; on wet
+// points h*/h = 1 + (zb* - zb)/h.)  zbme, zbpe: FP32 zb + zeta_ref.
 template <typename R>
-__device__ __forceinline__ void face_flux_dev_wb(const RefState<R> &rf, R g, double g64, R cu4,
-                                                 double zref, R zm, R dqm0, R dqm1, R zp, R dqp0,
-                                                 R dqp1, R n0, R n1, double zbm, double zbp,
-                                                 R &F, R &Fa0, R &Fa1, R &Pm0, R &Pm1, R &Pp0,
-                                                 R &Pp1) {
-  const double hr = (double)rf.hr;
-  const double zma = (double)zm + zref, zpa = (double)zp + zref;  // absolute free surface
-  // own-bathymetry depths (velocities and wave speeds)
+__device__ __forceinline__ void face_flux_dev_wb(const RefState<R> &rf, R g, R cu4, double zref,
+                                                 R zm, R dqm0, R dqm1, R zp, R dqp0, R dqp1,
+                                                 R n0, R n1, double zbm, double zbp, R zbme,
+                                                 R zbpe, R &F, R &Fa0, R &Fa1, R &Pm0, R &Pm1,
+                                                 R &Pp0, R &Pp1) {
+  // own-bathymetry depths for the velocities and wave speeds (FP32)
   R dvm0, dvm1, hmo, rhm, dvp0, dvp1, hpo, rhp;
-  vel_dev<R>(rf, cu4, (R)(zma + zbm - hr), dqm0, dqm1, dvm0, dvm1, hmo, rhm);
-  vel_dev<R>(rf, cu4, (R)(zpa + zbp - hr), dqp0, dqp1, dvp0, dvp1, hpo, rhp);
+  vel_dev<R>(rf, cu4, zm + (zbme - rf.hr), dqm0, dqm1, dvm0, dvm1, hmo, rhm);
+  vel_dev<R>(rf, cu4, zp + (zbpe - rf.hr), dqp0, dqp1, dvp0, dvp1, hpo, rhp);
   const R vm0 = rf.ur0 + dvm0, vm1 = rf.ur1 + dvm1, vp0 = rf.ur0 + dvp0, vp1 = rf.ur1 + dvp1;
   const R lm = m_abs(vm0 * n0 + vm1 * n1) + m_sqrt(g * hmo);
   const R lp = m_abs(vp0 * n0 + vp1 * n1) + m_sqrt(g * hpo);
   const R lambda = mx<R>(lp, lm);
   const R urn = rf.ur0 * n0 + rf.ur1 * n1;
+  // FP64 differences
+  const double zma = (double)zm + zref, zpa = (double)zp + zref;  // absolute free surface
   const double zbs = fmin(zbm, zbp);
   const double hm64 = fmax(zma + zbs, 1e-12), hp64 = fmax(zpa + zbs, 1e-12);
-  const double hmo64 = fmax(zma + zbm, 1e-12), hpo64 = fmax(zpa + zbp, 1e-12);
+  const R dbm = (R)(zbs - zbm), dbp = (R)(zbs - zbp);
+  const R dc = (R)(fmax(zma, -zbs) - fmax(zpa, -zbs));  // c- - c+
+  const R hsum = (R)(hp64 + hm64);
+  const R hm = (R)hm64, hp = (R)hp64;
   // reconstructed discharge deviations hu - q_r, hu = h* u
   R dhum0, dhum1, dhup0, dhup1;
-  const R cu = R(1e-12);
-  if (rhm > R(0) && hm64 > 1e-12) {  // wet: u = q / h_own, hu = (h*/h_own) q
-    const R r = (R)(hm64 / hmo64), c = (R)((zbs - zbm) / hmo64);
+  if (rhm > R(0) && hm64 > 1e-12) {  // wet: hu = (1 + (zb* - zb)/h) q
+    const R c = dbm * rhm, r = R(1) + c;
     dhum0 = r * dqm0 + rf.qr0 * c;
     dhum1 = r * dqm1 + rf.qr1 * c;
   } else {
-    dhum0 = (R)hm64 * vm0 - rf.qr0;
-    dhum1 = (R)hm64 * vm1 - rf.qr1;
+    dhum0 = hm * vm0 - rf.qr0;
+    dhum1 = hm * vm1 - rf.qr1;
   }
   if (rhp > R(0) && hp64 > 1e-12) {
-    const R r = (R)(hp64 / hpo64), c = (R)((zbs - zbp) / hpo64);
+    const R c = dbp * rhp, r = R(1) + c;
     dhup0 = r * dqp0 + rf.qr0 * c;
     dhup1 = r * dqp1 + rf.qr1 * c;
   } else {
-    dhup0 = (R)hp64 * vp0 - rf.qr0;
-    dhup1 = (R)hp64 * vp1 - rf.qr1;
+    dhup0 = hp * vp0 - rf.qr0;
+    dhup1 = hp * vp1 - rf.qr1;
   }
-  (void)cu;
-  const double cm = fmax(zma, -zbs), cp = fmax(zpa, -zbs);
-  const R dc = (R)(cm - cp);
   F = R(0.5) * ((dhum0 * n0 + dhum1 * n1) + (dhup0 * n0 + dhup1 * n1)) + R(0.5) * lambda * dc;
   // advective flux: velocity recomputed from hu at the reconstructed depth
   R dwm0, dwm1, dwp0, dwp1, hh;
-  vel_dev<R>(rf, cu4, (R)(hm64 - hr), dhum0, dhum1, dwm0, dwm1, hh);
-  vel_dev<R>(rf, cu4, (R)(hp64 - hr), dhup0, dhup1, dwp0, dwp1, hh);
+  vel_dev<R>(rf, cu4, (R)(hm64 - (double)rf.hr), dhum0, dhum1, dwm0, dwm1, hh);
+  vel_dev<R>(rf, cu4, (R)(hp64 - (double)rf.hr), dhup0, dhup1, dwp0, dwp1, hh);
   const R dunm = dwm0 * n0 + dwm1 * n1, dunp = dwp0 * n0 + dwp1 * n1;
   const R Xm0 = rf.qr0 * dunm + dhum0 * (urn + dunm), Xm1 = rf.qr1 * dunm + dhum1 * (urn + dunm);
   const R Xp0 = rf.qr0 * dunp + dhup0 * (urn + dunp), Xp1 = rf.qr1 * dunp + dhup1 * (urn + dunp);
   Fa0 = R(0.5) * (Xm0 + Xp0) + R(0.5) * lambda * (dhum0 - dhup0);
   Fa1 = R(0.5) * (Xm1 + Xp1) + R(0.5) * lambda * (dhum1 - dhup1);
-  const double sg = 0.25 * g64 * (hp64 + hm64) * (cp - cm);  // minus-side call; plus: -sg
-  const R sm = (R)sg;
+  const R sm = -(g * R(0.25)) * hsum * dc;  // g/4 (h+ + h-) (c+ - c-), minus-side call
   Pm0 = sm * n0; Pm1 = sm * n1;
   Pp0 = -sm * n0; Pp1 = -sm * n1;
 }
@@ -971,15 +971,12 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         R fr0 = 0, fr1 = 0;
         if (a.friction && !split) friction<R>(a.friction, g, v0, v1, cf, h, fr0, fr1);
         // -g h grad(zeta) (ShallowWater.h:405-432); with bathymetry the mixed form
-        // forms h = zeta + zb and the product in FP64 (well-balanced source)
-        R pg0 = -g * h * dz0, pg1 = -g * h * dz1;
+        // forms the depth h = zeta + zb of the source in FP64
+        R hs = h;
         if constexpr (MIX) {
-          if (sd0) {
-            const double h64 = fmax((double)z + zref + sd0[5 * k], 1e-12);
-            pg0 = (R)(-a.g * h64 * (double)dz0);
-            pg1 = (R)(-a.g * h64 * (double)dz1);
-          }
+          if (sd0) hs = (R)fmax((double)z + (zref + sd0[5 * k]), 1e-12);
         }
+        const R pg0 = -g * hs * dz0, pg1 = -g * hs * dz1;
         const R s0 = pg0 - fr0 + w0 + fc * qa1;
         const R s1 = pg1 - fr1 + w1 - fc * qa0;
         const R g00 = (Ji00 * F00 + Ji01 * F01) * w, g01 = (Ji10 * F00 + Ji11 * F01) * w;
@@ -1231,9 +1228,10 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
             R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
             if constexpr (MIX) {
               if (a.sdf)  // bathymetry: well-balanced differences in FP64
-                face_flux_dev_wb<R>(rf, g, a.g, cu4, zref, zm, qm0, qm1, zp, qp0, qp1, n0, n1,
-                                    a.sdf[sdo + 2 * k], a.sdf[sdo + 2 * k + 1], F, Fa0, Fa1, Pm0,
-                                    Pm1, Pp0, Pp1);
+                face_flux_dev_wb<R>(rf, g, cu4, zref, zm, qm0, qm1, zp, qp0, qp1, n0, n1,
+                                    a.sdf[sdo + 2 * k], a.sdf[sdo + 2 * k + 1],
+                                    a.sdfe[sdo + 2 * k], a.sdfe[sdo + 2 * k + 1], F, Fa0, Fa1,
+                                    Pm0, Pm1, Pp0, Pp1);
               else
                 face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F,
                                  Fa0, Fa1, Pm0, Pm1, Pp0, Pp1, true);
@@ -1278,8 +1276,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
           if constexpr (MIX) {
             if (a.sdf)  // bathymetry: well-balanced differences in FP64
-              face_flux_dev_wb<R>(rf, g, a.g, cu4, zref, zm, qm0, qm1, zp, qp0, qp1, n0, n1,
-                                  a.sdf[sdo + 2 * k], a.sdf[sdo + 2 * k + 1], F, Fa0, Fa1, Pm0,
+              face_flux_dev_wb<R>(rf, g, cu4, zref, zm, qm0, qm1, zp, qp0, qp1, n0, n1,
+                                  a.sdf[sdo + 2 * k], a.sdf[sdo + 2 * k + 1],
+                                  a.sdfe[sdo + 2 * k], a.sdfe[sdo + 2 * k + 1], F, Fa0, Fa1, Pm0,
                                   Pm1, Pp0, Pp1);
             else
               face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0,

@@ -145,6 +145,23 @@ class LearnedIndicator:
         return torch.sigmoid(self.forward(feat)) > threshold
 
 
+def dilate(flags, info, layers=1) -> np.ndarray:
+    """The flagged cells grown by `layers` layers of face neighbours (cell_info
+    columns 0..3; on a coarse face with two fine neighbours the one recorded):
+    the refinement buffer of a run without a network (hpTuner.h:247-305 flags,
+    grown so that the refined set stays valid for longer)."""
+    out = np.asarray(flags, bool).copy()
+    nb = np.asarray(info)[:, :4]
+    for _ in range(layers):
+        grown = out.copy()
+        for f in range(4):
+            has = nb[:, f] >= 0
+            grown[nb[has, f]] |= out[has]
+            grown[has] |= out[nb[has, f]]
+        out = grown
+    return out
+
+
 def remesh_count(flag_seq, predicted=None, members=None, n_members=1) -> int:
     """Remeshes of a run that refines where flagged.  The refined set starts as
     the flags at t = 0; afterwards a member remeshes when one of its currently
@@ -196,11 +213,13 @@ def training_pairs(records, horizon):
     return X, Y
 
 
-def evaluate(model, records, horizon, members, n_members, threshold=0.5):
+def evaluate(model, records, horizon, members, n_members, threshold=0.5, info=None,
+             dilate_layers=(1, 2)):
     """Precision / recall of the predicted flags `horizon` records ahead, the
     remesh counts of the vorticity indicator and of the learned indicator, and
     the mean size of the learned refinement set (flags or predicted) over the
-    flagged set."""
+    flagged set; with `info` (cell_info) also the remesh counts and set sizes of
+    the network-free buffer (flags dilated by k cell layers)."""
     import torch
     tp = fp = fn = 0
     preds, flags, ratio = [], [], []
@@ -216,6 +235,13 @@ def evaluate(model, records, horizon, members, n_members, threshold=0.5):
             fn += int((~p & y).sum())
     base = remesh_count(flags, None, members, n_members)
     learned = remesh_count(flags, preds, members, n_members)
-    return {"precision": tp / max(tp + fp, 1), "recall": tp / max(tp + fn, 1),
-            "remesh_vorticity": base, "remesh_learned": learned,
-            "refined_over_flagged": float(np.mean(ratio))}
+    out = {"precision": tp / max(tp + fp, 1), "recall": tp / max(tp + fn, 1),
+           "remesh_vorticity": base, "remesh_learned": learned,
+           "refined_over_flagged": float(np.mean(ratio))}
+    if info is not None:  # the network-free buffer: flags grown by k cell layers
+        for k in dilate_layers:
+            grown = [dilate(f, info, k) for f in flags]
+            out[f"remesh_dilated_{k}"] = remesh_count(flags, grown, members, n_members)
+            out[f"dilated_{k}_over_flagged"] = float(np.mean(
+                [g.sum() / max(f.sum(), 1) for g, f in zip(grown, flags)]))
+    return out

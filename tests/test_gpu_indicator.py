@@ -74,8 +74,9 @@ def test_mlp_forward_matches_oracle(gpu_lib, n):
     emulation: 1e-5 wherever no hidden activation lies within the hardware's
     summation-order uncertainty of a BF16 rounding boundary.  Where one does,
     the activation may round to the neighbouring BF16 value (one BF16 step,
-    2^-8 relative): fewer than 1% of the samples differ by more than 1e-5,
-    none by more than 1e-3 of the logit scale."""
+    2^-8 relative) and move the logit through the next layer: fewer than 1%
+    of the samples differ by more than 1e-5, none by more than 1e-2 of the
+    logit scale."""
     import torch
     p, norm, X, _ = random_net(1, n)
     m = model_with(p, norm)
@@ -84,7 +85,7 @@ def test_mlp_forward_matches_oracle(gpu_lib, n):
     scale = 1 + np.abs(zo).max()
     d = np.abs(z - zo)
     assert d[~prone].max() <= 1e-5 * scale
-    assert (d > 1e-5 * scale).mean() < 0.01 and d.max() <= 1e-3 * scale
+    assert (d > 1e-5 * scale).mean() < 0.01 and d.max() <= 1e-2 * scale
 
 
 @pytest.mark.parametrize("n", [100, 1000, 70000])
@@ -146,3 +147,46 @@ def test_train_and_evaluate_small_ensemble(gpu_lib):
     res = evaluate(model, recs2, 10, members, 4)
     assert res["recall"] > 0.8
     assert res["remesh_learned"] <= res["remesh_vorticity"]
+
+
+def test_remesh_runs_conserve_and_count(gpu_lib):
+    """p-adaptive remeshing of independent members: a remesh (degree map change
+    with state transfer) keeps the member's mass; the network-free buffer
+    (flags grown by one cell layer) remeshes no more often than the bare
+    flags, at a free-surface error within 10% of theirs."""
+    from oceano_gb300 import workloads as W
+    from oceano_gb300.adapt import AdaptiveMember, remesh_experiment
+    from oceano_gb300.basis import lobatto
+    members = W.ensemble_members(3, 1000)
+    for m in members:
+        m["target"] = 5000.0
+    mesh = W.member_mesh(members[0])
+    mesh = mesh.with_degree(np.ones(mesh.n_cells, np.int32))
+    am = AdaptiveMember(mesh, members[0]["vortex"], np.zeros(mesh.n_cells, bool))
+
+    def mass(member):
+        v = member.mesh.vertices
+        det = np.abs((v[:, 2] - v[:, 0]) * (v[:, 5] - v[:, 1]) - (v[:, 4] - v[:, 0]) * (v[:, 3] - v[:, 1]))
+        off = member.mesh.offsets()
+        tot = 0.0
+        for c in range(member.mesh.n_cells):
+            N = int(member.mesh.degree[c]) + 1
+            w = np.outer(lobatto(N)[1], lobatto(N)[1]).ravel()
+            tot += det[c] * (w @ member.z[off[c]:off[c + 1]])
+        return tot
+
+    am.step()
+    m0 = mass(am)
+    rng = np.random.default_rng(0)
+    am.remesh(rng.random(mesh.n_cells) < 0.3)
+    assert abs(mass(am) - m0) <= 1e-13 * abs(m0)
+    am.remesh(rng.random(mesh.n_cells) < 0.3)
+    assert abs(mass(am) - m0) <= 1e-13 * abs(m0)
+    am.step()
+    am.op.close()
+    bare = remesh_experiment(members, "vorticity", 15)
+    grown = remesh_experiment(members, "dilated", 15, layers=1)
+    assert grown["remeshes"] <= bare["remeshes"]
+    assert grown["refined_over_flagged"] >= 1.0
+    e0, e1 = bare["free_surface_l2_error"], grown["free_surface_l2_error"]
+    assert np.isfinite(e0) and np.isfinite(e1) and abs(e1 - e0) <= 0.1 * e0

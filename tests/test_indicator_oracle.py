@@ -86,3 +86,48 @@ def test_tensor_core_emulation_against_fp32_order():
     d = np.abs(z32.astype(np.float64) - ztc)
     assert d[~prone].max() <= 1e-5 * scale
     assert (d > 1e-5 * scale).mean() < 0.01 and d.max() <= 1e-3 * scale
+
+
+def test_dilate_grows_by_face_layers():
+    """dilate(): one layer adds the face neighbours (not the diagonal ones), two
+    layers the cells within two face steps; boundary cells have fewer."""
+    from oceano_gb300 import uniform_mesh
+    from oceano_gb300.indicator import cell_info, dilate
+    mesh = uniform_mesh(7, 7, (0.0, 1.0, 0.0, 1.0), False, 1)
+    info = cell_info(mesh)
+    centre = np.argmin(np.abs(mesh.vertices[:, 0] - 3 / 7) + np.abs(mesh.vertices[:, 1] - 3 / 7))
+    f = np.zeros(mesh.n_cells, bool)
+    f[centre] = True
+    assert dilate(f, info, 1).sum() == 5
+    assert dilate(f, info, 2).sum() == 13
+    corner = np.argmin(mesh.vertices[:, 0] + mesh.vertices[:, 1])
+    g = np.zeros(mesh.n_cells, bool)
+    g[corner] = True
+    assert dilate(g, info, 1).sum() == 3
+
+
+def test_degree_transfer_round_trip_and_conservation():
+    """p-adaptation transfer: degree 1 -> 2 -> 1 returns the degree-1 state;
+    2 -> 1 keeps the cell integrals of zeta and q (Gauss-Lobatto quadrature of
+    the nodal values is exact for these polynomial degrees)."""
+    from oceano_gb300.adapt import transfer_state
+    from oceano_gb300.basis import lobatto
+    rng = np.random.default_rng(5)
+    nc = 40
+    d1 = np.ones(nc, np.int32)
+    d2 = np.where(rng.random(nc) < 0.5, 2, 1).astype(np.int32)
+    n1 = int(((d1 + 1) ** 2).sum())
+    z1, q1 = rng.standard_normal(n1), rng.standard_normal(2 * n1)
+    z2, q2 = transfer_state(d1, d2, z1, q1)
+    zb, qb = transfer_state(d2, d1, z2, q2)
+    assert np.allclose(zb, z1, atol=1e-13) and np.allclose(qb, q1, atol=1e-13)
+    # conservation of 2 -> 1 on an arbitrary degree-2 state
+    dd = np.full(nc, 2, np.int32)
+    n2 = 9 * nc
+    z2, q2 = rng.standard_normal(n2), rng.standard_normal(2 * n2)
+    zc, qc = transfer_state(dd, d1, z2, q2)
+    w2 = np.outer(lobatto(3)[1], lobatto(3)[1]).ravel()
+    w1 = np.outer(lobatto(2)[1], lobatto(2)[1]).ravel()
+    assert np.allclose(z2.reshape(nc, 9) @ w2, zc.reshape(nc, 4) @ w1, atol=1e-13)
+    qa, qb2 = q2.reshape(nc, 2, 9), qc.reshape(nc, 2, 4)
+    assert np.allclose(qa @ w2, qb2 @ w1, atol=1e-13)
