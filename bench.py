@@ -124,11 +124,19 @@ class Workload:
                 zs, qs = zip(*[W.vortex_nodal_state(m, mm["vortex"]) for m, mm in zip(meshes, members)])
                 z0, q0 = np.concatenate(zs), np.concatenate(qs)
             self.desc = (f"64-member vortex ensemble, {mesh.n_cells} cells "
-                         f"(5k-40k per member, p=1,2), one operator, SSP-RK3 step")
+                         f"(5k-40k per member, p=1,2), one operator, own dt per member, "
+                         f"SSP-RK3 step")
             self.oracle_kw = dict(bcs={0: ("wall",)})
         else:
             raise ValueError(name)
         self.mesh = mesh
+        self.member_dt = None
+        if name == "ensemble" and gpu:  # every member keeps its own dt (per-cell scales)
+            from oceano_gb300.indicator import member_of_cells
+            dt_ref, scale = W.member_time_steps(self.op_d, z0, q0, member_of_cells(meshes), CFL)
+            for op in (self.op_m, self.op_d):
+                op.set_cell_time_scale(scale)
+            self.member_dt = (dt_ref, float(scale.min()), float(scale.max()))
         # degree-4 cells at the finest level of the hp mesh need a smaller Courant
         # number (CFL 0.075 diverges there within 20 steps, in the oracle as well)
         self.cfl = {"vortex": CFL_VORTEX, "hp": CFL_HP}.get(name, CFL)
@@ -136,6 +144,8 @@ class Workload:
             self.n = self.op_d.n_dofs
             self.z0, self.q0 = z0, q0
             self.dt = self.cfl / self.op_d.compute_cell_transport_speed(self.z0, self.q0)
+            if self.member_dt is not None:
+                self.dt = self.member_dt[0]
         else:
             orc = self.oracle()
             if z0 is None:

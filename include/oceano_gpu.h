@@ -238,6 +238,20 @@ oc_status oc_project_vortex(oc_op *op, double time, double *height, double *disc
 oc_status oc_transport_speed_noalloc(oc_op *op, const double *height, const double *discharge,
                                      double *speed);
 
+/* Independent instances with their own step size in one launch (no reference
+ * counterpart): oc_perform_time_step(dt) advances cell c by dt * scale[c]
+ * (scale[c] > 0; the cells of one instance share it), so that the members of
+ * an ensemble keep their own dt.  Boundary data are evaluated at the unscaled
+ * time.  scale = NULL restores 1.  Explicit schemes only (the additive scheme
+ * returns OC_ERR_UNSUPPORTED while scales are set); oc_perform_stage_hydro
+ * ignores them. */
+oc_status oc_set_cell_time_scale(oc_op *op, const double *scale);
+/* compute_cell_transport_speed (OceanDG.h:2505-2580) per cell: speed[c] is the
+ * maximum over the cell's Gauss-Lobatto (p+2)^2 points (the reference's value is
+ * the maximum over all cells); host or device array per `memory`. */
+oc_status oc_cell_transport_speed(oc_op *op, const double *height, const double *discharge,
+                                  int32_t memory, double *speed);
+
 /* Reference state of the mixed form (no reference counterpart; ignored by the
  * FP64 form): a constant depth h_ref = zeta_ref + zb_ref and discharge (qx, qy),
  * typically the undisturbed background of the run (h0, h0 u_inf).  The FP32

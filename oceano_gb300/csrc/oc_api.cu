@@ -43,7 +43,7 @@ cudaError_t upload_tables_hp_v2(const DegTables<double> *, const DegTables<float
 
 cudaError_t aux_upload_tables(const DegTables<double> *, const DegTables<float> *);
 cudaError_t launch_transport_speed(const AuxArgs &, const double *, const double *,
-                                   unsigned long long *, cudaStream_t);
+                                   unsigned long long *, double *, cudaStream_t);
 cudaError_t launch_velocity_field(const AuxArgs &, const double *, const double *, double *,
                                   cudaStream_t);
 cudaError_t launch_vorticity(const AuxArgs &, const double *, int, const double *,
@@ -147,6 +147,8 @@ struct oc_op {
   void *ts_rz[2] = {nullptr, nullptr}, *ts_rq[2] = {nullptr, nullptr};
   double *ts_z = nullptr, *ts_q = nullptr;  // solution when the caller passes host memory
   double *ts_z0 = nullptr, *ts_q0 = nullptr;  // one-stage schemes: copy of u^n (stage input)
+  double *d_cscale = nullptr;  // per-cell step-size scale (NULL: 1)
+  float *d_cscalef = nullptr;
   double *ts_aux = nullptr;
   float *ts_unzf = nullptr, *ts_unqf = nullptr;  // FP32 copies of u^n (mixed time step)
   // mixed form reference state (FP32-representable values)
@@ -866,6 +868,7 @@ static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, doub
       a.r_is_float = mixed ? 1 : 0;
     }
     a.un_z = z; a.un_q = q;
+    a.cscale = op->d_cscale; a.cscalef = op->d_cscalef;
     a.fast_mixed = mixed ? 1 : 0;
     a.un_zf = (mixed && st > 0) ? op->ts_unzf : nullptr;
     a.un_qf = (mixed && st > 0) ? op->ts_unqf : nullptr;
@@ -1019,6 +1022,8 @@ extern "C" oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time
   if (!op || !z || !q) return OC_ERR_INVALID_ARG;
   Scheme sc;
   if (!make_scheme(scheme, sc)) return fail(op, OC_ERR_INVALID_ARG, "unknown scheme");
+  if (sc.ark && op->d_cscale)
+    return fail(op, OC_ERR_UNSUPPORTED, "per-cell time scales with the additive scheme");
   oc_status st = check_boundaries(op);
   if (st != OC_OK) return st;
   st = ensure_ts(op, sc);
@@ -1113,7 +1118,7 @@ extern "C" oc_status oc_transport_speed(oc_op *op, const double *z, const double
     dz = op->st_rz; dq = op->st_rq;
   }
   OC_TRY(cudaMemsetAsync(op->d_speed, 0, sizeof(unsigned long long), op->stream));
-  OC_TRY(launch_transport_speed(aux_args(op), dz, dq, op->d_speed, op->stream));
+  OC_TRY(launch_transport_speed(aux_args(op), dz, dq, op->d_speed, nullptr, op->stream));
   op->launches++;
   unsigned long long bits = 0;
   OC_TRY(cudaMemcpyAsync(&bits, op->d_speed, 8, cudaMemcpyDeviceToHost, op->stream));
@@ -1341,6 +1346,63 @@ extern "C" oc_status oc_project_vortex(oc_op *op, double time, double *z, double
     OC_TRY(cudaMemcpyAsync(z, dz, nz * 8, cudaMemcpyDeviceToHost, op->stream));
     OC_TRY(cudaMemcpyAsync(q, dq, nq * 8, cudaMemcpyDeviceToHost, op->stream));
   }
+  return read_error(op);
+}
+
+extern "C" oc_status oc_set_cell_time_scale(oc_op *op, const double *scale) {
+  if (!op) return OC_ERR_INVALID_ARG;
+  if (!scale) {
+    if (op->d_cscale) {
+      OC_TRY(cudaStreamSynchronize(op->stream));
+      for (void *p : {(void *)op->d_cscale, (void *)op->d_cscalef}) {
+        cudaFree(p);
+        op->bufs.erase(std::find(op->bufs.begin(), op->bufs.end(), p));
+      }
+      op->d_cscale = nullptr;
+      op->d_cscalef = nullptr;
+    }
+  } else {
+    std::vector<float> f(op->n_cells);
+    for (int c = 0; c < op->n_cells; ++c) {
+      if (!(scale[c] > 0.0) || !std::isfinite(scale[c]))
+        return fail(op, OC_ERR_INVALID_ARG, "time scale of cell " + std::to_string(c) +
+                                                " is not a positive finite number");
+      f[c] = (float)scale[c];
+    }
+    if (!op->d_cscale) {
+      OC_TRY(alloc(op, (void **)&op->d_cscale, op->n_cells * sizeof(double)));
+      OC_TRY(alloc(op, (void **)&op->d_cscalef, op->n_cells * sizeof(float)));
+    }
+    OC_TRY(cudaStreamSynchronize(op->stream));
+    OC_TRY(cudaMemcpy(op->d_cscale, scale, op->n_cells * sizeof(double), cudaMemcpyHostToDevice));
+    OC_TRY(cudaMemcpy(op->d_cscalef, f.data(), op->n_cells * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  if (op->graph) {  // the captured step holds the old pointers
+    cudaGraphExecDestroy(op->graph);
+    op->graph = nullptr;
+  }
+  return OC_OK;
+}
+
+extern "C" oc_status oc_cell_transport_speed(oc_op *op, const double *z, const double *q,
+                                             int32_t memory, double *speed) {
+  if (!op || !z || !q || !speed) return OC_ERR_INVALID_ARG;
+  const size_t nz = op->n_dofs, nq = 2 * nz;
+  const double *dz = z, *dq = q;
+  double *out = speed;
+  if (memory == OC_MEM_HOST) {
+    if (ensure(op, &op->st_rz, nz) || ensure(op, &op->st_rq, nq) ||
+        ensure(op, &op->st_nz, std::max<size_t>(nz, op->n_cells)))
+      return OC_ERR_CUDA;
+    OC_TRY(cudaMemcpyAsync(op->st_rz, z, nz * 8, cudaMemcpyHostToDevice, op->stream));
+    OC_TRY(cudaMemcpyAsync(op->st_rq, q, nq * 8, cudaMemcpyHostToDevice, op->stream));
+    dz = op->st_rz; dq = op->st_rq; out = op->st_nz;
+  }
+  OC_TRY(cudaMemsetAsync(op->d_speed, 0, sizeof(unsigned long long), op->stream));
+  OC_TRY(launch_transport_speed(aux_args(op), dz, dq, op->d_speed, out, op->stream));
+  op->launches++;
+  if (memory == OC_MEM_HOST)
+    OC_TRY(cudaMemcpyAsync(speed, out, op->n_cells * 8, cudaMemcpyDeviceToHost, op->stream));
   return read_error(op);
 }
 

@@ -45,7 +45,7 @@ __device__ inline void from_points(int N, const double (*Si)[OC_MAXN], const dou
 // sigma_max(J^-1) sqrt(g h) + |J^-1 u|_inf; positive doubles are ordered like
 // their bit patterns, so the grid maximum is an atomicMax on 64-bit words.
 __global__ void transport_speed_kernel(const AuxArgs a, const double *z, const double *q,
-                                       unsigned long long *out) {
+                                       unsigned long long *out, double *per_cell) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   double local = 0;
   bool nonfinite = false;
@@ -94,6 +94,7 @@ __global__ void transport_speed_kernel(const AuxArgs a, const double *z, const d
       atomicOr(a.err, ERR_NONFINITE);
       local = 0;
     }
+    if (per_cell) per_cell[c] = local;
   }
   for (int o = 16; o > 0; o >>= 1) local = fmax(local, __shfl_xor_sync(OC_FULL, local, o));
   if ((threadIdx.x & 31) == 0 && local > 0)
@@ -206,8 +207,8 @@ cudaError_t aux_upload_tables(const DegTables<double> *td, const DegTables<float
 }
 
 cudaError_t launch_transport_speed(const AuxArgs &a, const double *z, const double *q,
-                                   unsigned long long *out, cudaStream_t st) {
-  transport_speed_kernel<<<(a.n_cells + 127) / 128, 128, 0, st>>>(a, z, q, out);
+                                   unsigned long long *out, double *per_cell, cudaStream_t st) {
+  transport_speed_kernel<<<(a.n_cells + 127) / 128, 128, 0, st>>>(a, z, q, out, per_cell);
   return cudaGetLastError();
 }
 

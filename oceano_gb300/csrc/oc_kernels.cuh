@@ -1412,6 +1412,19 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     return;
   }
 
+  // independent instances with their own step size (time-step path): the cell's
+  // residual scaled by dt_c / dt, so that every later sum f_j k_j carries it
+  if (a.cscale) {
+    if (member && t < N) {
+      const R sc = MIX ? (R)__ldg(a.cscalef + cell) : (R)__ldg(a.cscale + cell);
+#pragma unroll
+      for (int e = 0; e < 3; ++e)
+#pragma unroll
+        for (int ix = 0; ix < N; ++ix) RES[e * NN + t * N + ix] *= sc;
+    }
+    __syncwarp();
+  }
+
   // ---- 3. zeta: pre-lambda + local_apply_cell_mass_height (OceanDG.h:1830-1849)
   //         and local_apply_inverse_mass_matrix_height (:1373-1507) ------------
   // b = sum_{j<s} f_j kz_j (prologue) + f_s L_h zeta, in the reference's order

@@ -122,6 +122,10 @@ struct StageArgs {
   int bc_kind[OC_MAXBID], bc_fn[OC_MAXBID];
   double bc_c[OC_MAXBID][3];
   double vortex[8];
+  // per-cell step-size scale of the time-step path (NULL: 1): the residual of
+  // cell c is multiplied by cscale[c] before the Runge-Kutta update
+  const float *cscalef;
+  const double *cscale;
   // status word (bit flags of oc_status codes)
   int *err;
 };

@@ -184,6 +184,26 @@ class OceanoOperator:
                                        _memory(height, discharge), C.byref(out)), self.h)
         return out.value
 
+    def cell_transport_speed(self, height, discharge):
+        """Per-cell maxima of compute_cell_transport_speed (NumPy in, NumPy out,
+        or CUDA tensors in and a CUDA tensor out)."""
+        mem = _memory(height, discharge)
+        if mem == OC_MEM_DEVICE:
+            import torch
+            out = torch.empty(self.mesh.n_cells, dtype=torch.float64, device=height.device)
+        else:
+            out = np.zeros(self.mesh.n_cells)
+        check(lib().oc_cell_transport_speed(self.h, _ptr(height), _ptr(discharge), mem,
+                                            _ptr(out)), self.h)
+        return out
+
+    def set_cell_time_scale(self, scale=None):
+        """Per-cell step-size scale of perform_time_step (None restores 1)."""
+        s = None if scale is None else np.ascontiguousarray(scale, np.float64)
+        if s is not None and s.size != self.mesh.n_cells:
+            raise ValueError("one scale per cell")
+        check(lib().oc_set_cell_time_scale(self.h, _ptr(s)), self.h)
+
     def apply(self, time, src_height, src_discharge, dst_height, dst_discharge):
         mem = _memory(src_height, src_discharge, dst_height, dst_discharge)
         check(lib().oc_apply(self.h, time, _ptr(src_height), _ptr(src_discharge),

@@ -138,10 +138,25 @@ def vortex_nodal_state(mesh, vx, t=0.0):
     return h.copy(), q
 
 
+def member_time_steps(op, zeta, q, member_of_cell, cfl):
+    """Own step size of every member of a union mesh: dt_m = cfl / (maximum of the
+    member's per-cell transport speeds).  Returns (dt_ref = min dt_m, per-cell
+    scale dt_m / dt_ref) for OceanoOperator.set_cell_time_scale."""
+    sp = op.cell_transport_speed(zeta, q)
+    sp = sp.cpu().numpy() if hasattr(sp, "cpu") else np.asarray(sp)
+    member_of_cell = np.asarray(member_of_cell)
+    vmax = np.zeros(member_of_cell.max() + 1)
+    np.maximum.at(vmax, member_of_cell, sp)
+    dt_m = cfl / vmax
+    dt_ref = float(dt_m.min())
+    return dt_ref, (dt_m / dt_ref)[member_of_cell]
+
+
 def ensemble(n=64, precision="mixed", seed0=1000, members=None):
     """All members as one operator over the disjoint union of their meshes
-    (periodic in x, walls in y), advanced in lockstep with one dt.  Returns
-    (op, zeta, q, members, meshes)."""
+    (periodic in x, walls in y), advanced by one launch per stage.  Each member
+    keeps its own step size through member_time_steps + set_cell_time_scale.
+    Returns (op, zeta, q, members, meshes)."""
     members = members or ensemble_members(n, seed0)
     meshes = [member_mesh(m) for m in members]
     mesh = concatenate_meshes(meshes)

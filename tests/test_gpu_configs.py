@@ -9,6 +9,7 @@
   (time_stepping.h:136-255), FP64 and mixed, whole time steps.
 * apply() = M^-1 L_h (OceanDG.h:1658-1691) against the oracle's apply.
 * Device-side errors of calls on device vectors surface at oc_synchronize.
+* Ensemble members in one operator keep their own step size.
 All GPU calls go through the C ABI (ctypes binding of liboceano_gpu.so).
 """
 import numpy as np
@@ -165,3 +166,39 @@ def test_device_step_reports_nonfinite(gpu_lib, precision):
         op.synchronize()
     assert e.value.status == OC_ERR_NONFINITE
     op.synchronize()  # cleared
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ensemble_members_keep_their_own_dt(gpu_lib, precision):
+    """Independent members in one operator (one launch per stage), each with its
+    own step size through per-cell time scales, against every member advanced
+    alone by its own operator with its own dt: FP64 1e-13, mixed 1e-6."""
+    from oceano_gb300 import workloads as W
+    from oceano_gb300.indicator import member_of_cells
+    mem = W.ensemble_members(3, 1000)
+    for m in mem:
+        m["target"] = 5000.0
+    op, z, q, mem, meshes = W.ensemble(members=mem, precision=precision)
+    moc = member_of_cells(meshes)
+    dt_ref, scale = W.member_time_steps(op, z, q, moc, 0.075)
+    assert scale.min() == 1.0 and scale.max() > 1.0  # the members' dt differ
+    op.set_cell_time_scale(scale)
+    zz, qq = z.copy(), q.copy()
+    for it in range(3):
+        op.perform_time_step("ssp33", it * dt_ref, dt_ref, zz, qq)
+    off = op.mesh.offsets()
+    c0 = 0
+    tol = 1e-13 if precision == "fp64" else 1e-6
+    for k, (m, mesh) in enumerate(zip(mem, meshes)):
+        c1 = c0 + mesh.n_cells
+        opk = W.vortex_operator(mesh, precision, m["vortex"])
+        zk, qk = W.vortex_nodal_state(mesh, m["vortex"])
+        dtk = 0.075 / opk.compute_cell_transport_speed(zk, qk)
+        assert abs(dtk - dt_ref * scale[c0]) <= 1e-13 * dtk
+        for it in range(3):
+            opk.perform_time_step("ssp33", it * dtk, dtk, zk, qk)
+        a, b = off[c0], off[c1]
+        assert rel(zz[a:b], zk) < tol and rel(qq[2 * a:2 * b], qk) < tol
+        opk.close()
+        c0 = c1
+    op.set_cell_time_scale(None)
