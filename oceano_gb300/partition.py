@@ -7,8 +7,10 @@ ranges of balanced DoF counts.  Each rank gets a local mesh made of its owned
 cells followed by the ghost cells that share a face with them; faces between a
 ghost and a cell outside the rank are dropped, so the operator computes the
 owned cells exactly (all their faces are local) and garbage it never uses on
-the ghosts.  Before every stage the ghosts' stage input is refreshed from the
-owners (`HaloExchange.exchange`), the only data exchange of the path.
+the ghosts.  Before every stage the ghosts' face traces are refreshed from the
+owners (`HaloExchange.exchange`: the (p+1) nodal values of zeta, hu, hv per cut
+face side), the only data exchange of the path; dt comes from the owned cells'
+transport speeds through one allreduce MAX (OceanDG.h:2577).
 """
 from __future__ import annotations
 
@@ -122,36 +124,94 @@ def partition(mesh: Mesh, n_parts: int) -> list:
     return parts
 
 
-def _dof_idx(mesh: Mesh, cells):
-    """Local DoF indices (zeta layout, q layout) of the given local cells, in order."""
+def _face_dof(N: int, f: int, i: int) -> int:
+    """Lexicographic node index of node i on face f of a cell with N x N nodes."""
+    return i * N if f == 0 else i * N + N - 1 if f == 1 else i if f == 2 else (N - 1) * N + i
+
+
+def ghost_faces(part: Part) -> list:
+    """(local ghost cell, face number) pairs whose trace an owned cell of the part
+    reads: the ghost side of every local inner face between an owned cell and a
+    ghost (a coarse ghost split into two halves counts once), ordered by the
+    ghost's global cell id and face number."""
+    m, no = part.mesh, part.n_owned
+    ni = m.n_inner
+    cm, cp = m.cell_m[:ni], m.cell_p
+    pairs = set()
+    for i in np.nonzero((cm < no) & (cp >= no))[0]:
+        pairs.add((int(cp[i]), int(m.face_p[i])))
+    for i in np.nonzero((cp < no) & (cm >= no))[0]:
+        pairs.add((int(cm[i]), int(m.face_m[i])))
+    return sorted(pairs, key=lambda x: (int(part.global_cell[x[0]]), x[1]))
+
+
+def _trace_idx(mesh: Mesh, pairs):
+    """Local DoF indices (zeta layout, q layout) of the face traces (p+1 nodes per
+    face and variable) of the given (local cell, face) pairs, in order."""
     off = mesh.offsets()
-    nd = np.diff(off)
-    if len(cells) == 0:
+    z, q = [], []
+    for c, f in pairs:
+        N = int(mesh.degree[c]) + 1
+        d = np.array([_face_dof(N, f, i) for i in range(N)], np.int64)
+        z.append(off[c] + d)
+        q.append(2 * off[c] + d)
+        q.append(2 * off[c] + N * N + d)
+    if not z:
         return np.zeros(0, np.int64), np.zeros(0, np.int64)
-    z = np.concatenate([off[c] + np.arange(nd[c]) for c in cells])
-    q = np.concatenate([2 * off[c] + np.arange(2 * nd[c]) for c in cells])
-    return z, q
+    return np.concatenate(z), np.concatenate(q)
 
 
 def halo_plan(parts: list, rank: int):
     """(send, recv) of one rank: {other rank: (zeta idx, q idx)} into its local vectors.
-    Every rank derives the same plan from the same partition: the ghosts of rank g
-    owned by rank o travel o -> g in g's ghost order (ascending global cell id)."""
+    Only face traces travel: the (p+1) nodal values of zeta, hu and hv on every face
+    of a ghost that an owned cell reads (the operator reads nothing else of a ghost
+    for the owned cells' results; the ghosts' own residuals are discarded).  Every
+    rank derives the same plan from the same partition: the traces of rank g's
+    ghosts owned by rank o travel o -> g in g's ghost_faces order."""
     me = parts[rank]
     send, recv = {}, {}
+    mine = ghost_faces(me)
     for other in parts:
         if other.rank == rank:
             continue
-        # my ghosts owned by `other`
-        mine = [i for i in range(me.n_owned, me.mesh.n_cells) if me.owner[i] == other.rank]
-        if mine:
-            recv[other.rank] = _dof_idx(me.mesh, mine)
-        # other's ghosts owned by me, as local indices of my owned cells
-        theirs = other.global_cell[other.n_owned:][other.owner[other.n_owned:] == rank]
-        if len(theirs):
+        r = [(c, f) for c, f in mine if me.owner[c] == other.rank]
+        if r:
+            recv[other.rank] = _trace_idx(me.mesh, r)
+        theirs = [(int(other.global_cell[c]), f) for c, f in ghost_faces(other)
+                  if other.owner[c] == rank]
+        if theirs:
             pos = {int(c): i for i, c in enumerate(me.global_cell[:me.n_owned])}
-            send[other.rank] = _dof_idx(me.mesh, [pos[int(c)] for c in theirs])
+            send[other.rank] = _trace_idx(me.mesh, [(pos[c], f) for c, f in theirs])
     return send, recv
+
+
+def halo_bytes(parts: list, itemsize: int = 8) -> int:
+    """Bytes all ranks receive per exchange (one refresh of every ghost trace)."""
+    return sum(itemsize * (len(z) + len(q)) for r in range(len(parts))
+               for z, q in halo_plan(parts, r)[1].values())
+
+
+def partitioned_time_step_size(op, part: Part, zeta, q, courant: float, reduce_max=None):
+    """dt = courant / transport speed over the owned cells of all ranks
+    (compute_cell_transport_speed, OceanDG.h:2505-2580, with the MPI max of
+    :2577): per-cell speeds of the local mesh, the maximum over the owned cells,
+    then `reduce_max` (e.g. an allreduce MAX over the ranks) on that number."""
+    sp = op.cell_transport_speed(zeta, q)
+    sp = sp.cpu().numpy() if hasattr(sp, "cpu") else np.asarray(sp)
+    v = float(sp[:part.n_owned].max()) if part.n_owned else 0.0
+    if reduce_max is not None:
+        v = reduce_max(v)
+    return courant / v
+
+
+def torch_max(v: float) -> float:
+    """Allreduce MAX of one number over the torch.distributed process group."""
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 class HaloExchange:

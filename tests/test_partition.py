@@ -110,3 +110,90 @@ def test_gpu_partitioned_matches_single_mesh(gpu_lib, case):
         zr, qr = z[p.dof_index(mesh, "zeta")[:no]], q[p.dof_index(mesh, "q")[:2 * no]]
         assert np.linalg.norm(zp.cpu().numpy()[:no] - zr) <= 1e-12 * np.linalg.norm(zr)
         assert np.linalg.norm(qp.cpu().numpy()[:2 * no] - qr) <= 1e-12 * np.linalg.norm(qr)
+
+
+def test_halo_carries_face_traces_only():
+    """The halo moves the (p+1) nodal values of zeta, hu, hv of every ghost face an
+    owned cell reads: about a (p+1)-fold smaller exchange than whole ghost cells
+    (a ghost bordering two owned cells sends two traces)."""
+    from oceano_gb300 import vortex_mesh
+    from oceano_gb300.partition import ghost_faces, halo_bytes, partition
+    mesh = vortex_mesh(2, 3)  # 80x40 cells, p = 3
+    parts = partition(mesh, 4)
+    traces = halo_bytes(parts)
+    ghosts = sum(8 * 3 * 16 * (p.mesh.n_cells - p.n_owned) for p in parts)
+    n_faces = sum(len(ghost_faces(p)) for p in parts)
+    assert traces == n_faces * 3 * 4 * 8
+    assert traces < ghosts / 3.5  # (p+1) = 4 of the 16 nodes of a cell per face
+
+
+def test_time_step_size_over_owned_cells():
+    """dt of a partitioned run: the maximum over the owned cells of every rank
+    (ghost speeds ignored), reduced over the ranks."""
+    from oceano_gb300.partition import partitioned_time_step_size
+    mesh, full, z0, q0, dt, parts = setup("hanging_p2", 3)
+
+    class Speeds:  # per-cell speeds of a local mesh: the ghosts' are garbage
+        def __init__(self, part):
+            self.v = np.concatenate([np.linspace(1.0, 2.0 + part.rank, part.n_owned),
+                                     np.full(part.mesh.n_cells - part.n_owned, 1e9)])
+
+        def cell_transport_speed(self, z, q):
+            return self.v
+
+    local = [Speeds(p) for p in parts]
+    vmax = max(float(s.v[:p.n_owned].max()) for s, p in zip(local, parts))
+    for s, p in zip(local, parts):
+        dt = partitioned_time_step_size(s, p, None, None, 0.2, reduce_max=lambda v: vmax)
+        assert dt == 0.2 / vmax
+        assert partitioned_time_step_size(s, p, None, None, 0.2) == 0.2 / s.v[:p.n_owned].max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["hanging_p2", "mixed_degree", "hanging_p3_bathy"])
+def test_gpu_partitioned_mixed_matches_single_mesh(gpu_lib, case):
+    """The mixed form (FP32 bulk) on three parts, face traces exchanged in-process
+    between stages, against the same stage sequence on the unpartitioned mesh:
+    the owned cells see identical inputs, so their results agree to rounding."""
+    import torch
+    from oceano_gb300.operator import OceanoOperator
+    from oceano_gb300.partition import local_erk_step, partition, with_ghost_boundary
+    from oceano_gb300.workloads import apply_bcs
+    mesh, full, z0, q0, dt, parts = setup(case, 3)
+    mesh_f, bcs, pdata, friction = CASES[case]
+
+    def make(m):
+        op = OceanoOperator(m, friction=["none", "linear", "manning"][friction],
+                            precision="mixed", zeta_reference=1.0)
+        apply_bcs(op, with_ghost_boundary(bcs))
+        op.set_vortex(*VORTEX)
+        if pdata is not None:
+            op.initialize_data_at_quadrature(pdata)
+        return op
+
+    def stage_of(op):
+        def stage(st, s, t, f, rz, rq, kz, kq, sz, sq, nz, nq):
+            torch.cuda.synchronize()
+            op.perform_stage_hydro(st, s, t, f, [rz, rq], kz, kq, sz, sq, nz, nq)
+            op.synchronize()
+        return stage
+
+    def run(ps):
+        ops = [make(p.mesh) for p in ps]
+        zs = [torch.from_numpy(z0[p.dof_index(mesh, "zeta")].copy()).cuda() for p in ps]
+        qs = [torch.from_numpy(q0[p.dof_index(mesh, "q")].copy()).cuda() for p in ps]
+        tb = O.TABLEAUX["ssp33"]
+        for it in range(3):
+            local_erk_step([stage_of(op) for op in ops], ps, tb, it * dt, dt, zs, qs)
+        torch.cuda.synchronize()
+        return zs, qs
+
+    zs, qs = run(parts)
+    one = partition(mesh, 1)
+    zf, qf = run(one)
+    z, q = zf[0].cpu().numpy(), qf[0].cpu().numpy()
+    for p, zp, qp in zip(parts, zs, qs):
+        no = int(p.mesh.offsets()[p.n_owned])
+        zr, qr = z[p.dof_index(mesh, "zeta")[:no]], q[p.dof_index(mesh, "q")[:2 * no]]
+        assert np.linalg.norm(zp.cpu().numpy()[:no] - zr) <= 1e-14 * np.linalg.norm(zr)
+        assert np.linalg.norm(qp.cpu().numpy()[:2 * no] - qr) <= 1e-14 * np.linalg.norm(qr)
