@@ -337,6 +337,17 @@ oc_status oc_mlp_gradient(oc_mlp *m, const float *features, const float *labels,
 /* one Adam step (beta 0.9, 0.999, eps 1e-8) with the handle's gradient */
 oc_status oc_mlp_adam_step(oc_mlp *m, float lr);
 
+/* GPU time by the reference's TimerOutput scopes (no reference counterpart in the
+ * ABI: the reference times its own calls, OceanDG.h:1796, :1829, main.cc's
+ * "rk time stepping total" and "compute transport speed"; here the two stage
+ * scopes are one fused launch).  With timing on, the GPU work of each
+ * oc_perform_stage_hydro, oc_perform_time_step and oc_transport_speed call is
+ * bracketed by CUDA events on the handle's stream; every call also opens an NVTX
+ * range of that name.  oc_timer_summary writes one line per scope,
+ * "name<TAB>calls<TAB>total seconds<TAB>seconds per call", waiting for pending work. */
+oc_status oc_set_timing(oc_op *op, int32_t on);
+oc_status oc_timer_summary(oc_op *op, char *text, int64_t size);
+
 /* Waits for the handle's stream, then reports and clears the device-side error
  * flags raised since the last check: OC_ERR_UNKNOWN_BOUNDARY_ID from a face
  * kernel, OC_ERR_NONFINITE when a time step or a last stage wrote a non-finite

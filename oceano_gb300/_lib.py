@@ -93,6 +93,8 @@ EXPORTS = {
     "oc_mlp_adam_step": (C.c_int, [C.c_void_p, C.c_float]),
     "oc_set_reference_state": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double]),
     "oc_set_cell_time_scale": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "oc_set_timing": (C.c_int, [C.c_void_p, C.c_int32]),
+    "oc_timer_summary": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
     "oc_cell_transport_speed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                           C.c_void_p]),
     "oc_set_launch_mode": (C.c_int, [C.c_void_p, C.c_int32]),

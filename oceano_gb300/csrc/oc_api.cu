@@ -9,6 +9,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "oceano_gpu.h"
 #include "oc_layout.h"
 #include "oc_tables.hpp"
@@ -168,6 +170,17 @@ struct oc_op {
   unsigned *d_imax = nullptr;
   double *d_epart = nullptr;  // per-cell squared errors + the two results
   int imax_n = 0;
+  // timing by the reference's TimerOutput scope names (oc_set_timing)
+  int timing = 0;
+  struct Scope {
+    const char *name;
+    int64_t calls = 0;
+    double seconds = 0;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+  };
+  Scope scopes[3] = {{"rk_stage hydro - integrals L_h + inv mass + vec upd"},
+                     {"rk time stepping total"},
+                     {"compute transport speed"}};
   // graph cache of oc_perform_time_step
   int64_t graph_launches = 0;
   cudaGraphExec_t graph = nullptr;
@@ -188,6 +201,48 @@ struct oc_op {
 static oc_status fail(oc_op *op, oc_status s, const std::string &msg) {
   if (op) op->err = msg;
   return s;
+}
+
+// A timed region of the handle's stream: events recorded around the enqueued GPU
+// work of one call (no-ops unless timing is on), and an NVTX range around the call.
+enum { SCOPE_STAGE = 0, SCOPE_STEP = 1, SCOPE_SPEED = 2 };
+struct TimedScope {
+  oc_op *op;
+  int scope;
+  cudaEvent_t e0 = nullptr;
+  TimedScope(oc_op *o, int sc) : op(o), scope(sc) {
+    nvtxRangePushA(o->scopes[sc].name);
+    if (o->timing && cudaEventCreate(&e0) == cudaSuccess) cudaEventRecord(e0, o->stream);
+  }
+  ~TimedScope() {
+    if (e0) {
+      cudaEvent_t e1 = nullptr;
+      if (cudaEventCreate(&e1) == cudaSuccess && cudaEventRecord(e1, op->stream) == cudaSuccess) {
+        op->scopes[scope].pending.emplace_back(e0, e1);
+      } else {
+        cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+      }
+    }
+    nvtxRangePop();
+  }
+};
+
+// fold the recorded event pairs into the scope totals (waits for them)
+static void resolve_timers(oc_op *op) {
+  for (auto &sc : op->scopes) {
+    for (auto &ev : sc.pending) {
+      float ms = 0.f;
+      if (cudaEventSynchronize(ev.second) == cudaSuccess &&
+          cudaEventElapsedTime(&ms, ev.first, ev.second) == cudaSuccess) {
+        sc.calls += 1;
+        sc.seconds += 1e-3 * ms;
+      }
+      cudaEventDestroy(ev.first);
+      cudaEventDestroy(ev.second);
+    }
+    sc.pending.clear();
+  }
 }
 
 template <typename T>
@@ -284,6 +339,7 @@ oc_status oc_synchronize(oc_op *op) {
 void oc_destroy(oc_op *op) {
   if (!op) return;
   if (op->stream) cudaStreamSynchronize(op->stream);
+  resolve_timers(op);
   if (op->graph) cudaGraphExecDestroy(op->graph);
   for (void *p : op->bufs) cudaFree(p);
   delete[] op->h_dyn;
@@ -795,7 +851,10 @@ extern "C" oc_status oc_perform_stage_hydro(oc_op *op, uint32_t stage, uint32_t 
   a.out_q = (last && !ark) ? sq : (ark && last ? sq : nqp);
   a.aux_q = (ark && last) ? nqp : nullptr;
   a.out_rz = nullptr; a.out_rq = nullptr;
-  st = launch_groups(op, a, mixed ? 2 : 0);
+  {
+    TimedScope ts(op, SCOPE_STAGE);
+    st = launch_groups(op, a, mixed ? 2 : 0);
+  }
   if (st != OC_OK) return st;
   if (host) {
     cudaStream_t s = op->stream;
@@ -1078,7 +1137,10 @@ extern "C" oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time
     op->graph_scheme = scheme; op->graph_z = dz; op->graph_q = dq;
     op->graph_oz = oz; op->graph_oq = oq;
   }
-  OC_TRY(cudaGraphLaunch(op->graph, op->stream));
+  {
+    TimedScope ts(op, SCOPE_STEP);
+    OC_TRY(cudaGraphLaunch(op->graph, op->stream));
+  }
   op->launches += op->graph_launches;
   if (memory == OC_MEM_HOST) {
     if (!oz) {
@@ -1118,7 +1180,10 @@ extern "C" oc_status oc_transport_speed(oc_op *op, const double *z, const double
     dz = op->st_rz; dq = op->st_rq;
   }
   OC_TRY(cudaMemsetAsync(op->d_speed, 0, sizeof(unsigned long long), op->stream));
-  OC_TRY(launch_transport_speed(aux_args(op), dz, dq, op->d_speed, nullptr, op->stream));
+  {
+    TimedScope ts(op, SCOPE_SPEED);
+    OC_TRY(launch_transport_speed(aux_args(op), dz, dq, op->d_speed, nullptr, op->stream));
+  }
   op->launches++;
   unsigned long long bits = 0;
   OC_TRY(cudaMemcpyAsync(&bits, op->d_speed, 8, cudaMemcpyDeviceToHost, op->stream));
@@ -1347,6 +1412,27 @@ extern "C" oc_status oc_project_vortex(oc_op *op, double time, double *z, double
     OC_TRY(cudaMemcpyAsync(q, dq, nq * 8, cudaMemcpyDeviceToHost, op->stream));
   }
   return read_error(op);
+}
+
+extern "C" oc_status oc_set_timing(oc_op *op, int32_t on) {
+  if (!op) return OC_ERR_INVALID_ARG;
+  op->timing = on ? 1 : 0;
+  return OC_OK;
+}
+
+extern "C" oc_status oc_timer_summary(oc_op *op, char *text, int64_t size) {
+  if (!op || !text || size <= 0) return OC_ERR_INVALID_ARG;
+  resolve_timers(op);
+  std::string out;
+  char line[256];
+  for (const auto &sc : op->scopes) {
+    std::snprintf(line, sizeof line, "%s\t%lld\t%.9g\t%.9g\n", sc.name, (long long)sc.calls,
+                  sc.seconds, sc.calls ? sc.seconds / sc.calls : 0.0);
+    out += line;
+  }
+  if ((int64_t)out.size() + 1 > size) return fail(op, OC_ERR_INVALID_ARG, "timer text buffer too small");
+  std::memcpy(text, out.c_str(), out.size() + 1);
+  return OC_OK;
 }
 
 extern "C" oc_status oc_set_cell_time_scale(oc_op *op, const double *scale) {

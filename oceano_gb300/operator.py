@@ -254,6 +254,20 @@ class OceanoOperator:
             mark = np.ascontiguousarray(mark, np.uint8)
         check(lib().oc_conservative_coarsening(self.h, _ptr(mark), _ptr(height), mem), self.h)
 
+    def set_timing(self, on=True):
+        check(lib().oc_set_timing(self.h, 1 if on else 0), self.h)
+
+    def timer_summary(self) -> dict:
+        """{scope name: (calls, total seconds)} of the GPU work timed so far,
+        named like the reference's TimerOutput scopes."""
+        buf = C.create_string_buffer(4096)
+        check(lib().oc_timer_summary(self.h, buf, len(buf)), self.h)
+        out = {}
+        for line in buf.value.decode().strip().split("\n"):
+            name, calls, total, _ = line.split("\t")
+            out[name] = (int(calls), float(total))
+        return out
+
     def synchronize(self):
         check(lib().oc_synchronize(self.h), self.h)
 

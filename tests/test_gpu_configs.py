@@ -202,3 +202,24 @@ def test_ensemble_members_keep_their_own_dt(gpu_lib, precision):
         opk.close()
         c0 = c1
     op.set_cell_time_scale(None)
+
+
+def test_timers_by_reference_scope_names(gpu_lib):
+    """oc_set_timing / oc_timer_summary: GPU time of each call under the
+    reference's TimerOutput scope names, one call counted per call made."""
+    mesh, orc, op = setup("vortex_p2")
+    z, q = perturbed_state(orc, 1)
+    dt = 0.05 / orc.transport_speed(z, q)
+    op.set_timing(True)
+    for it in range(4):
+        op.perform_time_step("ssp33", it * dt, dt, z, q)
+    op.compute_cell_transport_speed(z, q)
+    n = orc.n
+    kz = [np.zeros(n) for _ in range(4)]
+    kq = [np.zeros(2 * n) for _ in range(4)]
+    op.perform_stage_hydro(0, 3, 0.0, np.array([dt]), [z, q], kz, kq, z.copy(), q.copy(),
+                           np.zeros(n), np.zeros(2 * n))
+    t = op.timer_summary()
+    assert t["rk time stepping total"][0] == 4 and t["rk time stepping total"][1] > 0
+    assert t["compute transport speed"][0] == 1
+    assert t["rk_stage hydro - integrals L_h + inv mass + vec upd"][0] == 1
