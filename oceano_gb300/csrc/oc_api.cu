@@ -44,6 +44,7 @@ cudaError_t upload_tables_hp_v1(const DegTables<double> *, const DegTables<float
 cudaError_t upload_tables_hp_v2(const DegTables<double> *, const DegTables<float> *);
 
 cudaError_t aux_upload_tables(const DegTables<double> *, const DegTables<float> *);
+cudaError_t launch_face_pass(const StageArgs &, int, cudaStream_t);
 cudaError_t launch_transport_speed(const AuxArgs &, const double *, const double *,
                                    unsigned long long *, double *, cudaStream_t);
 cudaError_t launch_velocity_field(const AuxArgs &, const double *, const double *, double *,
@@ -121,6 +122,11 @@ struct oc_op {
   std::vector<int> cfrec, cfsdo;               // per-cell face records for the kernels
   int *d_cfrec = nullptr, *d_cfsdo = nullptr;
   double *d_geo = nullptr, *d_fnrm = nullptr, *d_flen = nullptr;
+  // face pass: work items, output offsets, output buffer, FP32 face geometry
+  std::vector<int> fpts, fofs;
+  int *d_fpts = nullptr, *d_fofs = nullptr;
+  void *d_fout = nullptr;
+  float *d_fnrmf = nullptr, *d_flenf = nullptr;
   float *d_geof = nullptr;
   double *d_dscratch = nullptr;  // mixed form: FP64 zeta work area per (warp, team) slot
   DegTables<double> *d_tabd = nullptr;  // table copies in global memory (divergent reads)
@@ -460,7 +466,18 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
       if (sl[0] == -1) return bad(OC_ERR_INVALID_ARG, "hanging face without subface 0");
     }
   op->sd_size[3] = sf; op->sd_size[4] = sb;
-  // per-cell face records: (other zeta offset | boundary index, packed description)
+  // face pass: output offsets and work items (one per face quadrature point)
+  op->fofs.resize(nf);
+  int64_t fo_total = 0;
+  for (int f = 0; f < nf; ++f) {
+    const int npt = f < ni ? (op->fpack[f] >> 16) & 15 : (3 * op->deg[op->fcm[f]]) / 2 + 1;
+    op->fofs[f] = (int)fo_total;
+    fo_total += (f < ni ? 6 : 3) * npt;
+    for (int k = 0; k < npt; ++k) op->fpts.push_back((f << 3) | k);
+  }
+  if (fo_total >= (int64_t)1 << 31 || (int64_t)nf >= (int64_t)1 << 27)
+    return bad(OC_ERR_UNSUPPORTED, "too many faces for the face pass");
+  // per-cell face records: (face-pass output offset of this side, packed description)
   op->cfrec.assign(16 * (size_t)nc, 0);
   op->cfsdo.assign(8 * (size_t)nc, 0);
   for (int c = 0; c < nc; ++c)
@@ -473,13 +490,13 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
         const int fm = fpk & 15, fp = (fpk >> 4) & 15, sub1 = (fpk >> 8) & 15,
                   orient = (fpk >> 12) & 15, nfq = (fpk >> 16) & 15;
         const int oc = side ? op->fcm[f] : op->fcp[f];
-        other = op->off[oc];
+        other = op->fofs[f] + side * 3 * nfq;
         pk = (side ? fp : fm) | ((side ? fm : fp) << 2) | (op->deg[oc] << 4) | (sub1 << 7) |
              (orient << 9) | (side << 10) | (nfq << 11) | (1 << 14);
         sdo = op->fsd[f];
       } else if (ref < -1) {
         const int b = -ref - 2, f = ni + b;
-        other = b;
+        other = op->fofs[f];
         pk = (op->fpack[f] & 15) | (2 << 14) | (op->bbid[b] << 16);
         sdo = op->fsd[f];
       }
@@ -504,6 +521,14 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   OC_TRY(upload(op, &op->d_bbid, op->bbid.data(), op->bbid.size()));
   OC_TRY(upload(op, &op->d_fnrm, op->fnrm.data(), op->fnrm.size()));
   OC_TRY(upload(op, &op->d_flen, op->flen.data(), op->flen.size()));
+  {
+    std::vector<float> nf32(op->fnrm.begin(), op->fnrm.end()), lf32(op->flen.begin(), op->flen.end());
+    OC_TRY(upload(op, &op->d_fnrmf, nf32.data(), nf32.size()));
+    OC_TRY(upload(op, &op->d_flenf, lf32.data(), lf32.size()));
+  }
+  OC_TRY(upload(op, &op->d_fpts, op->fpts.data(), op->fpts.size()));
+  OC_TRY(upload(op, &op->d_fofs, op->fofs.data(), op->fofs.size()));
+  OC_TRY(alloc(op, &op->d_fout, std::max<size_t>(fo_total, 1) * sizeof(double)));
   for (int k = 0; k < 3; ++k) OC_TRY(upload(op, &op->d_sdo[k], op->sdo[k].data(), nc));
   OC_TRY(upload(op, &op->d_cfrec, op->cfrec.data(), op->cfrec.size()));
   OC_TRY(upload(op, &op->d_cfsdo, op->cfsdo.data(), op->cfsdo.size()));
@@ -678,6 +703,8 @@ static void fill_common(oc_op *op, StageArgs &a) {
   a.sdbe = op->d_sde[4];
   a.sdo0 = op->d_sdo[0]; a.sdo1 = op->d_sdo[1]; a.sdo2 = op->d_sdo[2];
   a.cfrec = op->d_cfrec;
+  a.fpts = op->d_fpts; a.n_fpts = (int64_t)op->fpts.size(); a.fofs = op->d_fofs;
+  a.fout = op->d_fout; a.fnrmf = op->d_fnrmf; a.flenf = op->d_flenf;
   a.geof = op->prm.precision == OC_PREC_MIXED ? op->d_geof : nullptr;
   a.uniform_nn = op->uniform_deg ? (op->uniform_deg + 1) * (op->uniform_deg + 1) : 0;
   a.h_ref = op->ref_h;
@@ -727,6 +754,9 @@ static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
   for (int p = 1; p <= OC_MAXDEG; ++p)
     if (op->group_n[p] && (cells_per_warp(p) / batch) * batch == 0)
       return fail(op, OC_ERR_UNSUPPORTED, "batch_width larger than the cells of a warp");
+  // face pass of the stage: every face's flux once, both sides' values
+  OC_TRY(launch_face_pass(a, variant, op->stream));
+  op->launches++;
   if (op->use_hp && variant != 2 && n_groups(op) > 1) {
     const int wpb = op->hp_wpb;
     int b0 = 0;

@@ -9,9 +9,9 @@
 //   2. evaluates the L_h cell integrals by sum factorisation (x-passes on
 //      node rows, y-passes on point columns, contractions in registers with
 //      constant-bank shape coefficients),
-//   3. evaluates the numerical flux of every face of the cell (conforming,
-//      either side of a hanging face, periodic, boundary) and keeps its own
-//      side; both neighbours evaluate a shared face identically,
+//   3. integrates the face contributions of its four faces (conforming, either
+//      side of a hanging face, periodic, boundary), which the stage's face
+//      pass (oc_face.cu) evaluated once per face and left per side,
 //   4. forms the zeta right-hand side and runs the wet/dry lumped-mass
 //      iteration (FP64: literally, with the batch stop rule; mixed form:
 //      the closed form of the same sweeps on fully wet cells, the literal
@@ -389,8 +389,8 @@ struct Dims {
   static constexpr int T = Q > G ? Q : G;
   static constexpr int NN = N * N, NT = N * T;
   static constexpr int CPW = 32 / T;
-  // scratch tiles of the sum factorisation (also hold the 8 x 3 x OC_MAXN neighbour traces)
-  static constexpr int XS = 6 * NT > 8 * 3 * OC_MAXN ? 6 * NT : 8 * 3 * OC_MAXN;
+  // scratch tiles of the sum factorisation, the zeta solve and the discharge inverse
+  static constexpr int XS = 6 * NT;
   // per-cell shared memory: compute-type region and FP64 region (elements)
   static constexpr int SZR = 10 * NN + XS + 3 * FVS;  // U 3, RES 3, RST 2, BZ 1, ZN 1; X; FV
   static constexpr int SZD = NN + 3 * NT + T + 2;
@@ -785,7 +785,6 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   R *ZN = BZ + NN;            // NN mixed form: zeta^n - zeta_ref
   R *X = ZN + NN;             // scratch tiles
   R *FV = X + D::XS;          // 3*FVS face point values
-  R *NB = X;                  // neighbour traces [slot][var][node] (face phase)
   auto Dreg = [&](int j) {  // FP64 team region of team j: shared (FP64 form) or global slot
     if constexpr (MIX)
       return a.dscratch + ((int64_t)(blockIdx.x * wpb + warp) * OC_MAXCPW + j) * OC_DSTRIDE;
@@ -1108,224 +1107,48 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 
   // ---- 2. faces: local_apply_face_* (OceanDG.h:936-1050) and
   //         local_apply_boundary_face_* (:1105-1339) ----------------------------
+  // The face pass of this stage (oc_face.cu) evaluated every face's flux once and
+  // left, per face side, the point values times sign and JxW; the record of a
+  // slot holds the offset of this side's values.  Each slot's values are
+  // integrated against the own basis: the trace rows of the own side (full face,
+  // or the subface rows on the coarse side of a hanging face), Gauss rows on
+  // boundary faces.
   const FaceRec *recs = reinterpret_cast<const FaceRec *>(w_rec + 16 * team);
-  // 2a. neighbour traces of every inner slot: [slot][var][node], in the scratch
-  // tiles (free between the cell integrals and the zeta solve); a smaller team
-  // region leaves more of the SM's shared memory / L1 to the L1 cache
-  if (member) {
-#pragma unroll
-    for (int ii = 0; ii < (8 * OC_MAXN + T - 1) / T; ++ii) {
-      const int e = t + ii * T;
-      if (e >= 8 * OC_MAXN) break;
-      const int sl = e / OC_MAXN, i = e - sl * OC_MAXN;
-      const FaceRec r = recs[sl];
-      const int Nn = r.nb_deg() + 1;
-      if (r.kind() == 1 && i < Nn) {
-        const int d = face_dof(Nn, r.nb_face(), i);
-        const int64_t oz = r.other, oq = 2 * (int64_t)r.other;
-        NB[(sl * 3 + 0) * OC_MAXN + i] = load_in<RIN, R>(a.rz, oz + d, zref);
-        NB[(sl * 3 + 1) * OC_MAXN + i] = load_in<RIN, R>(a.rq, oq + d, qref0);
-        NB[(sl * 3 + 2) * OC_MAXN + i] = load_in<RIN, R>(a.rq, oq + Nn * Nn + d, qref1);
-      }
-    }
-  }
-  __syncwarp();
-  // own outward normals and face lengths of the affine cell
-  const R J00 = gR[2], J01 = gR[3], J10 = gR[4], J11 = gR[5];
-  // Conforming faces between cells of this degree (the common case): the trace
-  // row of point k = t (both sides: no subface, standard orientation) and the
-  // integration column of node t, held in registers so that the face loop reads
-  // no lane-dependent constant-bank address.
-  R frow[N], fcol[G], fw;
+  // integration column of node t on a full face of this degree, in registers
+  R fcol[G];
   {
-    const int kk = t < G ? t : 0, tt = t < N ? t : 0;
-#pragma unroll
-    for (int i = 0; i < N; ++i) frow[i] = tb.F[0][G][kk][i];
+    const int tt = t < N ? t : 0;
 #pragma unroll
     for (int k = 0; k < G; ++k) fcol[k] = tb.F[0][G][k][tt];
-    fw = tb.wF[G][kk];
   }
-  // lane-dependent table entries of the hanging / degree-jump face paths come
-  // from the global copy (L1), where divergent addresses cost a few wavefronts
-  // instead of one constant-bank replay per distinct address
   const DegTables<R> *gt = reinterpret_cast<const DegTables<R> *>(
       sizeof(R) == 4 ? (const void *)a.gtabf : (const void *)a.gtabd);
   const DegTables<R> &tbg = gt[P - 1];
+  const R *fout = static_cast<const R *>(a.fout);
 #pragma unroll 1
   for (int sl = 0; sl < 8; ++sl) {
     const FaceRec r = recs[sl];
     const int kind = member ? r.kind() : 0;
     // second slots of conforming faces are empty in every team of most warps
     if (!__any_sync(OC_FULL, kind != 0)) continue;
-    // Warp-uniform choice of the inner-face path: the register-row path when every
-    // inner face of the warp in this slot joins two cells of this degree in standard
-    // orientation, else the table path for all of them (one path per warp: on hp
-    // meshes the teams of a warp meet different neighbour degrees, and two paths
-    // would run one after the other)
-    const bool reg_path = __all_sync(OC_FULL, kind != 1 || (r.nb_deg() == P && r.orient() == 0));
     const int fo = r.own_face();
     // DoF of node i on face fo: fbase + i * fstride (face_dof)
     const int fbase = fo == 0 ? 0 : fo == 1 ? N - 1 : fo == 2 ? 0 : (N - 1) * N;
     const int fstride = fo < 2 ? N : 1;
     int nfo = 0, tsel = 0;
-    if (kind != 0) {
-      // outward normal of the own face: J^-T n_ref / |.|; tangent length |J t_ref|
-      const R nr0 = fo == 0 ? R(-1) : fo == 1 ? R(1) : R(0);
-      const R nr1 = fo == 2 ? R(-1) : fo == 3 ? R(1) : R(0);
-      R on0 = Ji00 * nr0 + Ji10 * nr1, on1 = Ji01 * nr0 + Ji11 * nr1;
-      const R inv = R(1) / m_sqrt(on0 * on0 + on1 * on1);
-      on0 *= inv; on1 *= inv;
-      const R tx = fo < 2 ? J01 : J00, ty = fo < 2 ? J11 : J10;
-      R len = m_sqrt(tx * tx + ty * ty);
-      if (kind == 1) {
-        const int side = r.side(), sub = r.sub(), orient = r.orient(), nf = r.nf();
-        const int pn = r.nb_deg(), Nn = pn + 1;
-        const DegTables<R> &tn = gt[pn - 1];
-        if (side == 1 && sub >= 0) len *= R(0.5);  // coarse side: the fine half-face
-        const R n0 = side ? -on0 : on0, n1 = side ? -on1 : on1;  // minus normal
-        const int sdo = a.cfsdo ? w_sdo[8 * team + sl] : 0;
-        nfo = nf;
-        tsel = side ? sub + 1 : 0;
-        if (reg_path) {  // same degree: nf == G <= T, point k on both sides
-          if (t < G) {
-            const int k = t;
-            // trace rows: full face from registers; the coarse side of a hanging
-            // face (own on the plus side, the neighbour's on the minus side) reads
-            // the subface rows
-            const int nsel = side ? 0 : sub + 1;
-            R lo[N], ln[N];
-            if (tsel == 0) {
-#pragma unroll
-              for (int i = 0; i < N; ++i) lo[i] = frow[i];
-            } else {
-#pragma unroll
-              for (int i = 0; i < N; ++i) lo[i] = __ldg(&tbg.F[tsel][G][k][i]);
-            }
-            if (nsel == 0) {
-#pragma unroll
-              for (int i = 0; i < N; ++i) ln[i] = frow[i];
-            } else {
-#pragma unroll
-              for (int i = 0; i < N; ++i) ln[i] = __ldg(&tbg.F[nsel][G][k][i]);
-            }
-            R zo_ = 0, qo0 = 0, qo1 = 0, zn = 0, qn0 = 0, qn1 = 0;
-#pragma unroll
-            for (int i = 0; i < N; ++i) {
-              const int d = fbase + i * fstride;
-              zo_ += lo[i] * U[d];
-              qo0 += lo[i] * U[NN + d];
-              qo1 += lo[i] * U[2 * NN + d];
-              zn += ln[i] * NB[(sl * 3 + 0) * OC_MAXN + i];
-              qn0 += ln[i] * NB[(sl * 3 + 1) * OC_MAXN + i];
-              qn1 += ln[i] * NB[(sl * 3 + 2) * OC_MAXN + i];
-            }
-            const R zm = side ? zn : zo_, qm0 = side ? qn0 : qo0, qm1 = side ? qn1 : qo1;
-            const R zp = side ? zo_ : zn, qp0 = side ? qo0 : qn0, qp1 = side ? qo1 : qn1;
-            R zbm = MIX ? zbe_flat : R(0), zbp = zbm;
-            if (!MIX && a.sdf) {
-              zbm = (R)a.sdf[sdo + 2 * k]; zbp = (R)a.sdf[sdo + 2 * k + 1];
-            }
-            R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
-            if constexpr (MIX) {
-              if (a.sdf)  // bathymetry: well-balanced differences in FP64
-                face_flux_dev_wb<R>(rf, g, cu4, zref, zm, qm0, qm1, zp, qp0, qp1, n0, n1,
-                                    a.sdf[sdo + 2 * k], a.sdf[sdo + 2 * k + 1],
-                                    a.sdfe[sdo + 2 * k], a.sdfe[sdo + 2 * k + 1], F, Fa0, Fa1,
-                                    Pm0, Pm1, Pp0, Pp1);
-              else
-                face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F,
-                                 Fa0, Fa1, Pm0, Pm1, Pp0, Pp1, true);
-            } else
-              face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1,
-                           Pm0, Pm1, Pp0, Pp1);
-            const R jxw = fw * len;
-            const R sg = side ? R(1) : R(-1);
-            FV[k] = sg * F * jxw;
-            FV[FVS + k] = sg * (Fa0 + (side ? Pp0 : Pm0)) * jxw;
-            FV[2 * FVS + k] = sg * (Fa1 + (side ? Pp1 : Pm1)) * jxw;
-          }
-        } else
-        for (int k = t; k < nf; k += T) {
-          const int kp = orient ? nf - 1 - k : k;  // point index on the plus side
-          const int ko = side ? kp : k, kn = side ? k : kp;
-          R zo_ = 0, qo0 = 0, qo1 = 0, zn = 0, qn0 = 0, qn1 = 0;
-#pragma unroll
-          for (int i = 0; i < N; ++i) {  // own trace
-            const int d = face_dof(N, fo, i);
-            const R l = __ldg(&tbg.F[tsel][nf][ko][i]);
-            zo_ += l * U[d];
-            qo0 += l * U[NN + d];
-            qo1 += l * U[2 * NN + d];
-          }
-          const int nsel = side ? 0 : sub + 1;
-#pragma unroll
-          for (int i = 0; i < OC_MAXN; ++i) {  // neighbour trace (Nn <= OC_MAXN nodes)
-            if (i < Nn) {
-              const R l = __ldg(&tn.F[nsel][nf][kn][i]);
-              zn += l * NB[(sl * 3 + 0) * OC_MAXN + i];
-              qn0 += l * NB[(sl * 3 + 1) * OC_MAXN + i];
-              qn1 += l * NB[(sl * 3 + 2) * OC_MAXN + i];
-            }
-          }
-          const R zm = side ? zn : zo_, qm0 = side ? qn0 : qo0, qm1 = side ? qn1 : qo1;
-          const R zp = side ? zo_ : zn, qp0 = side ? qo0 : qn0, qp1 = side ? qo1 : qn1;
-          R zbm = MIX ? zbe_flat : R(0), zbp = zbm;
-          if (!MIX && a.sdf) {
-            zbm = (R)a.sdf[sdo + 2 * k]; zbp = (R)a.sdf[sdo + 2 * k + 1];
-          }
-          R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
-          if constexpr (MIX) {
-            if (a.sdf)  // bathymetry: well-balanced differences in FP64
-              face_flux_dev_wb<R>(rf, g, cu4, zref, zm, qm0, qm1, zp, qp0, qp1, n0, n1,
-                                  a.sdf[sdo + 2 * k], a.sdf[sdo + 2 * k + 1],
-                                  a.sdfe[sdo + 2 * k], a.sdfe[sdo + 2 * k + 1], F, Fa0, Fa1, Pm0,
-                                  Pm1, Pp0, Pp1);
-            else
-              face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0,
-                               Fa1, Pm0, Pm1, Pp0, Pp1, true);
-          } else
-            face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1, Pm0,
-                         Pm1, Pp0, Pp1);
-          const R jxw = __ldg(&tbg.wF[nf][k]) * len;
-          if (side == 0) {
-            FV[ko] = -F * jxw;
-            FV[FVS + ko] = (-Fa0 - Pm0) * jxw;
-            FV[2 * FVS + ko] = (-Fa1 - Pm1) * jxw;
-          } else {
-            FV[ko] = F * jxw;
-            FV[FVS + ko] = (Fa0 + Pp0) * jxw;
-            FV[2 * FVS + ko] = (Fa1 + Pp1) * jxw;
-          }
-        }
-      } else {  // boundary face
-        const int b = r.other;
-        const int bid = r.bid();
-        const int bkind = a.bc_kind[bid];
-        if (bkind == 0 && t == 0) atomicOr(a.err, ERR_UNKNOWN_BID);
-        const int sdo = a.cfsdo ? w_sdo[8 * team + sl] : 0;
-        const R n0 = on0, n1 = on1;
-        nfo = Q;
-        tsel = -1;
-        (void)b;
-        if (t < Q) {
-          const int k = t;
-          R zm = 0, qm0 = 0, qm1 = 0;
-#pragma unroll
-          for (int i = 0; i < N; ++i) {
-            const int d = face_dof(N, fo, i);
-            const R l = tb.BQ[k][i];
-            zm += l * U[d];
-            qm0 += l * U[NN + d];
-            qm1 += l * U[2 * NN + d];
-          }
-          R F, Fa0, Fa1;
-          boundary_flux<R, MIX>(a, bid, bkind, fo, tab<double>(P).xQ[k], geo, zref, sdo + k, g, cu4,
-                                zm, qm0, qm1, n0, n1, F, Fa0, Fa1);
-          const R jxw = tb.wQ[k] * len;
-          FV[k] = -F * jxw;
-          FV[FVS + k] = -Fa0 * jxw;
-          FV[2 * FVS + k] = -Fa1 * jxw;
-        }
+    if (kind == 1) {
+      nfo = r.nf();
+      tsel = r.side() ? r.sub() + 1 : 0;
+    } else if (kind == 2) {
+      nfo = Q;
+      tsel = -1;
+    }
+    if (nfo > 0) {
+      const int64_t base = r.other;
+      for (int k = t; k < nfo; k += T) {
+        FV[k] = ldro<R>(fout, base + k);
+        FV[FVS + k] = ldro<R>(fout, base + nfo + k);
+        FV[2 * FVS + k] = ldro<R>(fout, base + 2 * nfo + k);
       }
     }
     __syncwarp();
