@@ -45,6 +45,8 @@ cudaError_t upload_tables_hp_v2(const DegTables<double> *, const DegTables<float
 
 cudaError_t aux_upload_tables(const DegTables<double> *, const DegTables<float> *);
 cudaError_t launch_face_pass(const StageArgs &, int, cudaStream_t);
+cudaError_t launch_unf32(const StageArgs &, const double *, const double *, float *, float *,
+                         cudaStream_t);
 cudaError_t launch_transport_speed(const AuxArgs &, const double *, const double *,
                                    unsigned long long *, double *, cudaStream_t);
 cudaError_t launch_velocity_field(const AuxArgs &, const double *, const double *, double *,
@@ -694,6 +696,7 @@ oc_status oc_set_static_data(oc_op *op, const double *c0, const double *c1, cons
 
 static void fill_common(oc_op *op, StageArgs &a) {
   std::memset(&a, 0, sizeof(a));
+  a.n_cells = op->n_cells;
   a.deg = op->d_deg; a.off = op->d_off; a.geo = op->d_geo; a.slots = op->d_slots;
   a.fcm = op->d_fcm; a.fcp = op->d_fcp; a.fpack = op->d_fpack; a.fnrm = op->d_fnrm;
   a.flen = op->d_flen; a.fsd = op->d_fsd; a.bbid = op->d_bbid; a.n_inner = op->n_inner;
@@ -947,7 +950,10 @@ static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, doub
     const bool last = st == sc.s - 1;
     a.dyn = op->d_dyn + st;
     a.stage = st; a.n_stages = sc.s; a.ark = sc.ark; a.last = last; a.write_kq_last = 0;
-    if (st == 0) {
+    if (st == 0 && mixed) {
+      // mixed form: the FP32 deviations of u^n (written by unf32 before the stage)
+      a.rz = op->ts_unzf; a.rq = op->ts_unqf; a.r_is_float = 1;
+    } else if (st == 0) {
       // a one-stage scheme overwrites u^n in place: its stage input is a copy
       // (neighbour traces must not see outputs of other blocks)
       a.rz = sc.s == 1 ? op->ts_z0 : z; a.rq = sc.s == 1 ? op->ts_q0 : q;
@@ -961,8 +967,8 @@ static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, doub
     a.fast_mixed = mixed ? 1 : 0;
     a.un_zf = (mixed && st > 0) ? op->ts_unzf : nullptr;
     a.un_qf = (mixed && st > 0) ? op->ts_unqf : nullptr;
-    a.out_unzf = (mixed && st == 0) ? op->ts_unzf : nullptr;
-    a.out_unqf = (mixed && st == 0) ? op->ts_unqf : nullptr;
+    a.out_unzf = nullptr;  // the FP32 copy of u^n comes from unf32
+    a.out_unqf = nullptr;
     for (int j = 0; j <= sc.s; ++j) a.kz[j] = op->ts_kz[j];
     for (int j = 0; j < 2 * OC_MAXSTAGES; ++j) a.kq[j] = op->ts_kq[j];
     if (last) {  // u^{n+1} in place, or into (oz, oq) when given
@@ -983,7 +989,12 @@ static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, doub
 static oc_status enqueue_step(oc_op *op, const Scheme &sc, double *z, double *q,
                               double *oz = nullptr, double *oq = nullptr) {
   const bool mixed = op->prm.precision == OC_PREC_MIXED;
-  if (sc.s == 1) {
+  if (mixed) {  // FP32 deviations of u^n: stage 0's input and the later stages' u^n
+    StageArgs a0;
+    step_stage_args(op, sc, 0, z, q, a0, oz, oq);
+    OC_TRY(launch_unf32(a0, z, q, op->ts_unzf, op->ts_unqf, op->stream));
+    op->launches++;
+  } else if (sc.s == 1) {
     const size_t nz = op->n_dofs;
     OC_TRY(cudaMemcpyAsync(op->ts_z0, z, nz * 8, cudaMemcpyDeviceToDevice, op->stream));
     OC_TRY(cudaMemcpyAsync(op->ts_q0, q, 2 * nz * 8, cudaMemcpyDeviceToDevice, op->stream));
@@ -1042,6 +1053,11 @@ static oc_status autotune(oc_op *op, const Scheme &sc, const double *z, const do
     ce = cudaMemcpyAsync(op->ts_z0, z, nz * 8, cudaMemcpyDeviceToDevice, op->stream);
   if (ce == cudaSuccess && sc.s == 1)
     ce = cudaMemcpyAsync(op->ts_q0, q, nq * 8, cudaMemcpyDeviceToDevice, op->stream);
+  if (ce == cudaSuccess && op->prm.precision == OC_PREC_MIXED) {  // stage 0 input of the mixed step
+    StageArgs a0;
+    step_stage_args(op, sc, 0, tz, tq, a0);
+    ce = launch_unf32(a0, tz, tq, op->ts_unzf, op->ts_unqf, op->stream);
+  }
   if (ce != cudaSuccess) st = fail(op, OC_ERR_CUDA, cudaGetErrorString(ce));
   const int64_t launches = op->launches;
   const int reps = 5;

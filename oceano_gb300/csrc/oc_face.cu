@@ -134,6 +134,31 @@ __global__ void __launch_bounds__(256) face_kernel(const StageArgs a) {
   }
 }
 
+// FP32 deviations of the FP64 state, (zeta - zeta_ref, q - q_ref): the stage
+// input of the first stage of the mixed time step, and the copy of u^n its later
+// stages read.  One thread per (cell, node) slot of the largest degree.
+__global__ void __launch_bounds__(256) unf32_kernel(const StageArgs a, const double *z,
+                                                    const double *q, float *zf, float *qf) {
+  constexpr int S = OC_MAXN * OC_MAXN;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t c = i / S;
+  const int d = (int)(i - c * S);
+  if (c >= a.n_cells) return;
+  const int N = __ldg(a.deg + c) + 1, NN = N * N;
+  if (d >= NN) return;
+  const int64_t o = a.uniform_nn ? c * a.uniform_nn : (int64_t)__ldg(a.off + c);
+  zf[o + d] = (float)(__ldg(z + o + d) - a.zeta_ref);
+  qf[2 * o + d] = (float)(__ldg(q + 2 * o + d) - a.q_ref[0]);
+  qf[2 * o + NN + d] = (float)(__ldg(q + 2 * o + NN + d) - a.q_ref[1]);
+}
+
+cudaError_t launch_unf32(const StageArgs &a, const double *z, const double *q, float *zf,
+                         float *qf, cudaStream_t st) {
+  const int64_t n = (int64_t)a.n_cells * OC_MAXN * OC_MAXN;
+  unf32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a, z, q, zf, qf);
+  return cudaGetLastError();
+}
+
 // variant 0: FP64; 1: mixed with FP32 stage input; 2: mixed with FP64 stage input
 cudaError_t launch_face_pass(const StageArgs &a, int variant, cudaStream_t st) {
   if (a.n_fpts == 0) return cudaSuccess;

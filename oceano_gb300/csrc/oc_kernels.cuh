@@ -389,10 +389,12 @@ struct Dims {
   static constexpr int T = Q > G ? Q : G;
   static constexpr int NN = N * N, NT = N * T;
   static constexpr int CPW = 32 / T;
-  // scratch tiles of the sum factorisation, the zeta solve and the discharge inverse
-  static constexpr int XS = 6 * NT;
+  // scratch tiles of the sum factorisation, the zeta solve and the discharge
+  // inverse; between the cell integrals and the zeta solve they hold the face
+  // pass's point values of the cell's 8 face slots ([slot][var][FVS])
+  static constexpr int XS = 6 * NT > 8 * 3 * FVS ? 6 * NT : 8 * 3 * FVS;
   // per-cell shared memory: compute-type region and FP64 region (elements)
-  static constexpr int SZR = 10 * NN + XS + 3 * FVS;  // U 3, RES 3, RST 2, BZ 1, ZN 1; X; FV
+  static constexpr int SZR = 10 * NN + XS;  // U 3, RES 3, RST 2, BZ 1, ZN 1; X
   static constexpr int SZD = NN + 3 * NT + T + 2;
   // Team strides: padded so that the 32/T teams of a warp start on different
   // shared-memory banks (stride mod 32 chosen per degree and element size to
@@ -726,10 +728,10 @@ __device__ __forceinline__ void report_nonfinite(const StageArgs &a, bool bad) {
 //   MIX = false: FP64 plain form (R = KT = double).
 //   MIX = true : mixed form; R = float bulk, KT = type of the k registers.
 // Memory flow: warp-cooperative prologue (stage input, face records, partial
-// zeta right-hand side), team-local cell integrals, neighbour traces of all face
-// slots loaded into the scratch tiles for the face phase, team-local zeta and
-// discharge solves, warp-cooperative epilogue (RK update and stores).  Global
-// accesses of the prologue/epilogue are lane-contiguous over the warp's cells.
+// zeta right-hand side), team-local cell integrals, the face pass's point values
+// of the cell's face sides, team-local zeta and discharge solves,
+// warp-cooperative epilogue (RK update and stores).  Global accesses of the
+// prologue/epilogue are lane-contiguous over the warp's cells.
 // ---------------------------------------------------------------------------
 // resident 4-warp blocks per SM the mixed kernels are compiled for (register cap)
 #ifndef OC_MIXED_MIN_BLOCKS
@@ -784,7 +786,6 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   R *BZ = RST + 2 * NN;       // NN zeta right-hand side b = sum f k (mixed: then delta)
   R *ZN = BZ + NN;            // NN mixed form: zeta^n - zeta_ref
   R *X = ZN + NN;             // scratch tiles
-  R *FV = X + D::XS;          // 3*FVS face point values
   auto Dreg = [&](int j) {  // FP64 team region of team j: shared (FP64 form) or global slot
     if constexpr (MIX)
       return a.dscratch + ((int64_t)(blockIdx.x * wpb + warp) * OC_MAXCPW + j) * OC_DSTRIDE;
@@ -1125,6 +1126,22 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       sizeof(R) == 4 ? (const void *)a.gtabf : (const void *)a.gtabd);
   const DegTables<R> &tbg = gt[P - 1];
   const R *fout = static_cast<const R *>(a.fout);
+  // the values of all slots in one memory round trip, into the scratch tiles
+  R *FVA = X;
+  if (member) {
+#pragma unroll
+    for (int sl = 0; sl < 8; ++sl) {
+      const FaceRec r = recs[sl];
+      const int kind = r.kind();
+      const int nfo = kind == 1 ? r.nf() : kind == 2 ? Q : 0;
+      for (int k = t; k < nfo; k += T) {
+        FVA[(sl * 3 + 0) * FVS + k] = ldro<R>(fout, (int64_t)r.other + k);
+        FVA[(sl * 3 + 1) * FVS + k] = ldro<R>(fout, (int64_t)r.other + nfo + k);
+        FVA[(sl * 3 + 2) * FVS + k] = ldro<R>(fout, (int64_t)r.other + 2 * nfo + k);
+      }
+    }
+  }
+  __syncwarp();
 #pragma unroll 1
   for (int sl = 0; sl < 8; ++sl) {
     const FaceRec r = recs[sl];
@@ -1143,15 +1160,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       nfo = Q;
       tsel = -1;
     }
-    if (nfo > 0) {
-      const int64_t base = r.other;
-      for (int k = t; k < nfo; k += T) {
-        FV[k] = ldro<R>(fout, base + k);
-        FV[FVS + k] = ldro<R>(fout, base + nfo + k);
-        FV[2 * FVS + k] = ldro<R>(fout, base + 2 * nfo + k);
-      }
-    }
-    __syncwarp();
+    const R *FV = FVA + sl * 3 * FVS;
     // integration rows: registers when every face of the warp in this slot is a full
     // face of this degree's point set, else the global table copy (boundary faces:
     // Gauss rows; inner faces: the trace rows of the own side)

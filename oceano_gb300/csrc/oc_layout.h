@@ -57,6 +57,7 @@ struct RefStateF {
 // < -1: boundary face b encoded as -(b+2); -1: empty.
 struct StageArgs {
   // mesh
+  int n_cells;
   int n_group;                 // cells processed by this launch
   const int *group_cells;      // their ids (NULL: identity starting at group_first)
   int group_first;
