@@ -44,7 +44,8 @@ cudaError_t upload_tables_hp_v1(const DegTables<double> *, const DegTables<float
 cudaError_t upload_tables_hp_v2(const DegTables<double> *, const DegTables<float> *);
 
 cudaError_t aux_upload_tables(const DegTables<double> *, const DegTables<float> *);
-cudaError_t launch_face_pass(const StageArgs &, int, cudaStream_t);
+cudaError_t launch_face_pass(const StageArgs &, int, int, cudaStream_t);
+cudaError_t face_upload_tables(const DegTables<double> *, const DegTables<float> *);
 cudaError_t launch_unf32(const StageArgs &, const double *, const double *, float *, float *,
                          cudaStream_t);
 cudaError_t launch_transport_speed(const AuxArgs &, const double *, const double *,
@@ -124,9 +125,9 @@ struct oc_op {
   std::vector<int> cfrec, cfsdo;               // per-cell face records for the kernels
   int *d_cfrec = nullptr, *d_cfsdo = nullptr;
   double *d_geo = nullptr, *d_fnrm = nullptr, *d_flen = nullptr;
-  // face pass: work items, output offsets, output buffer, FP32 face geometry
-  std::vector<int> fpts, fofs;
-  int *d_fpts = nullptr, *d_fofs = nullptr;
+  // face pass: output offsets, output buffer, FP32 face geometry
+  std::vector<int> fofs;
+  int *d_fofs = nullptr;
   void *d_fout = nullptr;
   float *d_fnrmf = nullptr, *d_flenf = nullptr;
   float *d_geof = nullptr;
@@ -468,14 +469,13 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
       if (sl[0] == -1) return bad(OC_ERR_INVALID_ARG, "hanging face without subface 0");
     }
   op->sd_size[3] = sf; op->sd_size[4] = sb;
-  // face pass: output offsets and work items (one per face quadrature point)
+  // face pass: output offset of every face
   op->fofs.resize(nf);
   int64_t fo_total = 0;
   for (int f = 0; f < nf; ++f) {
     const int npt = f < ni ? (op->fpack[f] >> 16) & 15 : (3 * op->deg[op->fcm[f]]) / 2 + 1;
     op->fofs[f] = (int)fo_total;
     fo_total += (f < ni ? 6 : 3) * npt;
-    for (int k = 0; k < npt; ++k) op->fpts.push_back((f << 3) | k);
   }
   if (fo_total >= (int64_t)1 << 31 || (int64_t)nf >= (int64_t)1 << 27)
     return bad(OC_ERR_UNSUPPORTED, "too many faces for the face pass");
@@ -528,7 +528,6 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
     OC_TRY(upload(op, &op->d_fnrmf, nf32.data(), nf32.size()));
     OC_TRY(upload(op, &op->d_flenf, lf32.data(), lf32.size()));
   }
-  OC_TRY(upload(op, &op->d_fpts, op->fpts.data(), op->fpts.size()));
   OC_TRY(upload(op, &op->d_fofs, op->fofs.data(), op->fofs.size()));
   OC_TRY(alloc(op, &op->d_fout, std::max<size_t>(fo_total, 1) * sizeof(double)));
   for (int k = 0; k < 3; ++k) OC_TRY(upload(op, &op->d_sdo[k], op->sdo[k].data(), nc));
@@ -572,6 +571,7 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   OC_TRY(upload_tables_hp_v1(td.data(), tf.data()));
   OC_TRY(upload_tables_hp_v2(td.data(), tf.data()));
   OC_TRY(aux_upload_tables(td.data(), tf.data()));
+  OC_TRY(face_upload_tables(td.data(), tf.data()));
   OC_TRY(alloc(op, (void **)&op->d_err, sizeof(int)));
   OC_TRY(alloc(op, (void **)&op->d_speed, sizeof(unsigned long long)));
   OC_TRY(alloc(op, (void **)&op->d_dyn, sizeof(StageDyn) * (OC_MAXSTAGES + 1)));
@@ -706,7 +706,7 @@ static void fill_common(oc_op *op, StageArgs &a) {
   a.sdbe = op->d_sde[4];
   a.sdo0 = op->d_sdo[0]; a.sdo1 = op->d_sdo[1]; a.sdo2 = op->d_sdo[2];
   a.cfrec = op->d_cfrec;
-  a.fpts = op->d_fpts; a.n_fpts = (int64_t)op->fpts.size(); a.fofs = op->d_fofs;
+  a.n_bnd_faces = op->n_bnd; a.fofs = op->d_fofs;
   a.fout = op->d_fout; a.fnrmf = op->d_fnrmf; a.flenf = op->d_flenf;
   a.geof = op->prm.precision == OC_PREC_MIXED ? op->d_geof : nullptr;
   a.uniform_nn = op->uniform_deg ? (op->uniform_deg + 1) * (op->uniform_deg + 1) : 0;
@@ -758,7 +758,7 @@ static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
     if (op->group_n[p] && (cells_per_warp(p) / batch) * batch == 0)
       return fail(op, OC_ERR_UNSUPPORTED, "batch_width larger than the cells of a warp");
   // face pass of the stage: every face's flux once, both sides' values
-  OC_TRY(launch_face_pass(a, variant, op->stream));
+  OC_TRY(launch_face_pass(a, variant, op->uniform_deg, op->stream));
   op->launches++;
   if (op->use_hp && variant != 2 && n_groups(op) > 1) {
     const int wpb = op->hp_wpb;

@@ -374,6 +374,21 @@ __device__ __forceinline__ R load_in(const void *p, int64_t i, double ref) {
   }
 }
 
+// asynchronous global -> shared copy of one element (cp.async, no register
+// staging), and the wait of the calling thread for all of its copies
+template <typename T>
+__device__ __forceinline__ void cp_async(T *smem, const T *gmem) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (sizeof(T) == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 // read-only load of a stage register (FP32 or FP64)
 template <typename KT>
 __device__ __forceinline__ KT ldro(const void *p, int64_t i) {
@@ -835,6 +850,24 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   // writes buffers it may still read, so it waits for that launch to complete.
   // Without a programmatic launch the wait returns at once.
   asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  __syncwarp();
+  // the face pass's point values of the team's 8 face slots, copied asynchronously
+  // into the scratch tiles ([slot][var][FVS]; free until the cell integrals) while
+  // the stage input below is loaded: one memory round trip for both
+  const FaceRec *recs = reinterpret_cast<const FaceRec *>(w_rec + 16 * team);
+  if (member) {
+    const R *fout = static_cast<const R *>(a.fout);
+#pragma unroll
+    for (int sl = 0; sl < 8; ++sl) {
+      const FaceRec r = recs[sl];
+      const int kind = r.kind();
+      const int nfo = kind == 1 ? r.nf() : kind == 2 ? Q : 0;
+      for (int k = t; k < nfo; k += T)
+#pragma unroll
+        for (int v = 0; v < 3; ++v)
+          cp_async(X + (sl * 3 + v) * FVS + k, fout + (int64_t)r.other + v * nfo + k);
+    }
+  }
   R fR[OC_MAXSTAGES];  // coefficients in the compute type (mixed form: the FP32 copies)
   load_coefs<R>(a.dyn->ff, a.dyn->f, fR);
   R fRs = fR[0];  // f_s
@@ -887,11 +920,91 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       }
     }
   }
+  cp_async_wait_all();
   __syncwarp();
   const R Ji00 = gR[6], Ji01 = gR[7], Ji10 = gR[8], Ji11 = gR[9];
   const R det = gR[10];
 
-  // ---- 1. cell integrals: local_apply_cell_height (OceanDG.h:669-693),
+  // ---- 1. faces: local_apply_face_* (OceanDG.h:936-1050) and
+  //         local_apply_boundary_face_* (:1105-1339) ----------------------------
+  // The face pass of this stage (oc_face.cu) evaluated every face's flux once and
+  // left, per face side, the point values times sign and JxW; the record of a
+  // slot holds the offset of this side's values.  Each slot's values are
+  // integrated against the own basis: the trace rows of the own side (full face,
+  // or the subface rows on the coarse side of a hanging face), Gauss rows on
+  // boundary faces.
+  // integration column of node t on a full face of this degree, in registers
+  R fcol[G];
+  {
+    const int tt = t < N ? t : 0;
+#pragma unroll
+    for (int k = 0; k < G; ++k) fcol[k] = tb.F[0][G][k][tt];
+  }
+  const DegTables<R> *gt = reinterpret_cast<const DegTables<R> *>(
+      sizeof(R) == 4 ? (const void *)a.gtabf : (const void *)a.gtabd);
+  const DegTables<R> &tbg = gt[P - 1];
+  // the values of all slots were copied into the scratch tiles by the prologue
+  R *FVA = X;
+  if (member && t < N) {
+#pragma unroll
+    for (int e = 0; e < 3; ++e)
+#pragma unroll
+      for (int ix = 0; ix < N; ++ix) RES[e * NN + t * N + ix] = R(0);
+  }
+  __syncwarp();
+#pragma unroll 1
+  for (int sl = 0; sl < 8; ++sl) {
+    const FaceRec r = recs[sl];
+    const int kind = member ? r.kind() : 0;
+    // second slots of conforming faces are empty in every team of most warps
+    if (!__any_sync(OC_FULL, kind != 0)) continue;
+    const int fo = r.own_face();
+    // DoF of node i on face fo: fbase + i * fstride (face_dof)
+    const int fbase = fo == 0 ? 0 : fo == 1 ? N - 1 : fo == 2 ? 0 : (N - 1) * N;
+    const int fstride = fo < 2 ? N : 1;
+    int nfo = 0, tsel = 0;
+    if (kind == 1) {
+      nfo = r.nf();
+      tsel = r.side() ? r.sub() + 1 : 0;
+    } else if (kind == 2) {
+      nfo = Q;
+      tsel = -1;
+    }
+    const R *FV = FVA + sl * 3 * FVS;
+    // integration rows: registers when every face of the warp in this slot is a full
+    // face of this degree's point set, else the global table copy (boundary faces:
+    // Gauss rows; inner faces: the trace rows of the own side)
+    const bool reg_cols = __all_sync(OC_FULL, nfo == 0 || (tsel == 0 && nfo == G));
+    if (nfo > 0 && t < N) {  // integrate the own-side values against the own basis
+      R cz = 0, c0 = 0, c1 = 0;
+      if (reg_cols) {
+#pragma unroll
+        for (int k = 0; k < G; ++k) {
+          cz += fcol[k] * FV[k];
+          c0 += fcol[k] * FV[FVS + k];
+          c1 += fcol[k] * FV[2 * FVS + k];
+        }
+      } else {
+        const R *col = tsel < 0 ? &tbg.BQ[0][t] : &tbg.F[tsel][nfo][0][t];  // stride OC_MAXN
+#pragma unroll
+        for (int k = 0; k < (Q > OC_MAXF ? Q : OC_MAXF); ++k) {  // nfo <= max(Q, OC_MAXF)
+          if (k < nfo) {
+            const R l = __ldg(col + k * OC_MAXN);
+            cz += l * FV[k];
+            c0 += l * FV[FVS + k];
+            c1 += l * FV[2 * FVS + k];
+          }
+        }
+      }
+      const int d = fbase + t * fstride;
+      RES[d] += cz;
+      RES[NN + d] += c0;
+      RES[2 * NN + d] += c1;
+    }
+    __syncwarp();
+  }
+
+  // ---- 2. cell integrals: local_apply_cell_height (OceanDG.h:669-693),
   //         local_apply_cell_discharge / _nonstiff / _stiff (:695-826) ---------
   if (member && t < N) {  // x-pass on rows iy = t
     R z[N], q0[N], q1[N];
@@ -1018,9 +1131,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           r0 += d * X[2 * NT + t * T + qx] + b * X[3 * NT + t * T + qx];
           r1 += d * X[4 * NT + t * T + qx] + b * X[5 * NT + t * T + qx];
         }
-        RES[t * N + ix] = rz;
-        RES[NN + t * N + ix] = r0;
-        RES[2 * NN + t * N + ix] = r1;
+        RES[t * N + ix] += rz;
+        RES[NN + t * N + ix] += r0;
+        RES[2 * NN + t * N + ix] += r1;
       }
     }
     __syncwarp();
@@ -1102,94 +1215,6 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         RST[t * N + ix] = r0;
         RST[NN + t * N + ix] = r1;
       }
-    }
-    __syncwarp();
-  }
-
-  // ---- 2. faces: local_apply_face_* (OceanDG.h:936-1050) and
-  //         local_apply_boundary_face_* (:1105-1339) ----------------------------
-  // The face pass of this stage (oc_face.cu) evaluated every face's flux once and
-  // left, per face side, the point values times sign and JxW; the record of a
-  // slot holds the offset of this side's values.  Each slot's values are
-  // integrated against the own basis: the trace rows of the own side (full face,
-  // or the subface rows on the coarse side of a hanging face), Gauss rows on
-  // boundary faces.
-  const FaceRec *recs = reinterpret_cast<const FaceRec *>(w_rec + 16 * team);
-  // integration column of node t on a full face of this degree, in registers
-  R fcol[G];
-  {
-    const int tt = t < N ? t : 0;
-#pragma unroll
-    for (int k = 0; k < G; ++k) fcol[k] = tb.F[0][G][k][tt];
-  }
-  const DegTables<R> *gt = reinterpret_cast<const DegTables<R> *>(
-      sizeof(R) == 4 ? (const void *)a.gtabf : (const void *)a.gtabd);
-  const DegTables<R> &tbg = gt[P - 1];
-  const R *fout = static_cast<const R *>(a.fout);
-  // the values of all slots in one memory round trip, into the scratch tiles
-  R *FVA = X;
-  if (member) {
-#pragma unroll
-    for (int sl = 0; sl < 8; ++sl) {
-      const FaceRec r = recs[sl];
-      const int kind = r.kind();
-      const int nfo = kind == 1 ? r.nf() : kind == 2 ? Q : 0;
-      for (int k = t; k < nfo; k += T) {
-        FVA[(sl * 3 + 0) * FVS + k] = ldro<R>(fout, (int64_t)r.other + k);
-        FVA[(sl * 3 + 1) * FVS + k] = ldro<R>(fout, (int64_t)r.other + nfo + k);
-        FVA[(sl * 3 + 2) * FVS + k] = ldro<R>(fout, (int64_t)r.other + 2 * nfo + k);
-      }
-    }
-  }
-  __syncwarp();
-#pragma unroll 1
-  for (int sl = 0; sl < 8; ++sl) {
-    const FaceRec r = recs[sl];
-    const int kind = member ? r.kind() : 0;
-    // second slots of conforming faces are empty in every team of most warps
-    if (!__any_sync(OC_FULL, kind != 0)) continue;
-    const int fo = r.own_face();
-    // DoF of node i on face fo: fbase + i * fstride (face_dof)
-    const int fbase = fo == 0 ? 0 : fo == 1 ? N - 1 : fo == 2 ? 0 : (N - 1) * N;
-    const int fstride = fo < 2 ? N : 1;
-    int nfo = 0, tsel = 0;
-    if (kind == 1) {
-      nfo = r.nf();
-      tsel = r.side() ? r.sub() + 1 : 0;
-    } else if (kind == 2) {
-      nfo = Q;
-      tsel = -1;
-    }
-    const R *FV = FVA + sl * 3 * FVS;
-    // integration rows: registers when every face of the warp in this slot is a full
-    // face of this degree's point set, else the global table copy (boundary faces:
-    // Gauss rows; inner faces: the trace rows of the own side)
-    const bool reg_cols = __all_sync(OC_FULL, nfo == 0 || (tsel == 0 && nfo == G));
-    if (nfo > 0 && t < N) {  // integrate the own-side values against the own basis
-      R cz = 0, c0 = 0, c1 = 0;
-      if (reg_cols) {
-#pragma unroll
-        for (int k = 0; k < G; ++k) {
-          cz += fcol[k] * FV[k];
-          c0 += fcol[k] * FV[FVS + k];
-          c1 += fcol[k] * FV[2 * FVS + k];
-        }
-      } else {
-        const R *col = tsel < 0 ? &tbg.BQ[0][t] : &tbg.F[tsel][nfo][0][t];  // stride OC_MAXN
-#pragma unroll
-        for (int k = 0; k < (Q > OC_MAXF ? Q : OC_MAXF); ++k) {  // nfo <= max(Q, OC_MAXF)
-          if (k < nfo) {
-            const R l = __ldg(col + k * OC_MAXN);
-            cz += l * FV[k];
-            c0 += l * FV[FVS + k];
-            c1 += l * FV[2 * FVS + k];
-          }
-        }
-      }
-      const int d = fbase + t * fstride;
-      RES[d] += cz;
-      RES[NN + d] += c0;
-      RES[2 * NN + d] += c1;
     }
     __syncwarp();
   }

@@ -75,11 +75,10 @@ struct StageArgs {
   const int *fsd;              // inner: offset into sdf; boundary: offset into sdb
   const int *bbid;             // [n_bnd] boundary id
   int n_inner;
-  // face pass: work items (face << 3 | point), the offset of every face's output
+  // face pass: boundary faces, the offset of every face's output
   // (inner: minus [3][nf] then plus [3][nf]; boundary: [3][Q]) and the output
   // (R values: double in the FP64 form, float in the mixed form)
-  const int *fpts;
-  int64_t n_fpts;
+  int n_bnd_faces;
   const int *fofs;
   void *fout;
   const float *fnrmf, *flenf;  // FP32 copies of fnrm, flen
