@@ -122,8 +122,8 @@ struct oc_op {
   int *d_deg = nullptr, *d_off = nullptr, *d_slots = nullptr, *d_fcm = nullptr,
       *d_fcp = nullptr, *d_fpack = nullptr, *d_fsd = nullptr, *d_bbid = nullptr;
   int *d_sdo[3] = {nullptr, nullptr, nullptr};
-  std::vector<int> cfrec, cfsdo;               // per-cell face records for the kernels
-  int *d_cfrec = nullptr, *d_cfsdo = nullptr;
+  std::vector<int> cfrec, cfsdo, cfofs;        // per-cell face records for the kernels
+  int *d_cfrec = nullptr, *d_cfsdo = nullptr, *d_cfofs = nullptr;
   double *d_geo = nullptr, *d_fnrm = nullptr, *d_flen = nullptr;
   // face pass: output offsets, output buffer, FP32 face geometry
   std::vector<int> fofs;
@@ -479,32 +479,37 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   }
   if (fo_total >= (int64_t)1 << 31 || (int64_t)nf >= (int64_t)1 << 27)
     return bad(OC_ERR_UNSUPPORTED, "too many faces for the face pass");
-  // per-cell face records: (face-pass output offset of this side, packed description)
+  // per-cell face records: (other zeta offset | boundary index, packed description),
+  // and the face-pass output offset of each slot side
   op->cfrec.assign(16 * (size_t)nc, 0);
   op->cfsdo.assign(8 * (size_t)nc, 0);
+  op->cfofs.assign(8 * (size_t)nc, -1);
   for (int c = 0; c < nc; ++c)
     for (int sl = 0; sl < 8; ++sl) {
       const int ref = op->slots[8 * (size_t)c + sl];
-      int other = -1, pk = 0, sdo = 0;
+      int other = -1, pk = 0, sdo = 0, fofs = -1;
       if (ref >= 0) {
         const int f = ref >> 1, side = ref & 1;
         const int fpk = op->fpack[f];
         const int fm = fpk & 15, fp = (fpk >> 4) & 15, sub1 = (fpk >> 8) & 15,
                   orient = (fpk >> 12) & 15, nfq = (fpk >> 16) & 15;
         const int oc = side ? op->fcm[f] : op->fcp[f];
-        other = op->fofs[f] + side * 3 * nfq;
+        other = op->off[oc];
+        fofs = op->fofs[f] + side * 3 * nfq;
         pk = (side ? fp : fm) | ((side ? fm : fp) << 2) | (op->deg[oc] << 4) | (sub1 << 7) |
              (orient << 9) | (side << 10) | (nfq << 11) | (1 << 14);
         sdo = op->fsd[f];
       } else if (ref < -1) {
         const int b = -ref - 2, f = ni + b;
-        other = op->fofs[f];
+        other = b;
+        fofs = op->fofs[f];
         pk = (op->fpack[f] & 15) | (2 << 14) | (op->bbid[b] << 16);
         sdo = op->fsd[f];
       }
       op->cfrec[16 * (size_t)c + 2 * sl] = other;
       op->cfrec[16 * (size_t)c + 2 * sl + 1] = pk;
       op->cfsdo[8 * (size_t)c + sl] = sdo;
+      op->cfofs[8 * (size_t)c + sl] = fofs;
     }
   // device
   OC_TRY(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
@@ -533,6 +538,7 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   for (int k = 0; k < 3; ++k) OC_TRY(upload(op, &op->d_sdo[k], op->sdo[k].data(), nc));
   OC_TRY(upload(op, &op->d_cfrec, op->cfrec.data(), op->cfrec.size()));
   OC_TRY(upload(op, &op->d_cfsdo, op->cfsdo.data(), op->cfsdo.size()));
+  OC_TRY(upload(op, &op->d_cfofs, op->cfofs.data(), op->cfofs.size()));
   for (int p = 1; p <= OC_MAXDEG; ++p) {
     std::vector<int> g;
     for (int c = 0; c < nc; ++c)
@@ -706,6 +712,7 @@ static void fill_common(oc_op *op, StageArgs &a) {
   a.sdbe = op->d_sde[4];
   a.sdo0 = op->d_sdo[0]; a.sdo1 = op->d_sdo[1]; a.sdo2 = op->d_sdo[2];
   a.cfrec = op->d_cfrec;
+  a.cfofs = op->d_cfofs;
   a.n_bnd_faces = op->n_bnd; a.fofs = op->d_fofs;
   a.fout = op->d_fout; a.fnrmf = op->d_fnrmf; a.flenf = op->d_flenf;
   a.geof = op->prm.precision == OC_PREC_MIXED ? op->d_geof : nullptr;
@@ -757,9 +764,12 @@ static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
   for (int p = 1; p <= OC_MAXDEG; ++p)
     if (op->group_n[p] && (cells_per_warp(p) / batch) * batch == 0)
       return fail(op, OC_ERR_UNSUPPORTED, "batch_width larger than the cells of a warp");
-  // face pass of the stage: every face's flux once, both sides' values
-  OC_TRY(launch_face_pass(a, variant, op->uniform_deg, op->stream));
-  op->launches++;
+  // face pass of the FP64 stage: every face's flux once, both sides' values (the
+  // mixed stage kernels evaluate their faces themselves)
+  if (variant == 0) {
+    OC_TRY(launch_face_pass(a, variant, op->uniform_deg, op->stream));
+    op->launches++;
+  }
   if (op->use_hp && variant != 2 && n_groups(op) > 1) {
     const int wpb = op->hp_wpb;
     int b0 = 0;

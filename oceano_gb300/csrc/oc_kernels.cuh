@@ -306,6 +306,19 @@ __device__ __forceinline__ void face_flux_dev_wb(const RefState<R> &rf, R g, R c
   Pp0 = -sm * n0; Pp1 = -sm * n1;
 }
 
+// face_flux_dev_wb kept out of line where it is called inside the fused face loop
+// of the mixed stage kernel (bathymetry only): the common flat-bathymetry loop
+// keeps its small instruction footprint
+template <typename R>
+__device__ __noinline__ void face_flux_dev_wb_call(const RefState<R> &rf, R g, R cu4, double zref,
+                                                   R zm, R dqm0, R dqm1, R zp, R dqp0, R dqp1,
+                                                   R n0, R n1, double zbm, double zbp, R zbme,
+                                                   R zbpe, R &F, R &Fa0, R &Fa1, R &Pm0,
+                                                   R &Pm1, R &Pp0, R &Pp1) {
+  face_flux_dev_wb<R>(rf, g, cu4, zref, zm, dqm0, dqm1, zp, dqp0, dqp1, n0, n1, zbm, zbp, zbme,
+                      zbpe, F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1);
+}
+
 // Icbc_ShallowWaterVortex.h:139-226 (regularity p=2), FP64
 __host__ __device__ inline double vortex_H(double x) {
   const double cosx = cos(x), cos2x = cos(2. * x), sin2x = sin(2. * x), sinx = sin(x);
@@ -433,7 +446,8 @@ struct Dims {
   static constexpr int norm_offset() { return d_offset<R>() + CPW * bytes_d_smem<R>(); }
   template <typename R>
   static constexpr int int_offset() { return norm_offset<R>() + CPW * 8; }
-  static constexpr int INTS = 2 + 16 + 8 + 1;  // cell, offset, 8 slot records, 8 sdo, flag
+  static constexpr int INTS = 2 + 16 + 8 + 1 + 8;  // cell, offset, 8 slot records, 8 sdo, flag,
+                                                   // 8 face-pass offsets
   template <typename R>
   static constexpr int warp_bytes() { return ((int_offset<R>() + CPW * INTS * 4 + 15) / 16) * 16; }
 };
@@ -782,6 +796,11 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   // the mixed time-step path (FP32 registers) forms internal stage inputs in FP32
   constexpr bool fast = MIX && sizeof(KT) == 4;
+  // FP64 form: faces from the stage's face pass (each face once, oc_face.cu);
+  // mixed form: faces evaluated here by both neighbours, which costs fewer
+  // instructions than a separate pass in FP32 (where FP64's 1/64 rate does not
+  // make the flux the bottleneck)
+  constexpr bool FPASS = !MIX;
   const double zref = MIX ? a.zeta_ref : 0.0;
   const R g = MIX ? (R)a.gf : (R)a.g, cu4 = MIX ? (R)a.cu4f : (R)a.cu4;
   const R zbe_flat = MIX ? (R)a.zreff : R(0);  // zb + zeta_ref where no bathymetry is given
@@ -793,7 +812,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   auto Rreg = [&](int j) { return reinterpret_cast<R *>(wbase + j * D::template bytes_r<R>()); };
   int *ints = reinterpret_cast<int *>(wbase + D::template int_offset<R>());
   int *w_cell = ints, *w_off = ints + CPWMAX, *w_rec = ints + 2 * CPWMAX,
-      *w_sdo = ints + 18 * CPWMAX, *w_flag = ints + 26 * CPWMAX;
+      *w_sdo = ints + 18 * CPWMAX, *w_flag = ints + 26 * CPWMAX, *w_fo = ints + 27 * CPWMAX;
   double *warp_norm = reinterpret_cast<double *>(wbase + D::template norm_offset<R>());
   R *U = Rreg(team);          // 3*NN stage input z, q0, q1
   R *RES = U + 3 * NN;        // 3*NN residual; later the discharge result
@@ -845,6 +864,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   if (a.cfsdo)
     for (int e = lane; e < nvalid * 8; e += 32)
       w_sdo[e] = a.cfsdo[8 * (int64_t)w_cell[e >> 3] + (e & 7)];
+  if (FPASS)
+    for (int e = lane; e < nvalid * 8; e += 32)
+      w_fo[e] = __ldg(a.cfofs + 8 * (int64_t)w_cell[e >> 3] + (e & 7));
   // Everything above reads only the mesh (written before the stream's first stage
   // launch); from here on the kernel reads the previous launch's results and
   // writes buffers it may still read, so it waits for that launch to complete.
@@ -855,17 +877,18 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   // into the scratch tiles ([slot][var][FVS]; free until the cell integrals) while
   // the stage input below is loaded: one memory round trip for both
   const FaceRec *recs = reinterpret_cast<const FaceRec *>(w_rec + 16 * team);
-  if (member) {
+  if (FPASS && member) {
     const R *fout = static_cast<const R *>(a.fout);
 #pragma unroll
     for (int sl = 0; sl < 8; ++sl) {
       const FaceRec r = recs[sl];
       const int kind = r.kind();
       const int nfo = kind == 1 ? r.nf() : kind == 2 ? Q : 0;
+      const int64_t fo = w_fo[8 * team + sl];
       for (int k = t; k < nfo; k += T)
 #pragma unroll
         for (int v = 0; v < 3; ++v)
-          cp_async(X + (sl * 3 + v) * FVS + k, fout + (int64_t)r.other + v * nfo + k);
+          cp_async(X + (sl * 3 + v) * FVS + k, fout + fo + v * nfo + k);
     }
   }
   R fR[OC_MAXSTAGES];  // coefficients in the compute type (mixed form: the FP32 copies)
@@ -934,15 +957,15 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   // or the subface rows on the coarse side of a hanging face), Gauss rows on
   // boundary faces.
   // integration column of node t on a full face of this degree, in registers
-  R fcol[G];
+  R pcol[G];
   {
     const int tt = t < N ? t : 0;
 #pragma unroll
-    for (int k = 0; k < G; ++k) fcol[k] = tb.F[0][G][k][tt];
+    for (int k = 0; k < G; ++k) pcol[k] = tb.F[0][G][k][tt];
   }
-  const DegTables<R> *gt = reinterpret_cast<const DegTables<R> *>(
+  const DegTables<R> *pgt = reinterpret_cast<const DegTables<R> *>(
       sizeof(R) == 4 ? (const void *)a.gtabf : (const void *)a.gtabd);
-  const DegTables<R> &tbg = gt[P - 1];
+  const DegTables<R> &ptb = pgt[P - 1];
   // the values of all slots were copied into the scratch tiles by the prologue
   R *FVA = X;
   if (member && t < N) {
@@ -952,6 +975,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       for (int ix = 0; ix < N; ++ix) RES[e * NN + t * N + ix] = R(0);
   }
   __syncwarp();
+  if constexpr (FPASS) {
 #pragma unroll 1
   for (int sl = 0; sl < 8; ++sl) {
     const FaceRec r = recs[sl];
@@ -980,12 +1004,12 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       if (reg_cols) {
 #pragma unroll
         for (int k = 0; k < G; ++k) {
-          cz += fcol[k] * FV[k];
-          c0 += fcol[k] * FV[FVS + k];
-          c1 += fcol[k] * FV[2 * FVS + k];
+          cz += pcol[k] * FV[k];
+          c0 += pcol[k] * FV[FVS + k];
+          c1 += pcol[k] * FV[2 * FVS + k];
         }
       } else {
-        const R *col = tsel < 0 ? &tbg.BQ[0][t] : &tbg.F[tsel][nfo][0][t];  // stride OC_MAXN
+        const R *col = tsel < 0 ? &ptb.BQ[0][t] : &ptb.F[tsel][nfo][0][t];  // stride OC_MAXN
 #pragma unroll
         for (int k = 0; k < (Q > OC_MAXF ? Q : OC_MAXF); ++k) {  // nfo <= max(Q, OC_MAXF)
           if (k < nfo) {
@@ -1002,6 +1026,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       RES[2 * NN + d] += c1;
     }
     __syncwarp();
+  }
   }
 
   // ---- 2. cell integrals: local_apply_cell_height (OceanDG.h:669-693),
@@ -1217,6 +1242,267 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       }
     }
     __syncwarp();
+  }
+
+  if constexpr (!FPASS) {
+  R *NB = X;                      // neighbour traces [slot][var][node]
+  R *FV = X + 8 * 3 * OC_MAXN;    // 3*FVS face point values
+  // ---- 3. faces of the mixed form, in this kernel: local_apply_face_* (OceanDG.h:936-1050)
+  //         and local_apply_boundary_face_* (:1105-1339); each face evaluated
+  //         identically by both neighbours, own side kept ------------------------
+  // 2a. neighbour traces of every inner slot: [slot][var][node], in the scratch
+  // tiles (free between the cell integrals and the zeta solve); a smaller team
+  // region leaves more of the SM's shared memory / L1 to the L1 cache
+  if (member) {
+#pragma unroll
+    for (int ii = 0; ii < (8 * OC_MAXN + T - 1) / T; ++ii) {
+      const int e = t + ii * T;
+      if (e >= 8 * OC_MAXN) break;
+      const int sl = e / OC_MAXN, i = e - sl * OC_MAXN;
+      const FaceRec r = recs[sl];
+      const int Nn = r.nb_deg() + 1;
+      if (r.kind() == 1 && i < Nn) {
+        const int d = face_dof(Nn, r.nb_face(), i);
+        const int64_t oz = r.other, oq = 2 * (int64_t)r.other;
+        NB[(sl * 3 + 0) * OC_MAXN + i] = load_in<RIN, R>(a.rz, oz + d, zref);
+        NB[(sl * 3 + 1) * OC_MAXN + i] = load_in<RIN, R>(a.rq, oq + d, qref0);
+        NB[(sl * 3 + 2) * OC_MAXN + i] = load_in<RIN, R>(a.rq, oq + Nn * Nn + d, qref1);
+      }
+    }
+  }
+  __syncwarp();
+  // own outward normals and face lengths of the affine cell
+  const R J00 = gR[2], J01 = gR[3], J10 = gR[4], J11 = gR[5];
+  // Conforming faces between cells of this degree (the common case): the trace
+  // row of point k = t (both sides: no subface, standard orientation) and the
+  // integration column of node t, held in registers so that the face loop reads
+  // no lane-dependent constant-bank address.
+  R frow[N], fcol[G], fw;
+  {
+    const int kk = t < G ? t : 0, tt = t < N ? t : 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) frow[i] = tb.F[0][G][kk][i];
+#pragma unroll
+    for (int k = 0; k < G; ++k) fcol[k] = tb.F[0][G][k][tt];
+    fw = tb.wF[G][kk];
+  }
+  // lane-dependent table entries of the hanging / degree-jump face paths come
+  // from the global copy (L1), where divergent addresses cost a few wavefronts
+  // instead of one constant-bank replay per distinct address
+  const DegTables<R> *gt = reinterpret_cast<const DegTables<R> *>(
+      sizeof(R) == 4 ? (const void *)a.gtabf : (const void *)a.gtabd);
+  const DegTables<R> &tbg = gt[P - 1];
+#pragma unroll 1
+  for (int sl = 0; sl < 8; ++sl) {
+    const FaceRec r = recs[sl];
+    const int kind = member ? r.kind() : 0;
+    // second slots of conforming faces are empty in every team of most warps
+    if (!__any_sync(OC_FULL, kind != 0)) continue;
+    // Warp-uniform choice of the inner-face path: the register-row path when every
+    // inner face of the warp in this slot joins two cells of this degree in standard
+    // orientation, else the table path for all of them (one path per warp: on hp
+    // meshes the teams of a warp meet different neighbour degrees, and two paths
+    // would run one after the other)
+    const bool reg_path = __all_sync(OC_FULL, kind != 1 || (r.nb_deg() == P && r.orient() == 0));
+    const int fo = r.own_face();
+    // DoF of node i on face fo: fbase + i * fstride (face_dof)
+    const int fbase = fo == 0 ? 0 : fo == 1 ? N - 1 : fo == 2 ? 0 : (N - 1) * N;
+    const int fstride = fo < 2 ? N : 1;
+    int nfo = 0, tsel = 0;
+    if (kind != 0) {
+      // outward normal of the own face: J^-T n_ref / |.|; tangent length |J t_ref|
+      const R nr0 = fo == 0 ? R(-1) : fo == 1 ? R(1) : R(0);
+      const R nr1 = fo == 2 ? R(-1) : fo == 3 ? R(1) : R(0);
+      R on0 = Ji00 * nr0 + Ji10 * nr1, on1 = Ji01 * nr0 + Ji11 * nr1;
+      const R inv = R(1) / m_sqrt(on0 * on0 + on1 * on1);
+      on0 *= inv; on1 *= inv;
+      const R tx = fo < 2 ? J01 : J00, ty = fo < 2 ? J11 : J10;
+      R len = m_sqrt(tx * tx + ty * ty);
+      if (kind == 1) {
+        const int side = r.side(), sub = r.sub(), orient = r.orient(), nf = r.nf();
+        const int pn = r.nb_deg(), Nn = pn + 1;
+        const DegTables<R> &tn = gt[pn - 1];
+        if (side == 1 && sub >= 0) len *= R(0.5);  // coarse side: the fine half-face
+        const R n0 = side ? -on0 : on0, n1 = side ? -on1 : on1;  // minus normal
+        const int sdo = a.cfsdo ? w_sdo[8 * team + sl] : 0;
+        nfo = nf;
+        tsel = side ? sub + 1 : 0;
+        if (reg_path) {  // same degree: nf == G <= T, point k on both sides
+          if (t < G) {
+            const int k = t;
+            // trace rows: full face from registers; the coarse side of a hanging
+            // face (own on the plus side, the neighbour's on the minus side) reads
+            // the subface rows
+            const int nsel = side ? 0 : sub + 1;
+            R lo[N], ln[N];
+            if (tsel == 0) {
+#pragma unroll
+              for (int i = 0; i < N; ++i) lo[i] = frow[i];
+            } else {
+#pragma unroll
+              for (int i = 0; i < N; ++i) lo[i] = __ldg(&tbg.F[tsel][G][k][i]);
+            }
+            if (nsel == 0) {
+#pragma unroll
+              for (int i = 0; i < N; ++i) ln[i] = frow[i];
+            } else {
+#pragma unroll
+              for (int i = 0; i < N; ++i) ln[i] = __ldg(&tbg.F[nsel][G][k][i]);
+            }
+            R zo_ = 0, qo0 = 0, qo1 = 0, zn = 0, qn0 = 0, qn1 = 0;
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+              const int d = fbase + i * fstride;
+              zo_ += lo[i] * U[d];
+              qo0 += lo[i] * U[NN + d];
+              qo1 += lo[i] * U[2 * NN + d];
+              zn += ln[i] * NB[(sl * 3 + 0) * OC_MAXN + i];
+              qn0 += ln[i] * NB[(sl * 3 + 1) * OC_MAXN + i];
+              qn1 += ln[i] * NB[(sl * 3 + 2) * OC_MAXN + i];
+            }
+            const R zm = side ? zn : zo_, qm0 = side ? qn0 : qo0, qm1 = side ? qn1 : qo1;
+            const R zp = side ? zo_ : zn, qp0 = side ? qo0 : qn0, qp1 = side ? qo1 : qn1;
+            R zbm = MIX ? zbe_flat : R(0), zbp = zbm;
+            if (!MIX && a.sdf) {
+              zbm = (R)a.sdf[sdo + 2 * k]; zbp = (R)a.sdf[sdo + 2 * k + 1];
+            }
+            R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
+            if constexpr (MIX) {
+              if (a.sdf)  // bathymetry: well-balanced differences in FP64
+                face_flux_dev_wb_call<R>(rf, g, cu4, zref, zm, qm0, qm1, zp, qp0, qp1, n0, n1,
+                                    a.sdf[sdo + 2 * k], a.sdf[sdo + 2 * k + 1],
+                                    a.sdfe[sdo + 2 * k], a.sdfe[sdo + 2 * k + 1], F, Fa0, Fa1,
+                                    Pm0, Pm1, Pp0, Pp1);
+              else
+                face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F,
+                                 Fa0, Fa1, Pm0, Pm1, Pp0, Pp1, true);
+            } else
+              face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1,
+                           Pm0, Pm1, Pp0, Pp1);
+            const R jxw = fw * len;
+            const R sg = side ? R(1) : R(-1);
+            FV[k] = sg * F * jxw;
+            FV[FVS + k] = sg * (Fa0 + (side ? Pp0 : Pm0)) * jxw;
+            FV[2 * FVS + k] = sg * (Fa1 + (side ? Pp1 : Pm1)) * jxw;
+          }
+        } else
+        for (int k = t; k < nf; k += T) {
+          const int kp = orient ? nf - 1 - k : k;  // point index on the plus side
+          const int ko = side ? kp : k, kn = side ? k : kp;
+          R zo_ = 0, qo0 = 0, qo1 = 0, zn = 0, qn0 = 0, qn1 = 0;
+#pragma unroll
+          for (int i = 0; i < N; ++i) {  // own trace
+            const int d = face_dof(N, fo, i);
+            const R l = __ldg(&tbg.F[tsel][nf][ko][i]);
+            zo_ += l * U[d];
+            qo0 += l * U[NN + d];
+            qo1 += l * U[2 * NN + d];
+          }
+          const int nsel = side ? 0 : sub + 1;
+#pragma unroll
+          for (int i = 0; i < OC_MAXN; ++i) {  // neighbour trace (Nn <= OC_MAXN nodes)
+            if (i < Nn) {
+              const R l = __ldg(&tn.F[nsel][nf][kn][i]);
+              zn += l * NB[(sl * 3 + 0) * OC_MAXN + i];
+              qn0 += l * NB[(sl * 3 + 1) * OC_MAXN + i];
+              qn1 += l * NB[(sl * 3 + 2) * OC_MAXN + i];
+            }
+          }
+          const R zm = side ? zn : zo_, qm0 = side ? qn0 : qo0, qm1 = side ? qn1 : qo1;
+          const R zp = side ? zo_ : zn, qp0 = side ? qo0 : qn0, qp1 = side ? qo1 : qn1;
+          R zbm = MIX ? zbe_flat : R(0), zbp = zbm;
+          if (!MIX && a.sdf) {
+            zbm = (R)a.sdf[sdo + 2 * k]; zbp = (R)a.sdf[sdo + 2 * k + 1];
+          }
+          R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
+          if constexpr (MIX) {
+            if (a.sdf)  // bathymetry: well-balanced differences in FP64
+              face_flux_dev_wb_call<R>(rf, g, cu4, zref, zm, qm0, qm1, zp, qp0, qp1, n0, n1,
+                                  a.sdf[sdo + 2 * k], a.sdf[sdo + 2 * k + 1],
+                                  a.sdfe[sdo + 2 * k], a.sdfe[sdo + 2 * k + 1], F, Fa0, Fa1, Pm0,
+                                  Pm1, Pp0, Pp1);
+            else
+              face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0,
+                               Fa1, Pm0, Pm1, Pp0, Pp1, true);
+          } else
+            face_flux<R>(g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0, Fa1, Pm0,
+                         Pm1, Pp0, Pp1);
+          const R jxw = __ldg(&tbg.wF[nf][k]) * len;
+          if (side == 0) {
+            FV[ko] = -F * jxw;
+            FV[FVS + ko] = (-Fa0 - Pm0) * jxw;
+            FV[2 * FVS + ko] = (-Fa1 - Pm1) * jxw;
+          } else {
+            FV[ko] = F * jxw;
+            FV[FVS + ko] = (Fa0 + Pp0) * jxw;
+            FV[2 * FVS + ko] = (Fa1 + Pp1) * jxw;
+          }
+        }
+      } else {  // boundary face
+        const int b = r.other;
+        const int bid = r.bid();
+        const int bkind = a.bc_kind[bid];
+        if (bkind == 0 && t == 0) atomicOr(a.err, ERR_UNKNOWN_BID);
+        const int sdo = a.cfsdo ? w_sdo[8 * team + sl] : 0;
+        const R n0 = on0, n1 = on1;
+        nfo = Q;
+        tsel = -1;
+        (void)b;
+        if (t < Q) {
+          const int k = t;
+          R zm = 0, qm0 = 0, qm1 = 0;
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            const int d = face_dof(N, fo, i);
+            const R l = tb.BQ[k][i];
+            zm += l * U[d];
+            qm0 += l * U[NN + d];
+            qm1 += l * U[2 * NN + d];
+          }
+          R F, Fa0, Fa1;
+          boundary_flux<R, MIX>(a, bid, bkind, fo, tab<double>(P).xQ[k], geo, zref, sdo + k, g, cu4,
+                                zm, qm0, qm1, n0, n1, F, Fa0, Fa1);
+          const R jxw = tb.wQ[k] * len;
+          FV[k] = -F * jxw;
+          FV[FVS + k] = -Fa0 * jxw;
+          FV[2 * FVS + k] = -Fa1 * jxw;
+        }
+      }
+    }
+    __syncwarp();
+    // integration rows: registers when every face of the warp in this slot is a full
+    // face of this degree's point set, else the global table copy (boundary faces:
+    // Gauss rows; inner faces: the trace rows of the own side)
+    const bool reg_cols = __all_sync(OC_FULL, nfo == 0 || (tsel == 0 && nfo == G));
+    if (nfo > 0 && t < N) {  // integrate the own-side values against the own basis
+      R cz = 0, c0 = 0, c1 = 0;
+      if (reg_cols) {
+#pragma unroll
+        for (int k = 0; k < G; ++k) {
+          cz += fcol[k] * FV[k];
+          c0 += fcol[k] * FV[FVS + k];
+          c1 += fcol[k] * FV[2 * FVS + k];
+        }
+      } else {
+        const R *col = tsel < 0 ? &tbg.BQ[0][t] : &tbg.F[tsel][nfo][0][t];  // stride OC_MAXN
+#pragma unroll
+        for (int k = 0; k < (Q > OC_MAXF ? Q : OC_MAXF); ++k) {  // nfo <= max(Q, OC_MAXF)
+          if (k < nfo) {
+            const R l = __ldg(col + k * OC_MAXN);
+            cz += l * FV[k];
+            c0 += l * FV[FVS + k];
+            c1 += l * FV[2 * FVS + k];
+          }
+        }
+      }
+      const int d = fbase + t * fstride;
+      RES[d] += cz;
+      RES[NN + d] += c0;
+      RES[2 * NN + d] += c1;
+    }
+    __syncwarp();
+  }
+
   }
 
   // ---- apply(): dst = M^-1 L_h(src), exact Gauss p+1 inverse for all variables ----

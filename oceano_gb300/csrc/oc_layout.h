@@ -68,6 +68,7 @@ struct StageArgs {
   const int *slots;            // [n_cells*8]: 2 refs per face number (host bookkeeping)
   const int *cfrec;            // [n_cells*16]: 8 face records (other, packed word)
   const int *cfsdo;            // [n_cells*8]: static face-data offsets, NULL without data
+  const int *cfofs;            // [n_cells*8]: face-pass output offset of each slot side
   const int *fcm, *fcp;        // [n_inner+n_bnd], [n_inner]
   const int *fpack;            // fm | fp<<4 | (sub+1)<<8 | orient<<12 | nf<<16
   const double *fnrm;          // [n_faces*2] minus normal
