@@ -40,8 +40,7 @@ def _sources():
         units.append((os.path.join(CSRC, "oc_stage_hp.cu"), f"oc_stage_hp_v{v}.o",
                       [f"-DOC_HP_VARIANT={v}", "-ftz=true", "-prec-div=false",
                        "-prec-sqrt=false"]))
-    units.append((os.path.join(CSRC, "oc_face.cu"), "oc_face.o",
-                  ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]))
+    units.append((os.path.join(CSRC, "oc_face.cu"), "oc_face.o", []))
     units.append((os.path.join(CSRC, "oc_aux.cu"), "oc_aux.o", []))
     units.append((os.path.join(CSRC, "oc_api.cu"), "oc_api.o", []))
     units.append((os.path.join(CSRC, "oc_noalloc.cu"), "oc_noalloc.o", []))

@@ -44,10 +44,8 @@ cudaError_t upload_tables_hp_v1(const DegTables<double> *, const DegTables<float
 cudaError_t upload_tables_hp_v2(const DegTables<double> *, const DegTables<float> *);
 
 cudaError_t aux_upload_tables(const DegTables<double> *, const DegTables<float> *);
-cudaError_t launch_face_pass(const StageArgs &, int, int, cudaStream_t);
+cudaError_t launch_face_pass(const StageArgs &, int, cudaStream_t);
 cudaError_t face_upload_tables(const DegTables<double> *, const DegTables<float> *);
-cudaError_t launch_unf32(const StageArgs &, const double *, const double *, float *, float *,
-                         cudaStream_t);
 cudaError_t launch_transport_speed(const AuxArgs &, const double *, const double *,
                                    unsigned long long *, double *, cudaStream_t);
 cudaError_t launch_velocity_field(const AuxArgs &, const double *, const double *, double *,
@@ -129,7 +127,6 @@ struct oc_op {
   std::vector<int> fofs;
   int *d_fofs = nullptr;
   void *d_fout = nullptr;
-  float *d_fnrmf = nullptr, *d_flenf = nullptr;
   float *d_geof = nullptr;
   double *d_dscratch = nullptr;  // mixed form: FP64 zeta work area per (warp, team) slot
   DegTables<double> *d_tabd = nullptr;  // table copies in global memory (divergent reads)
@@ -528,11 +525,6 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   OC_TRY(upload(op, &op->d_bbid, op->bbid.data(), op->bbid.size()));
   OC_TRY(upload(op, &op->d_fnrm, op->fnrm.data(), op->fnrm.size()));
   OC_TRY(upload(op, &op->d_flen, op->flen.data(), op->flen.size()));
-  {
-    std::vector<float> nf32(op->fnrm.begin(), op->fnrm.end()), lf32(op->flen.begin(), op->flen.end());
-    OC_TRY(upload(op, &op->d_fnrmf, nf32.data(), nf32.size()));
-    OC_TRY(upload(op, &op->d_flenf, lf32.data(), lf32.size()));
-  }
   OC_TRY(upload(op, &op->d_fofs, op->fofs.data(), op->fofs.size()));
   OC_TRY(alloc(op, &op->d_fout, std::max<size_t>(fo_total, 1) * sizeof(double)));
   for (int k = 0; k < 3; ++k) OC_TRY(upload(op, &op->d_sdo[k], op->sdo[k].data(), nc));
@@ -714,7 +706,7 @@ static void fill_common(oc_op *op, StageArgs &a) {
   a.cfrec = op->d_cfrec;
   a.cfofs = op->d_cfofs;
   a.n_bnd_faces = op->n_bnd; a.fofs = op->d_fofs;
-  a.fout = op->d_fout; a.fnrmf = op->d_fnrmf; a.flenf = op->d_flenf;
+  a.fout = op->d_fout;
   a.geof = op->prm.precision == OC_PREC_MIXED ? op->d_geof : nullptr;
   a.uniform_nn = op->uniform_deg ? (op->uniform_deg + 1) * (op->uniform_deg + 1) : 0;
   a.h_ref = op->ref_h;
@@ -767,7 +759,7 @@ static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
   // face pass of the FP64 stage: every face's flux once, both sides' values (the
   // mixed stage kernels evaluate their faces themselves)
   if (variant == 0) {
-    OC_TRY(launch_face_pass(a, variant, op->uniform_deg, op->stream));
+    OC_TRY(launch_face_pass(a, op->uniform_deg, op->stream));
     op->launches++;
   }
   if (op->use_hp && variant != 2 && n_groups(op) > 1) {
@@ -960,10 +952,7 @@ static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, doub
     const bool last = st == sc.s - 1;
     a.dyn = op->d_dyn + st;
     a.stage = st; a.n_stages = sc.s; a.ark = sc.ark; a.last = last; a.write_kq_last = 0;
-    if (st == 0 && mixed) {
-      // mixed form: the FP32 deviations of u^n (written by unf32 before the stage)
-      a.rz = op->ts_unzf; a.rq = op->ts_unqf; a.r_is_float = 1;
-    } else if (st == 0) {
+    if (st == 0) {
       // a one-stage scheme overwrites u^n in place: its stage input is a copy
       // (neighbour traces must not see outputs of other blocks)
       a.rz = sc.s == 1 ? op->ts_z0 : z; a.rq = sc.s == 1 ? op->ts_q0 : q;
@@ -977,8 +966,9 @@ static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, doub
     a.fast_mixed = mixed ? 1 : 0;
     a.un_zf = (mixed && st > 0) ? op->ts_unzf : nullptr;
     a.un_qf = (mixed && st > 0) ? op->ts_unqf : nullptr;
-    a.out_unzf = nullptr;  // the FP32 copy of u^n comes from unf32
-    a.out_unqf = nullptr;
+    // stage 0 of the mixed step leaves the FP32 deviations of u^n for the later stages
+    a.out_unzf = (mixed && st == 0) ? op->ts_unzf : nullptr;
+    a.out_unqf = (mixed && st == 0) ? op->ts_unqf : nullptr;
     for (int j = 0; j <= sc.s; ++j) a.kz[j] = op->ts_kz[j];
     for (int j = 0; j < 2 * OC_MAXSTAGES; ++j) a.kq[j] = op->ts_kq[j];
     if (last) {  // u^{n+1} in place, or into (oz, oq) when given
@@ -999,12 +989,7 @@ static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, doub
 static oc_status enqueue_step(oc_op *op, const Scheme &sc, double *z, double *q,
                               double *oz = nullptr, double *oq = nullptr) {
   const bool mixed = op->prm.precision == OC_PREC_MIXED;
-  if (mixed) {  // FP32 deviations of u^n: stage 0's input and the later stages' u^n
-    StageArgs a0;
-    step_stage_args(op, sc, 0, z, q, a0, oz, oq);
-    OC_TRY(launch_unf32(a0, z, q, op->ts_unzf, op->ts_unqf, op->stream));
-    op->launches++;
-  } else if (sc.s == 1) {
+  if (sc.s == 1) {
     const size_t nz = op->n_dofs;
     OC_TRY(cudaMemcpyAsync(op->ts_z0, z, nz * 8, cudaMemcpyDeviceToDevice, op->stream));
     OC_TRY(cudaMemcpyAsync(op->ts_q0, q, 2 * nz * 8, cudaMemcpyDeviceToDevice, op->stream));
@@ -1063,11 +1048,6 @@ static oc_status autotune(oc_op *op, const Scheme &sc, const double *z, const do
     ce = cudaMemcpyAsync(op->ts_z0, z, nz * 8, cudaMemcpyDeviceToDevice, op->stream);
   if (ce == cudaSuccess && sc.s == 1)
     ce = cudaMemcpyAsync(op->ts_q0, q, nq * 8, cudaMemcpyDeviceToDevice, op->stream);
-  if (ce == cudaSuccess && op->prm.precision == OC_PREC_MIXED) {  // stage 0 input of the mixed step
-    StageArgs a0;
-    step_stage_args(op, sc, 0, tz, tq, a0);
-    ce = launch_unf32(a0, tz, tq, op->ts_unzf, op->ts_unqf, op->stream);
-  }
   if (ce != cudaSuccess) st = fail(op, OC_ERR_CUDA, cudaGetErrorString(ce));
   const int64_t launches = op->launches;
   const int reps = 5;

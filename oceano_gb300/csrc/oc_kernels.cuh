@@ -10,8 +10,10 @@
 //      node rows, y-passes on point columns, contractions in registers with
 //      constant-bank shape coefficients),
 //   3. integrates the face contributions of its four faces (conforming, either
-//      side of a hanging face, periodic, boundary), which the stage's face
-//      pass (oc_face.cu) evaluated once per face and left per side,
+//      side of a hanging face, periodic, boundary): the FP64 form integrates
+//      the values the stage's face pass (oc_face.cu) evaluated once per face
+//      and left per side; the mixed form evaluates each face point itself
+//      from the neighbour's trace, the flux of an inner face once per side,
 //   4. forms the zeta right-hand side and runs the wet/dry lumped-mass
 //      iteration (FP64: literally, with the batch stop rule; mixed form:
 //      the closed form of the same sweeps on fully wet cells, the literal
@@ -54,6 +56,19 @@ __device__ __forceinline__ float m_log(float x) { return logf(x); }
 __device__ __forceinline__ double m_log(double x) { return log(x); }
 __device__ __forceinline__ float m_fma(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double m_fma(double a, double b, double c) { return fma(a, b, c); }
+// two independent fused multiply-adds, x += a0 b0 and y += a1 b1: one packed
+// FFMA2 instruction in FP32 (sm_100 and later), two DFMAs in FP64; each lane's
+// result is the scalar fma's
+__device__ __forceinline__ void fma2(float &x, float &y, float a0, float b0, float a1, float b1) {
+  const float2 r = __ffma2_rn(make_float2(a0, a1), make_float2(b0, b1), make_float2(x, y));
+  x = r.x;
+  y = r.y;
+}
+__device__ __forceinline__ void fma2(double &x, double &y, double a0, double b0, double a1,
+                                     double b1) {
+  x = fma(a0, b0, x);
+  y = fma(a1, b1, y);
+}
 
 template <typename R>
 __device__ __forceinline__ R mx(R a, R b) { return a < b ? b : a; }  // std::max
@@ -418,11 +433,19 @@ struct Dims {
   static constexpr int NN = N * N, NT = N * T;
   static constexpr int CPW = 32 / T;
   // scratch tiles of the sum factorisation, the zeta solve and the discharge
-  // inverse; between the cell integrals and the zeta solve they hold the face
-  // pass's point values of the cell's 8 face slots ([slot][var][FVS])
-  static constexpr int XS = 6 * NT > 8 * 3 * FVS ? 6 * NT : 8 * 3 * FVS;
+  // inverse.  Between the cell integrals and the zeta solve they hold the face
+  // data: in the mixed form (FP32 compute type) the neighbour traces of the 8
+  // face slots ([slot][var][OC_MAXN]) and one face's point values (3 FVS); in
+  // the FP64 form the face pass's point values of the 8 slots ([slot][var][FVS]).
+  // A smaller team region leaves more of the SM's shared memory to the L1 cache.
+  template <typename R>
+  static constexpr int xs() {
+    constexpr int f = sizeof(R) == 4 ? 8 * 3 * OC_MAXN + 3 * FVS : 8 * 3 * FVS;
+    return 6 * NT > f ? 6 * NT : f;
+  }
   // per-cell shared memory: compute-type region and FP64 region (elements)
-  static constexpr int SZR = 10 * NN + XS;  // U 3, RES 3, RST 2, BZ 1, ZN 1; X
+  template <typename R>
+  static constexpr int szr() { return 10 * NN + xs<R>(); }  // U 3, RES 3, RST 2, BZ 1, ZN 1; X
   static constexpr int SZD = NN + 3 * NT + T + 2;
   // Team strides: padded so that the 32/T teams of a warp start on different
   // shared-memory banks (stride mod 32 chosen per degree and element size to
@@ -431,7 +454,7 @@ struct Dims {
   static constexpr int pad_d = P == 1 ? 5 : P == 2 ? 2 : P == 3 ? 3 : 4;
   template <typename R>
   static constexpr int bytes_r() {
-    return (((SZR + 7) / 8) * 8 + (sizeof(R) == 4 ? pad_f : pad_d)) * (int)sizeof(R);
+    return (((szr<R>() + 7) / 8) * 8 + (sizeof(R) == 4 ? pad_f : pad_d)) * (int)sizeof(R);
   }
   static constexpr int bytes_d() { return (((SZD + 31) / 32) * 32 + pad_d) * 8; }
   static_assert(SZD <= OC_DSTRIDE, "FP64 zeta work area exceeds its global stride");
@@ -757,8 +780,9 @@ __device__ __forceinline__ void report_nonfinite(const StageArgs &a, bool bad) {
 //   MIX = false: FP64 plain form (R = KT = double).
 //   MIX = true : mixed form; R = float bulk, KT = type of the k registers.
 // Memory flow: warp-cooperative prologue (stage input, face records, partial
-// zeta right-hand side), team-local cell integrals, the face pass's point values
-// of the cell's face sides, team-local zeta and discharge solves,
+// zeta right-hand side), team-local face contributions (FP64: the face pass's
+// point values of the cell's face sides; mixed: after the cell integrals, from
+// the neighbour traces), team-local cell integrals, zeta and discharge solves,
 // warp-cooperative epilogue (RK update and stores).  Global accesses of the
 // prologue/epilogue are lane-contiguous over the warp's cells.
 // ---------------------------------------------------------------------------
@@ -801,6 +825,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   // instructions than a separate pass in FP32 (where FP64's 1/64 rate does not
   // make the flux the bottleneck)
   constexpr bool FPASS = !MIX;
+  static_assert(MIX == (sizeof(R) == 4), "the scratch layout assumes FP32 exactly in the mixed form");
   const double zref = MIX ? a.zeta_ref : 0.0;
   const R g = MIX ? (R)a.gf : (R)a.g, cu4 = MIX ? (R)a.cu4f : (R)a.cu4;
   const R zbe_flat = MIX ? (R)a.zreff : R(0);  // zb + zeta_ref where no bathymetry is given
@@ -1044,10 +1069,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       R b0 = 0, d0 = 0, a0 = 0, a1 = 0;
 #pragma unroll
       for (int ix = 0; ix < N; ++ix) {
-        b0 += tb.BQ[qx][ix] * z[ix];
-        d0 += tb.DQ[qx][ix] * z[ix];
-        a0 += tb.BQ[qx][ix] * q0[ix];
-        a1 += tb.BQ[qx][ix] * q1[ix];
+        fma2(b0, a0, tb.BQ[qx][ix], z[ix], tb.BQ[qx][ix], q0[ix]);
+        fma2(d0, a1, tb.DQ[qx][ix], z[ix], tb.BQ[qx][ix], q1[ix]);
       }
       X[0 * NT + t * T + qx] = b0;
       X[1 * NT + t * T + qx] = d0;
@@ -1073,11 +1096,10 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
         for (int iy = 0; iy < N; ++iy) {
           const R xb = X[0 * NT + iy * T + t], xd = X[1 * NT + iy * T + t];
-          z += tb.BQ[qy][iy] * xb;
-          zx += tb.BQ[qy][iy] * xd;
+          const R b = tb.BQ[qy][iy];
+          fma2(z, zx, b, xb, b, xd);
+          fma2(q0, q1, b, X[2 * NT + iy * T + t], b, X[3 * NT + iy * T + t]);
           zy += tb.DQ[qy][iy] * xb;
-          q0 += tb.BQ[qy][iy] * X[2 * NT + iy * T + t];
-          q1 += tb.BQ[qy][iy] * X[3 * NT + iy * T + t];
         }
         const int k = qy * Q + t;
         R zb = MIX ? zbe_flat : R(0), cf = 0, w0 = 0, w1 = 0, fc = 0;
@@ -1123,12 +1145,10 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
         for (int iy = 0; iy < N; ++iy) {
           const R b = tb.BQ[qy][iy], d = tb.DQ[qy][iy];
-          Az[iy] += b * gz0;
-          Cz[iy] += d * gz1;
-          A0[iy] += b * g00;
-          C0[iy] += d * g01 + b * sv0;
-          A1[iy] += b * g10;
-          C1[iy] += d * g11 + b * sv1;
+          fma2(Az[iy], Cz[iy], b, gz0, d, gz1);
+          fma2(A0[iy], A1[iy], b, g00, b, g10);
+          fma2(C0[iy], C1[iy], d, g01, d, g11);
+          fma2(C0[iy], C1[iy], b, sv0, b, sv1);
         }
       }
     }
@@ -1152,9 +1172,10 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
         for (int qx = 0; qx < Q; ++qx) {
           const R b = tb.BQ[qx][ix], d = tb.DQ[qx][ix];
-          rz += d * X[0 * NT + t * T + qx] + b * X[1 * NT + t * T + qx];
-          r0 += d * X[2 * NT + t * T + qx] + b * X[3 * NT + t * T + qx];
-          r1 += d * X[4 * NT + t * T + qx] + b * X[5 * NT + t * T + qx];
+          fma2(r0, r1, d, X[2 * NT + t * T + qx], d, X[4 * NT + t * T + qx]);
+          fma2(r0, r1, b, X[3 * NT + t * T + qx], b, X[5 * NT + t * T + qx]);
+          rz += d * X[0 * NT + t * T + qx];
+          rz += b * X[1 * NT + t * T + qx];
         }
         RES[t * N + ix] += rz;
         RES[NN + t * N + ix] += r0;

@@ -82,7 +82,6 @@ struct StageArgs {
   int n_bnd_faces;
   const int *fofs;
   void *fout;
-  const float *fnrmf, *flenf;  // FP32 copies of fnrm, flen
   // static data (NULL = zero); *e arrays are FP32 copies with zeta_reference folded into zb
   const double *sd0, *sd1, *sd2, *sdf, *sdb;
   const float *sd0e, *sd1e, *sd2e, *sdfe, *sdbe;
