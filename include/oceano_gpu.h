@@ -33,7 +33,8 @@ typedef enum {
   OC_ERR_TIMEOUT = 4,
   OC_ERR_CUDA = 5,
   OC_ERR_UNSUPPORTED = 6,
-  OC_ERR_NOMEM = 7
+  OC_ERR_NOMEM = 7,
+  OC_ERR_BOUNDS = 8 /* bounds-checked build: an index read from a mesh table out of range */
 } oc_status;
 
 /* where the vector pointers of a call live */
@@ -354,6 +355,21 @@ oc_status oc_timer_summary(oc_op *op, char *text, int64_t size);
  * u^{n+1}.  Calls on device vectors (OC_MEM_DEVICE) return without waiting, so
  * their device-side errors surface here (or at the next call on host vectors). */
 oc_status oc_synchronize(oc_op *op);
+
+/* Bounds-checked build.  A library compiled with OC_BOUNDS_CHECK range-checks
+ * every index its kernels read from the mesh tables (cell ids and degrees, DoF
+ * offsets, face records, boundary ids, static-data and face-pass offsets) where
+ * it is loaded; an index out of range is replaced by 0 so that no access leaves
+ * its array, and the next call that reads the device flags (oc_synchronize, or
+ * any call on host vectors) returns OC_ERR_BOUNDS, with the site and the index
+ * of the first failure in oc_last_error.  Without the macro the checks compile
+ * to nothing.  oc_bounds_checked returns 1 in the bounds-checked build, else 0.
+ * oc_bounds_selftest runs one device thread that checks an index outside its
+ * range (no memory is accessed with it) and returns what the flags then report:
+ * OC_ERR_BOUNDS ("bounds check failed: self-test index 5") in the
+ * bounds-checked build, OC_OK otherwise. */
+int32_t oc_bounds_checked(void);
+oc_status oc_bounds_selftest(oc_op *op);
 /* the stream the handle launches on */
 void *oc_stream(oc_op *op);
 /* kernels launched by this handle since creation (launch accounting) */

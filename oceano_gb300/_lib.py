@@ -11,9 +11,12 @@ import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboceano_gpu.so")
+# bounds-checked variant (oceano_gb300.build.build(bounds_check=True)), loaded
+# instead when the environment sets OCEANO_BOUNDS_CHECK=1
+LIB_CHECKED_PATH = os.path.join(HERE, "liboceano_gpu_checked.so")
 
 OC_OK, OC_ERR_INVALID_ARG, OC_ERR_UNKNOWN_BOUNDARY_ID, OC_ERR_NONFINITE, OC_ERR_TIMEOUT, \
-    OC_ERR_CUDA, OC_ERR_UNSUPPORTED, OC_ERR_NOMEM = range(8)
+    OC_ERR_CUDA, OC_ERR_UNSUPPORTED, OC_ERR_NOMEM, OC_ERR_BOUNDS = range(9)
 OC_MEM_HOST, OC_MEM_DEVICE = 0, 1
 OC_PREC_FP64, OC_PREC_MIXED = 0, 1
 BC_KIND = {"none": 0, "wall": 1, "supercritical_inflow": 2, "supercritical_outflow": 3,
@@ -102,15 +105,23 @@ EXPORTS = {
     "oc_synchronize": (C.c_int, [C.c_void_p]),
     "oc_stream": (C.c_void_p, [C.c_void_p]),
     "oc_launch_count": (C.c_int64, [C.c_void_p]),
+    "oc_bounds_checked": (C.c_int32, []),
+    "oc_bounds_selftest": (C.c_int, [C.c_void_p]),
 }
 
 _lib = None
 
 
-def lib(path: str = LIB_PATH):
+def default_path() -> str:
+    """The bounds-checked library when OCEANO_BOUNDS_CHECK=1, else the regular one."""
+    return LIB_CHECKED_PATH if os.environ.get("OCEANO_BOUNDS_CHECK") == "1" else LIB_PATH
+
+
+def lib(path: str | None = None):
     """Load the library (raises if it is absent: there is no fallback path)."""
     global _lib
     if _lib is None:
+        path = path or default_path()
         if not os.path.exists(path):
             raise RuntimeError(f"{path} is missing: run oceano_gb300.build.build() first")
         L = C.CDLL(path)

@@ -15,6 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liboceano_gpu.so")
+LIB_CHECKED = os.path.join(HERE, "liboceano_gpu_checked.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -55,14 +56,20 @@ def _newest_source() -> float:
     return max(os.path.getmtime(f) for f in files)
 
 
-def build(force: bool = False, verbose: bool = False, extra=()) -> str:
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _newest_source():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, extra=(), bounds_check: bool = False) -> str:
+    """Compile the library; bounds_check=True builds the bounds-checked variant
+    (OC_BOUNDS_CHECK: every index read from a mesh table range-checked into the
+    device error word) as liboceano_gpu_checked.so, in its own build folder."""
+    lib, build_dir = (LIB_CHECKED, BUILD + "_checked") if bounds_check else (LIB, BUILD)
+    if bounds_check:
+        extra = [*extra, "-DOC_BOUNDS_CHECK"]
+    if not force and os.path.exists(lib) and os.path.getmtime(lib) >= _newest_source():
+        return lib
+    os.makedirs(build_dir, exist_ok=True)
     nvcc = _nvcc()
     jobs = []
     for src, obj, defs in _sources():
-        cmd = [nvcc, *ARCH, *FLAGS, *defs, *extra, "-c", src, "-o", os.path.join(BUILD, obj)]
+        cmd = [nvcc, *ARCH, *FLAGS, *defs, *extra, "-c", src, "-o", os.path.join(build_dir, obj)]
         jobs.append(cmd)
 
     def run(cmd):
@@ -76,14 +83,15 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
                 print(r.stdout[-4000:], r.stderr[-8000:])
             if r.returncode:
                 raise RuntimeError(f"nvcc failed: {cmd[-3]}")
-    objs = [os.path.join(BUILD, o) for _, o, _ in _sources()]
-    tmp = LIB + ".tmp"
+    objs = [os.path.join(build_dir, o) for _, o, _ in _sources()]
+    tmp = lib + ".tmp"
     subprocess.check_call([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
     import sys
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv,
-                extra=["-Xptxas", "-v"] if "--ptxas" in sys.argv else []))
+                extra=["-Xptxas", "-v"] if "--ptxas" in sys.argv else [],
+                bounds_check="--bounds-check" in sys.argv))

@@ -43,6 +43,7 @@ cudaError_t upload_tables_hp_v0(const DegTables<double> *, const DegTables<float
 cudaError_t upload_tables_hp_v1(const DegTables<double> *, const DegTables<float> *);
 cudaError_t upload_tables_hp_v2(const DegTables<double> *, const DegTables<float> *);
 
+cudaError_t launch_bounds_selftest(int *, cudaStream_t);
 cudaError_t aux_upload_tables(const DegTables<double> *, const DegTables<float> *);
 cudaError_t launch_face_pass(const StageArgs &, int, cudaStream_t);
 cudaError_t face_upload_tables(const DegTables<double> *, const DegTables<float> *);
@@ -127,6 +128,7 @@ struct oc_op {
   std::vector<int> fofs;
   int *d_fofs = nullptr;
   void *d_fout = nullptr;
+  int64_t n_fout = 0;  // elements of the face-pass output
   float *d_geof = nullptr;
   double *d_dscratch = nullptr;  // mixed form: FP64 zeta work area per (warp, team) slot
   DegTables<double> *d_tabd = nullptr;  // table copies in global memory (divergent reads)
@@ -526,6 +528,7 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   OC_TRY(upload(op, &op->d_fnrm, op->fnrm.data(), op->fnrm.size()));
   OC_TRY(upload(op, &op->d_flen, op->flen.data(), op->flen.size()));
   OC_TRY(upload(op, &op->d_fofs, op->fofs.data(), op->fofs.size()));
+  op->n_fout = fo_total;
   OC_TRY(alloc(op, &op->d_fout, std::max<size_t>(fo_total, 1) * sizeof(double)));
   for (int k = 0; k < 3; ++k) OC_TRY(upload(op, &op->d_sdo[k], op->sdo[k].data(), nc));
   OC_TRY(upload(op, &op->d_cfrec, op->cfrec.data(), op->cfrec.size()));
@@ -570,7 +573,7 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   OC_TRY(upload_tables_hp_v2(td.data(), tf.data()));
   OC_TRY(aux_upload_tables(td.data(), tf.data()));
   OC_TRY(face_upload_tables(td.data(), tf.data()));
-  OC_TRY(alloc(op, (void **)&op->d_err, sizeof(int)));
+  OC_TRY(alloc(op, (void **)&op->d_err, kErrWords * sizeof(int)));
   OC_TRY(alloc(op, (void **)&op->d_speed, sizeof(unsigned long long)));
   OC_TRY(alloc(op, (void **)&op->d_dyn, sizeof(StageDyn) * (OC_MAXSTAGES + 1)));
   op->h_dyn = new StageDyn[OC_MAXSTAGES + 1];
@@ -581,7 +584,7 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   OC_TRY(configure_stage_hp_v0());
   OC_TRY(configure_stage_hp_v1());
   OC_TRY(configure_stage_hp_v2());
-  OC_TRY(cudaMemset(op->d_err, 0, sizeof(int)));
+  OC_TRY(cudaMemset(op->d_err, 0, kErrWords * sizeof(int)));
   OC_TRY(cudaDeviceSynchronize());
   *out = op;
   return OC_OK;
@@ -707,6 +710,8 @@ static void fill_common(oc_op *op, StageArgs &a) {
   a.cfofs = op->d_cfofs;
   a.n_bnd_faces = op->n_bnd; a.fofs = op->d_fofs;
   a.fout = op->d_fout;
+  a.n_dofs = op->n_dofs; a.n_fout = op->n_fout;
+  for (int k = 0; k < 5; ++k) a.n_sd[k] = op->sd_size[k];
   a.geof = op->prm.precision == OC_PREC_MIXED ? op->d_geof : nullptr;
   a.uniform_nn = op->uniform_deg ? (op->uniform_deg + 1) * (op->uniform_deg + 1) : 0;
   a.h_ref = op->ref_h;
@@ -795,14 +800,19 @@ static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
 }
 
 static oc_status read_error(oc_op *op) {
-  int e = 0;
-  OC_TRY(cudaMemcpyAsync(&e, op->d_err, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
+  int e[kErrWords] = {0, 0, 0, 0};
+  OC_TRY(cudaMemcpyAsync(e, op->d_err, sizeof(e), cudaMemcpyDeviceToHost, op->stream));
   OC_TRY(cudaStreamSynchronize(op->stream));
-  if (e) {
-    OC_TRY(cudaMemset(op->d_err, 0, sizeof(int)));
-    if (e & (1 << 2)) return fail(op, OC_ERR_UNKNOWN_BOUNDARY_ID, "unknown boundary id in a kernel");
-    if (e & (1 << 3)) return fail(op, OC_ERR_NONFINITE, "non-finite value detected");
-    return fail(op, OC_ERR_CUDA, "device error flag " + std::to_string(e));
+  if (e[0]) {
+    OC_TRY(cudaMemset(op->d_err, 0, sizeof(e)));
+    if (e[0] & ERR_BOUNDS) {  // bounds-checked build: site and index of the first failure
+      const int64_t idx = (int64_t)(((uint64_t)(uint32_t)e[3] << 32) | (uint32_t)e[2]);
+      return fail(op, OC_ERR_BOUNDS, std::string("bounds check failed: ") + bounds_site_name(e[1]) +
+                                         " index " + std::to_string(idx));
+    }
+    if (e[0] & ERR_UNKNOWN_BID) return fail(op, OC_ERR_UNKNOWN_BOUNDARY_ID, "unknown boundary id in a kernel");
+    if (e[0] & ERR_NONFINITE) return fail(op, OC_ERR_NONFINITE, "non-finite value detected");
+    return fail(op, OC_ERR_CUDA, "device error flag " + std::to_string(e[0]));
   }
   return OC_OK;
 }
@@ -1200,8 +1210,25 @@ static AuxArgs aux_args(oc_op *op) {
   const double cu = op->prm.threshold_wetdry;
   a.g = op->prm.g; a.cu4 = cu * cu * cu * cu;
   for (int k = 0; k < 8; ++k) a.vortex[k] = op->vortex[k];
+  a.n_dofs = op->n_dofs;
+  for (int k = 0; k < 5; ++k) a.n_sd[k] = op->sd_size[k];
   a.err = op->d_err;
   return a;
+}
+
+extern "C" int32_t oc_bounds_checked(void) {
+#ifdef OC_BOUNDS_CHECK
+  return 1;
+#else
+  return 0;
+#endif
+}
+
+extern "C" oc_status oc_bounds_selftest(oc_op *op) {
+  if (!op) return OC_ERR_INVALID_ARG;
+  OC_TRY(launch_bounds_selftest(op->d_err, op->stream));
+  op->launches++;
+  return read_error(op);
 }
 
 extern "C" oc_status oc_transport_speed(oc_op *op, const double *z, const double *q,

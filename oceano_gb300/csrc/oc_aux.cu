@@ -50,10 +50,10 @@ __global__ void transport_speed_kernel(const AuxArgs a, const double *z, const d
   double local = 0;
   bool nonfinite = false;
   if (c < a.n_cells) {
-    const int p = a.deg[c], N = p + 1, G = p + 2, n = N * N;
+    const int p = checked_degree(a.err, a.deg[c]), N = p + 1, G = p + 2, n = N * N;
     const DegTables<double> &tb = tab<double>(p);
     const double *J = a.geo + 11 * (int64_t)c;
-    const int64_t zo = a.off[c];
+    const int64_t zo = checked(a.err, a.off[c], a.n_dofs - n + 1, BS_OFFSET);
     double u[OC_MAXN * OC_MAXN], zv[OC_MAXF * OC_MAXF], q0[OC_MAXF * OC_MAXF],
         q1[OC_MAXF * OC_MAXF];
     for (int i = 0; i < n; ++i) u[i] = z[zo + i];
@@ -62,7 +62,7 @@ __global__ void transport_speed_kernel(const AuxArgs a, const double *z, const d
     eval_tile(N, G, tb.BG, u, q0);
     for (int i = 0; i < n; ++i) u[i] = q[2 * zo + n + i];
     eval_tile(N, G, tb.BG, u, q1);
-    const double *zb1 = a.sd1 ? a.sd1 + a.sdo1[c] : nullptr;
+    const double *zb1 = a.sd1 ? a.sd1 + cell_data(a.err, a.sdo1, c, a.n_sd[1], G * G) : nullptr;
     for (int k = 0; k < G * G; ++k) {
       const double zb = zb1 ? zb1[k] : 0.;
       double v0, v1;
@@ -107,12 +107,12 @@ __global__ void velocity_field_kernel(const AuxArgs a, const double *z, const do
                                       double *u) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.n_cells) return;
-  const int p = a.deg[c], N = p + 1, n = N * N;
+  const int p = checked_degree(a.err, a.deg[c]), N = p + 1, n = N * N;
   const DegTables<double> &tb = tab<double>(p);
-  const int64_t zo = a.off[c];
+  const int64_t zo = checked(a.err, a.off[c], a.n_dofs - n + 1, BS_OFFSET);
   const double *zc = z + zo, *q0c = q + 2 * zo, *q1c = q + 2 * zo + n;
   double *u0 = u + 2 * zo, *u1 = u + 2 * zo + n;
-  const double *sd = a.sd2 ? a.sd2 + a.sdo2[c] : nullptr;
+  const double *sd = a.sd2 ? a.sd2 + cell_data(a.err, a.sdo2, c, a.n_sd[2], 2 * n) : nullptr;
   for (int i = 0; i < 2 * n; ++i) u0[i] = 0.;
   for (int qy = 0; qy < N; ++qy)
     for (int qx = 0; qx < N; ++qx) {
@@ -141,10 +141,10 @@ __global__ void vorticity_kernel(const AuxArgs a, const double *u, int nq, const
                                  const double *Dm, float *out) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.n_cells) return;
-  const int p = a.deg[c], N = p + 1, n = N * N;
+  const int p = checked_degree(a.err, a.deg[c]), N = p + 1, n = N * N;
   const double *Bp = B + (p - 1) * 8 * OC_MAXN, *Dp = Dm + (p - 1) * 8 * OC_MAXN;
   const double *J = a.geo + 11 * (int64_t)c;
-  const double *uc = u + 2 * (int64_t)a.off[c];
+  const double *uc = u + 2 * checked(a.err, a.off[c], a.n_dofs - n + 1, BS_OFFSET);
   float mv = 0.f;
   for (int qy = 0; qy < nq; ++qy)
     for (int qx = 0; qx < nq; ++qx) {
@@ -173,11 +173,11 @@ __global__ void vorticity_kernel(const AuxArgs a, const double *u, int nq, const
 __global__ void project_vortex_kernel(const AuxArgs a, double time, double *z, double *q) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.n_cells) return;
-  const int p = a.deg[c], N = p + 1, n = N * N;
+  const int p = checked_degree(a.err, a.deg[c]), N = p + 1, n = N * N;
   const DegTables<double> &tb = tab<double>(p);
   const double *J = a.geo + 11 * (int64_t)c;
-  const double *sd = a.sd2 ? a.sd2 + a.sdo2[c] : nullptr;
-  const int64_t zo = a.off[c];
+  const double *sd = a.sd2 ? a.sd2 + cell_data(a.err, a.sdo2, c, a.n_sd[2], 2 * n) : nullptr;
+  const int64_t zo = checked(a.err, a.off[c], a.n_dofs - n + 1, BS_OFFSET);
   const VortexParams vp = vortex_params(a.vortex);
   double *zc = z + zo, *q0 = q + 2 * zo, *q1 = q + 2 * zo + n;
   for (int i = 0; i < n; ++i) zc[i] = 0.;
@@ -225,12 +225,12 @@ __global__ void errors_kernel(const AuxArgs a, double time, const double *sd0, c
                               const double *z, const double *q, double *part) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.n_cells) return;
-  const int p = a.deg[c], N = p + 1, n = N * N, Q = (3 * p) / 2 + 1;
+  const int p = checked_degree(a.err, a.deg[c]), N = p + 1, n = N * N, Q = (3 * p) / 2 + 1;
   const DegTables<double> &tb = tab<double>(p);
   const double *J = a.geo + 11 * (int64_t)c;
-  const int64_t zo = a.off[c];
+  const int64_t zo = checked(a.err, a.off[c], a.n_dofs - n + 1, BS_OFFSET);
   const double *zc = z + zo, *q0 = q + 2 * zo, *q1 = q + 2 * zo + n;
-  const double *sd = sd0 ? sd0 + sdo0[c] : nullptr;
+  const double *sd = sd0 ? sd0 + cell_data(a.err, sdo0, c, a.n_sd[0], 5 * Q * Q) : nullptr;
   const VortexParams vp = vortex_params(a.vortex);
   double e0 = 0., e1 = 0.;
   for (int qy = 0; qy < Q; ++qy)
@@ -288,11 +288,11 @@ __global__ void conservative_coarsening_kernel(const AuxArgs a, const unsigned c
                                                double *z) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.n_cells || !mark[c]) return;
-  const int p = a.deg[c], N = p + 1, n = N * N, G = p + 2;
+  const int p = checked_degree(a.err, a.deg[c]), N = p + 1, n = N * N, G = p + 2;
   const DegTables<double> &tb = tab<double>(p);
   const double det = a.geo[11 * (int64_t)c + 10];
-  double *zc = z + a.off[c];
-  const double *sd = a.sd1 ? a.sd1 + a.sdo1[c] : nullptr;
+  double *zc = z + checked(a.err, a.off[c], a.n_dofs - n + 1, BS_OFFSET);
+  const double *sd = a.sd1 ? a.sd1 + cell_data(a.err, a.sdo1, c, a.n_sd[1], G * G) : nullptr;
   double area = 0., integral = 0.;
   for (int gy = 0; gy < G; ++gy)
     for (int gx = 0; gx < G; ++gx) {
@@ -309,6 +309,14 @@ __global__ void conservative_coarsening_kernel(const AuxArgs a, const unsigned c
     const double v = integral * (1. / area);
     for (int i = 0; i < n; ++i) zc[i] = v;
   }
+}
+
+// one thread: an index outside its range through the bounds check (no access)
+__global__ void bounds_selftest_kernel(int *err) { checked(err, 5, 3, BS_SELFTEST); }
+
+cudaError_t launch_bounds_selftest(int *err, cudaStream_t st) {
+  bounds_selftest_kernel<<<1, 1, 0, st>>>(err);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_errors(const AuxArgs &a, double time, const double *sd0, const int *sdo0,
@@ -340,7 +348,7 @@ __global__ void features_kernel(const AuxArgs a, const double *z, const double *
                                 float *feat, float *flags, float *wn) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.n_cells) return;
-  const int p = a.deg[c], N = p + 1, n = N * N;
+  const int p = checked_degree(a.err, a.deg[c]), N = p + 1, n = N * N;
   const DegTables<double> &tb = tab<double>(p);
   // integral weights of the nodal basis on [0,1] (Gauss p+1 is exact for them)
   double mw[OC_MAXN];
@@ -349,7 +357,7 @@ __global__ void features_kernel(const AuxArgs a, const double *z, const double *
     for (int k = 0; k < N; ++k) s += tb.wM[k] * tb.BM[k][i];
     mw[i] = s;
   }
-  const int64_t zo = a.off[c];
+  const int64_t zo = checked(a.err, a.off[c], a.n_dofs - n + 1, BS_OFFSET);
   double zm = 0, q0 = 0, q1 = 0;
   for (int iy = 0; iy < N; ++iy)
     for (int ix = 0; ix < N; ++ix) {

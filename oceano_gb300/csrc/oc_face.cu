@@ -53,11 +53,28 @@ __global__ void __launch_bounds__(128) face_kernel(const StageArgs a) {
   }
   // mesh data only before the wait (written before the stream's first stage)
   const int fpk = __ldg(a.fpack + f);
-  const int cm = __ldg(a.fcm + f);
-  const int pm = P ? P : __ldg(a.deg + cm), Nm = pm + 1;
-  const int64_t om = a.uniform_nn ? (int64_t)cm * a.uniform_nn : (int64_t)__ldg(a.off + cm);
-  R *out = static_cast<R *>(a.fout) + __ldg(a.fofs + f);
-  const int fsd = __ldg(a.fsd + f);
+  const int cm = (int)checked(a.err, __ldg(a.fcm + f), a.n_cells, BS_FACE_CELL);
+  const int pm = P ? P : checked_degree(a.err, __ldg(a.deg + cm)), Nm = pm + 1;
+  const int64_t om = checked(
+      a.err, a.uniform_nn ? (int64_t)cm * a.uniform_nn : (int64_t)__ldg(a.off + cm),
+      a.n_dofs - Nm * Nm + 1, BS_OFFSET);
+  const bool inner = f < a.n_inner;
+  const int nf = P ? P + 2 : (fpk >> 16) & 15;  // points of an inner face
+  const int Qm = (3 * pm) / 2 + 1;              // points of a boundary face
+#ifdef OC_BOUNDS_CHECK
+  if (inner && (nf < 2 || nf > OC_MAXF || ((fpk >> 8) & 15) > 2)) {  // pack word: nf, subface
+    checked(a.err, fpk, 0, BS_RECORD);
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+    return;
+  }
+#endif
+  const int64_t fo =
+      checked(a.err, __ldg(a.fofs + f), a.n_fout - (inner ? 6 * nf : 3 * Qm) + 1, BS_FACE_OUT);
+  R *out = static_cast<R *>(a.fout) + fo;
+  int fsd = __ldg(a.fsd + f);
+  if (inner ? a.sdf != nullptr : a.sdb != nullptr)
+    fsd = (int)checked(a.err, fsd, inner ? a.n_sd[3] - 2 * nf + 1 : a.n_sd[4] - Qm + 1,
+                       BS_FACE_DATA);
   const R n0 = __ldg(a.fnrm + 2 * f), n1 = __ldg(a.fnrm + 2 * f + 1), len = __ldg(a.flen + f);
   const DegTables<R> *gt = reinterpret_cast<const DegTables<R> *>(a.gtabd);
   const R g = a.g, cu4 = a.cu4;
@@ -77,12 +94,13 @@ __global__ void __launch_bounds__(128) face_kernel(const StageArgs a) {
       qm1n[n] = __ldg(rq + 2 * om + Nm * Nm + d);
     }
   }
-  if (f < a.n_inner) {
+  if (inner) {
     const int fp = (fpk >> 4) & 15, sub = ((fpk >> 8) & 15) - 1, orient = (fpk >> 12) & 15;
-    const int nf = P ? P + 2 : (fpk >> 16) & 15;
-    const int cp = __ldg(a.fcp + f);
-    const int pp = P ? P : __ldg(a.deg + cp), Np = pp + 1;
-    const int64_t op = a.uniform_nn ? (int64_t)cp * a.uniform_nn : (int64_t)__ldg(a.off + cp);
+    const int cp = (int)checked(a.err, __ldg(a.fcp + f), a.n_cells, BS_FACE_CELL);
+    const int pp = P ? P : checked_degree(a.err, __ldg(a.deg + cp)), Np = pp + 1;
+    const int64_t op = checked(
+        a.err, a.uniform_nn ? (int64_t)cp * a.uniform_nn : (int64_t)__ldg(a.off + cp),
+        a.n_dofs - Np * Np + 1, BS_OFFSET);
     R zpn[NMAX], qp0n[NMAX], qp1n[NMAX];
 #pragma unroll
     for (int n = 0; n < NMAX; ++n) {
@@ -136,13 +154,13 @@ __global__ void __launch_bounds__(128) face_kernel(const StageArgs a) {
     }
   } else {  // boundary face: Gauss n_q points of the cell
     const int b = f - a.n_inner;
-    const int bid = __ldg(a.bbid + b);
+    const int bid = (int)checked(a.err, __ldg(a.bbid + b), OC_MAXBID, BS_BOUNDARY);
     const int bkind = a.bc_kind[bid];
     if (bkind == 0) {
       atomicOr(a.err, ERR_UNKNOWN_BID);
       return;
     }
-    const int Q = (3 * pm) / 2 + 1;
+    const int Q = Qm;
     const DegTables<R> &tm = gt[pm - 1];
     const DegTables<double> &td = reinterpret_cast<const DegTables<double> *>(a.gtabd)[pm - 1];
     const double *geo = a.geo + 11 * (int64_t)cm;

@@ -39,7 +39,48 @@ __device__ __forceinline__ const DegTables<double> &tab<double>(int p) { return 
 template <>
 __device__ __forceinline__ const DegTables<float> &tab<float>(int p) { return c_tabf[p - 1]; }
 
-enum { ERR_UNKNOWN_BID = 1 << 2, ERR_NONFINITE = 1 << 3 };
+// ---------------------------------------------------------------------------
+// Bounds-checked build (OC_BOUNDS_CHECK).  Every index a kernel reads from a
+// mesh table -- cell ids, degrees, DoF offsets, face records, static-data and
+// face-pass offsets -- is range-checked where it is loaded.  An index outside
+// its range sets ERR_BOUNDS, records the site and the index in err[1..3] (the
+// first failure only) and is replaced by 0, so that the accesses it feeds stay
+// in bounds; the host then reports OC_ERR_BOUNDS with the site and the index.
+// Without the macro the checks compile to nothing.
+// ---------------------------------------------------------------------------
+#ifdef OC_BOUNDS_CHECK
+static __device__ __noinline__ void bounds_fail(int *err, int site, int64_t i) {
+  atomicOr(err, ERR_BOUNDS);
+  if (atomicCAS(err + 1, 0, site) == 0) {
+    err[2] = (int)(uint32_t)(uint64_t)i;
+    err[3] = (int)(uint32_t)((uint64_t)i >> 32);
+  }
+}
+#endif
+// index i, valid in [0, n); an offset followed by `extent` elements of an
+// array of `size` elements is checked with n = size - extent + 1
+__device__ __forceinline__ int64_t checked(int *err, int64_t i, int64_t n, int site) {
+#ifdef OC_BOUNDS_CHECK
+  if (i < 0 || i >= n) {
+    bounds_fail(err, site, i);
+    return 0;
+  }
+#else
+  (void)err; (void)n; (void)site;
+#endif
+  return i;
+}
+// degree p of a cell, valid in [1, OC_MAXDEG] (replaced by 1)
+__device__ __forceinline__ int checked_degree(int *err, int p) {
+  return 1 + (int)checked(err, p - 1, OC_MAXDEG, BS_DEGREE);
+}
+
+// offset of a cell's block of `extent` static-data values (sd0: 5 Q^2, sd1:
+// (p+2)^2, sd2: 2 (p+1)^2) in an array of n elements
+__device__ __forceinline__ int64_t cell_data(int *err, const int *sdo, int cell, int64_t n,
+                                             int extent) {
+  return checked(err, __ldg(sdo + cell), n - extent + 1, BS_CELL_DATA);
+}
 // boundary kinds (values of OC_BC_* in oceano_gpu.h)
 enum { OC_BC_WALL_ = 1, OC_BC_SUPIN_ = 2, OC_BC_SUPOUT_ = 3, OC_BC_HEIGHT_ = 4,
        OC_BC_DISCHARGE_ = 5, OC_BC_ABSORB_ = 6 };
@@ -575,7 +616,7 @@ __device__ void zeta_iteration_fp64(const StageArgs &a, int cell, double *DZ, do
   const DegTables<double> &tb = tab<double>(P);
   const double *geo = a.geo + 11 * (int64_t)cell;
   const double det = geo[10];
-  const double *zb1 = a.sd1 ? a.sd1 + a.sdo1[cell] : nullptr;
+  const double *zb1 = a.sd1 ? a.sd1 + cell_data(a.err, a.sdo1, cell, a.n_sd[1], G * G) : nullptr;
   // epsilon lift (OceanDG.h:1399-1422)
   {
     int ndry = 0;
@@ -754,6 +795,39 @@ struct FaceRec {
   __device__ __forceinline__ int bid() const { return (pk >> 16) & 15; }
 };
 
+#ifdef OC_BOUNDS_CHECK
+// Face record of a slot of a cell of degree p (bounds-checked build): packed
+// fields in range, the neighbour's DoFs or the boundary face, the static face
+// data (sdo) and the face-pass values (fo) of the slot inside their arrays.  A
+// malformed record becomes an empty slot; a bad offset becomes 0.
+static __device__ __noinline__ void check_record(const StageArgs &a, FaceRec &r, int p,
+                                                 int *sdo, int *fo) {
+  const int kind = r.kind();
+  if (kind == 0) return;
+  bool ok = kind <= 2;
+  if (kind == 1)
+    ok = ok && r.nb_deg() >= 1 && r.nb_deg() <= OC_MAXDEG && r.nf() >= 2 && r.nf() <= OC_MAXF &&
+         r.sub() <= 1;
+  if (!ok) {
+    checked(a.err, r.pk, 0, BS_RECORD);
+    r.pk = 0;
+    r.other = 0;
+    return;
+  }
+  const int nfo = kind == 1 ? r.nf() : (3 * p) / 2 + 1;
+  if (kind == 1) {
+    const int nn = (r.nb_deg() + 1) * (r.nb_deg() + 1);
+    r.other = (int)checked(a.err, r.other, a.n_dofs - nn + 1, BS_NEIGHBOUR);
+  } else {
+    r.other = (int)checked(a.err, r.other, a.n_bnd_faces, BS_BOUNDARY);
+  }
+  if (sdo)
+    *sdo = (int)checked(a.err, *sdo, kind == 1 ? a.n_sd[3] - 2 * nfo + 1 : a.n_sd[4] - nfo + 1,
+                        BS_FACE_DATA);
+  if (fo) *fo = (int)checked(a.err, *fo, a.n_fout - 3 * nfo + 1, BS_FACE_OUT);
+}
+#endif
+
 // Stage coefficients in the compute type: the FP32 copies for the FP32 bulk (one
 // 16-byte read-only load, no FP64 conversion), the FP64 values otherwise.
 template <typename R>
@@ -856,9 +930,11 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   if (lane < CPWMAX) {
     const int j = lane;
     const int gi = nvalid > 0 ? gi0 + (j < nvalid ? j : 0) : 0;  // idle warps read cell 0
-    const int c = group_cells ? group_cells[gi] : group_first + gi;
+    const int c = (int)checked(a.err, group_cells ? group_cells[gi] : group_first + gi,
+                               a.n_cells, BS_CELL);
     w_cell[j] = c;
-    w_off[j] = a.uniform_nn ? c * a.uniform_nn : a.off[c];
+    w_off[j] = (int)checked(a.err, a.uniform_nn ? (int64_t)c * a.uniform_nn : a.off[c],
+                            a.n_dofs - NN + 1, BS_OFFSET);
     w_flag[j] = 0;
   }
   __syncwarp();
@@ -892,6 +968,12 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   if (FPASS)
     for (int e = lane; e < nvalid * 8; e += 32)
       w_fo[e] = __ldg(a.cfofs + 8 * (int64_t)w_cell[e >> 3] + (e & 7));
+#ifdef OC_BOUNDS_CHECK
+  __syncwarp();
+  for (int e = lane; e < nvalid * 8; e += 32)
+    check_record(a, reinterpret_cast<FaceRec *>(w_rec)[e], P, a.cfsdo ? w_sdo + e : nullptr,
+                 FPASS ? w_fo + e : nullptr);
+#endif
   // Everything above reads only the mesh (written before the stream's first stage
   // launch); from here on the kernel reads the previous launch's results and
   // writes buffers it may still read, so it waits for that launch to complete.
@@ -1085,8 +1167,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
     for (int i = 0; i < N; ++i) Az[i] = Cz[i] = A0[i] = C0[i] = A1[i] = C1[i] = 0;
     if (member && t < Q) {  // y-pass, pointwise model, y-integration on column qx = t
-      const double *sd0 = a.sd0 ? a.sd0 + a.sdo0[cell] : nullptr;
-      const float *sd0e = a.sd0e ? a.sd0e + a.sdo0[cell] : nullptr;
+      const int64_t so0 = a.sd0 ? cell_data(a.err, a.sdo0, cell, a.n_sd[0], 5 * Q * Q) : 0;
+      const double *sd0 = a.sd0 ? a.sd0 + so0 : nullptr;
+      const float *sd0e = a.sd0e ? a.sd0e + so0 : nullptr;
       // not unrolled: the point loop is the largest block of the kernel, and a
       // smaller instruction footprint leaves fewer warps waiting on instruction
       // fetch (the shape coefficients become uniform constant loads)
@@ -1212,8 +1295,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
     for (int i = 0; i < N; ++i) S0[i] = S1[i] = 0;
     if (member && t < Q) {
-      const double *sd0 = a.sd0 ? a.sd0 + a.sdo0[cell] : nullptr;
-      const float *sd0e = a.sd0e ? a.sd0e + a.sdo0[cell] : nullptr;
+      const int64_t so0 = a.sd0 ? cell_data(a.err, a.sdo0, cell, a.n_sd[0], 5 * Q * Q) : 0;
+      const double *sd0 = a.sd0 ? a.sd0 + so0 : nullptr;
+      const float *sd0e = a.sd0e ? a.sd0e + so0 : nullptr;
 #pragma unroll
       for (int qy = 0; qy < Q; ++qy) {
         R z = 0, q0 = 0, q1 = 0;
@@ -1631,7 +1715,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       }
     }
     __syncwarp();
-    const float *zb1e = a.sd1e ? a.sd1e + a.sdo1[cell] : nullptr;
+    const float *zb1e = a.sd1e ? a.sd1e + cell_data(a.err, a.sdo1, cell, a.n_sd[1], G * G) : nullptr;
     if (exact0 && !sure0 && member && t < G) {
 #pragma unroll
       for (int gy = 0; gy < G; ++gy) {
@@ -1721,7 +1805,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     double rhs[N], dummy[N];
     {
       const double det_d = geo[10];
-      const double *zb1 = a.sd1 ? a.sd1 + a.sdo1[cell] : nullptr;
+      const double *zb1 = a.sd1 ? a.sd1 + cell_data(a.err, a.sdo1, cell, a.n_sd[1], G * G) : nullptr;
       const DegTables<double> &td = tab<double>(P);
       gl_eval_apply_integrate<P>(
           DZ, DX, t, work,
@@ -1863,8 +1947,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
     for (int i = 0; i < N; ++i) m0[i] = m1[i] = 0;
     if (member && t < N) {
-      const double *sd2 = a.sd2 ? a.sd2 + a.sdo2[cell] : nullptr;
-      const float *sd2e = a.sd2e ? a.sd2e + a.sdo2[cell] : nullptr;
+      const int64_t so2 = a.sd2 ? cell_data(a.err, a.sdo2, cell, a.n_sd[2], 2 * NN) : 0;
+      const double *sd2 = a.sd2 ? a.sd2 + so2 : nullptr;
+      const float *sd2e = a.sd2e ? a.sd2e + so2 : nullptr;
 #pragma unroll
       for (int qy = 0; qy < N; ++qy) {
         R vz = 0, v0 = 0, v1 = 0, n0 = 0, n1 = 0;

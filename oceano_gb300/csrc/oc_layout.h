@@ -12,6 +12,32 @@
 #define OC_MAXCPW 10    // cells per warp at p = 1 (the most of any degree)
 #define OC_DSTRIDE 144  // doubles per cell of the FP64 zeta work area, >= N^2 + 3 N T + T + 2
 
+// Device error word (StageArgs::err, AuxArgs::err): err[0] holds flags, err[1]
+// the site of the first failed bounds check of the bounds-checked build
+// (OC_BOUNDS_CHECK) and err[2], err[3] the low and high 32 bits of its index.
+constexpr int kErrWords = 4;
+enum ErrFlag { ERR_UNKNOWN_BID = 1 << 2, ERR_NONFINITE = 1 << 3, ERR_BOUNDS = 1 << 4 };
+enum BoundsSite {
+  BS_SELFTEST = 1,  // oc_bounds_selftest
+  BS_CELL,          // cell id of a degree group
+  BS_DEGREE,        // cell degree
+  BS_OFFSET,        // DoF offset of a cell
+  BS_RECORD,        // packed fields of a face record / face pack word
+  BS_NEIGHBOUR,     // DoF offset of a face neighbour
+  BS_BOUNDARY,      // boundary face index or boundary id
+  BS_FACE_DATA,     // static face-data offset
+  BS_FACE_OUT,      // face-pass output offset
+  BS_CELL_DATA,     // static cell-data offset
+  BS_FACE_CELL      // cell id of a face side
+};
+inline const char *bounds_site_name(int s) {
+  static const char *names[] = {"none", "self-test", "cell id", "cell degree", "cell DoF offset",
+                                "face record", "neighbour DoF offset", "boundary face",
+                                "face static-data offset", "face-pass output offset",
+                                "cell static-data offset", "face cell id"};
+  return s >= 0 && s <= BS_FACE_CELL ? names[s] : "unknown site";
+}
+
 // Per-degree tables; matrices are [point][node] on [0,1].
 template <typename R>
 struct DegTables {
@@ -134,7 +160,11 @@ struct StageArgs {
   // cell c is multiplied by cscale[c] before the Runge-Kutta update
   const float *cscalef;
   const double *cscale;
-  // status word (bit flags of oc_status codes)
+  // extents checked by the bounds-checked build (OC_BOUNDS_CHECK): DoFs per
+  // variable, elements of the face-pass output and of sd0, sd1, sd2, sdf, sdb
+  int64_t n_dofs, n_fout, n_sd[5];
+  // status word: err[0] bit flags of oc_status codes; err[1..3] the site and
+  // the index of the first failed bounds check (bounds-checked build)
   int *err;
 };
 
@@ -148,5 +178,6 @@ struct AuxArgs {
   const int *sdo1, *sdo2;
   double g, cu4;
   double vortex[8];
+  int64_t n_dofs, n_sd[5];  // extents checked by the bounds-checked build
   int *err;
 };

@@ -65,12 +65,12 @@ __global__ void noalloc_speed_partials(const AuxArgs a, const double *z, const d
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   double local = 0;
   if (c < a.n_cells) {
-    const int p = a.deg[c], N = p + 1, G = p + 2;
+    const int p = checked_degree(a.err, a.deg[c]), N = p + 1, G = p + 2;
     const DegTables<double> &tb = tab<double>(p);
     const double *J = a.geo + 11 * (int64_t)c;
-    const int64_t zo = a.off[c];
     const int n = N * N;
-    const double *zb1 = a.sd1 ? a.sd1 + a.sdo1[c] : nullptr;
+    const int64_t zo = checked(a.err, a.off[c], a.n_dofs - n + 1, BS_OFFSET);
+    const double *zb1 = a.sd1 ? a.sd1 + cell_data(a.err, a.sdo1, c, a.n_sd[1], G * G) : nullptr;
     for (int gy = 0; gy < G; ++gy)
       for (int gx = 0; gx < G; ++gx) {
         double zv = 0, q0 = 0, q1 = 0;
