@@ -36,9 +36,9 @@ cudaError_t upload_tables_p4(const DegTables<double> *, const DegTables<float> *
 cudaError_t configure_stage_hp_v0();
 cudaError_t configure_stage_hp_v1();
 cudaError_t configure_stage_hp_v2();
-cudaError_t launch_stage_hp_v0(const StageArgs &, int, int, cudaStream_t);
-cudaError_t launch_stage_hp_v1(const StageArgs &, int, int, cudaStream_t);
-cudaError_t launch_stage_hp_v2(const StageArgs &, int, int, cudaStream_t);
+cudaError_t launch_stage_hp_v0(const StageArgs &, int, int, bool, cudaStream_t);
+cudaError_t launch_stage_hp_v1(const StageArgs &, int, int, bool, cudaStream_t);
+cudaError_t launch_stage_hp_v2(const StageArgs &, int, int, bool, cudaStream_t);
 cudaError_t upload_tables_hp_v0(const DegTables<double> *, const DegTables<float> *);
 cudaError_t upload_tables_hp_v1(const DegTables<double> *, const DegTables<float> *);
 cudaError_t upload_tables_hp_v2(const DegTables<double> *, const DegTables<float> *);
@@ -293,11 +293,12 @@ static cudaError_t launch_stage(int p, const StageArgs &a, int variant, int grid
   }
 }
 
-static cudaError_t launch_stage_hp(int hv, const StageArgs &a, int grid, int wpb, cudaStream_t s) {
+static cudaError_t launch_stage_hp(int hv, const StageArgs &a, int grid, int wpb, bool lean,
+                                   cudaStream_t s) {
   switch (hv) {
-    case 0: return launch_stage_hp_v0(a, grid, wpb, s);
-    case 1: return launch_stage_hp_v1(a, grid, wpb, s);
-    default: return launch_stage_hp_v2(a, grid, wpb, s);
+    case 0: return launch_stage_hp_v0(a, grid, wpb, false, s);
+    case 1: return launch_stage_hp_v1(a, grid, wpb, lean, s);
+    default: return launch_stage_hp_v2(a, grid, wpb, lean, s);
   }
 }
 
@@ -780,7 +781,7 @@ static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
       b0 += a.hp_blocks[p];
     }
     const int hv = variant == 0 ? 0 : (a.r_is_float ? 1 : 2);
-    OC_TRY(launch_stage_hp(hv, a, b0, wpb, op->stream));
+    OC_TRY(launch_stage_hp(hv, a, b0, wpb, variant == 3, op->stream));
     op->launches++;
     return OC_OK;
   }
@@ -995,6 +996,16 @@ static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, doub
   }
 }
 
+// kernel variant of the time-step path: 0 FP64; 1 mixed; 3 the mixed kernel
+// compiled without static data, friction, per-cell time scale and ARK scheme,
+// for workloads that use none of them
+static int step_variant(const oc_op *op, const Scheme &sc) {
+  if (op->prm.precision != OC_PREC_MIXED) return 0;
+  bool lean = !sc.ark && op->prm.friction_model == 0 && !op->d_cscale;
+  for (int k = 0; k < 5; ++k) lean = lean && !op->d_sd[k];
+  return lean ? 3 : 1;
+}
+
 // enqueue the stages of one time step on op->stream (capturable)
 static oc_status enqueue_step(oc_op *op, const Scheme &sc, double *z, double *q,
                               double *oz = nullptr, double *oq = nullptr) {
@@ -1007,7 +1018,7 @@ static oc_status enqueue_step(oc_op *op, const Scheme &sc, double *z, double *q,
   for (int st = 0; st < sc.s; ++st) {
     StageArgs a;
     step_stage_args(op, sc, st, z, q, a, oz, oq);
-    oc_status s = launch_groups(op, a, mixed ? 1 : 0);
+    oc_status s = launch_groups(op, a, step_variant(op, sc));
     if (s != OC_OK) return s;
   }
   return OC_OK;
@@ -1021,14 +1032,15 @@ static oc_status time_stage(oc_op *op, const Scheme &sc, double *z, double *q, i
   StageArgs a0, a1;
   step_stage_args(op, sc, 0, z, q, a0);
   step_stage_args(op, sc, sc.s > 2 ? 1 : 0, z, q, a1);
-  oc_status s = launch_groups(op, a0, mixed ? 1 : 0);
+  const int variant = step_variant(op, sc);
+  oc_status s = launch_groups(op, a0, variant);
   if (s != OC_OK) return s;
   cudaEvent_t e0, e1;
   OC_TRY(cudaEventCreate(&e0));
   OC_TRY(cudaEventCreate(&e1));
-  for (int r = 0; r < 2 && s == OC_OK; ++r) s = launch_groups(op, a1, mixed ? 1 : 0);  // warm-up
+  for (int r = 0; r < 2 && s == OC_OK; ++r) s = launch_groups(op, a1, variant);  // warm-up
   cudaEventRecord(e0, op->stream);
-  for (int r = 0; r < reps && s == OC_OK; ++r) s = launch_groups(op, a1, mixed ? 1 : 0);
+  for (int r = 0; r < reps && s == OC_OK; ++r) s = launch_groups(op, a1, variant);
   cudaEventRecord(e1, op->stream);
   cudaError_t ce = cudaEventSynchronize(e1);
   float t = 0.f;

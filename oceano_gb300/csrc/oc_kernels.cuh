@@ -867,7 +867,7 @@ __device__ __forceinline__ void report_nonfinite(const StageArgs &a, bool bad) {
 // One block of the stage: `blk` is the block index within the degree group of
 // n_group cells (listed by group_cells, or group_first + i when NULL); the FP64
 // work-area slots of the mixed form are indexed by the launch-wide block index.
-template <int P, typename R, typename KT, bool MIX, typename RIN>
+template <int P, typename R, typename KT, bool MIX, typename RIN, bool LEAN>
 __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *smem_raw,
                                            const int blk, const int n_group,
                                            const int *group_cells, const int group_first) {
@@ -899,6 +899,18 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   // instructions than a separate pass in FP32 (where FP64's 1/64 rate does not
   // make the flux the bottleneck)
   constexpr bool FPASS = !MIX;
+  // LEAN: a workload without static data (bathymetry, friction coefficients,
+  // sources), friction model, per-cell time scale or ARK scheme (the host checks
+  // this); the branches of those features are compiled out of the variant
+  const bool ark = !LEAN && a.ark;
+  const int friction_m = LEAN ? 0 : a.friction;
+  const double *sd0_p = LEAN ? nullptr : a.sd0, *sd1_p = LEAN ? nullptr : a.sd1,
+               *sd2_p = LEAN ? nullptr : a.sd2, *sdf_p = LEAN ? nullptr : a.sdf;
+  const float *sd0e_p = LEAN ? nullptr : a.sd0e, *sd1e_p = LEAN ? nullptr : a.sd1e,
+              *sd2e_p = LEAN ? nullptr : a.sd2e, *sdfe_p = LEAN ? nullptr : a.sdfe;
+  const int *cfsdo_p = LEAN ? nullptr : a.cfsdo;
+  const double *cscale_p = LEAN ? nullptr : a.cscale;
+  const float *cscalef_p = LEAN ? nullptr : a.cscalef;
   static_assert(MIX == (sizeof(R) == 4), "the scratch layout assumes FP32 exactly in the mixed form");
   const double zref = MIX ? a.zeta_ref : 0.0;
   const R g = MIX ? (R)a.gf : (R)a.g, cu4 = MIX ? (R)a.cu4f : (R)a.cu4;
@@ -962,16 +974,16 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     const int j = nvalid + (e >> 4);
     w_rec[j * 16 + (e & 15)] = (e & 1) ? 0 : -1;
   }
-  if (a.cfsdo)
+  if (cfsdo_p)
     for (int e = lane; e < nvalid * 8; e += 32)
-      w_sdo[e] = a.cfsdo[8 * (int64_t)w_cell[e >> 3] + (e & 7)];
+      w_sdo[e] = cfsdo_p[8 * (int64_t)w_cell[e >> 3] + (e & 7)];
   if (FPASS)
     for (int e = lane; e < nvalid * 8; e += 32)
       w_fo[e] = __ldg(a.cfofs + 8 * (int64_t)w_cell[e >> 3] + (e & 7));
 #ifdef OC_BOUNDS_CHECK
   __syncwarp();
   for (int e = lane; e < nvalid * 8; e += 32)
-    check_record(a, reinterpret_cast<FaceRec *>(w_rec)[e], P, a.cfsdo ? w_sdo + e : nullptr,
+    check_record(a, reinterpret_cast<FaceRec *>(w_rec)[e], P, cfsdo_p ? w_sdo + e : nullptr,
                  FPASS ? w_fo + e : nullptr);
 #endif
   // Everything above reads only the mesh (written before the stream's first stage
@@ -1020,7 +1032,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     // fast ERK path: the discharge part of the update known before this stage,
     // QB = (last stage ? 0 : q^n) + sum_{j<s} f_j k_q[j+1] (RST region, unused by
     // the explicit stage), loaded with the stage input so that the epilogue loads nothing
-    if (fast && !a.ark && !a.apply_mode) {
+    if (fast && !ark && !a.apply_mode) {
       R qb0 = 0, qb1 = 0;
 #pragma unroll
       for (int jj = 0; jj < OC_MAXSTAGES; ++jj)
@@ -1161,15 +1173,15 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     }
   }
   __syncwarp();
-  const bool split = a.ark && !a.last;  // ARK internal stage: stiff part separate
+  const bool split = ark && !a.last;  // ARK internal stage: stiff part separate
   {
     R Az[N], Cz[N], A0[N], C0[N], A1[N], C1[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) Az[i] = Cz[i] = A0[i] = C0[i] = A1[i] = C1[i] = 0;
     if (member && t < Q) {  // y-pass, pointwise model, y-integration on column qx = t
-      const int64_t so0 = a.sd0 ? cell_data(a.err, a.sdo0, cell, a.n_sd[0], 5 * Q * Q) : 0;
-      const double *sd0 = a.sd0 ? a.sd0 + so0 : nullptr;
-      const float *sd0e = a.sd0e ? a.sd0e + so0 : nullptr;
+      const int64_t so0 = sd0_p ? cell_data(a.err, a.sdo0, cell, a.n_sd[0], 5 * Q * Q) : 0;
+      const double *sd0 = sd0_p ? sd0_p + so0 : nullptr;
+      const float *sd0e = sd0e_p ? sd0e_p + so0 : nullptr;
       // not unrolled: the point loop is the largest block of the kernel, and a
       // smaller instruction footprint leaves fewer warps waiting on instruction
       // fetch (the shape coefficients become uniform constant loads)
@@ -1212,7 +1224,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         }
         const R dz0 = Ji00 * zx + Ji10 * zy, dz1 = Ji01 * zx + Ji11 * zy;
         R fr0 = 0, fr1 = 0;
-        if (a.friction && !split) friction<R>(a.friction, g, v0, v1, cf, h, fr0, fr1);
+        if (friction_m && !split) friction<R>(friction_m, g, v0, v1, cf, h, fr0, fr1);
         // -g h grad(zeta) (ShallowWater.h:405-432); with bathymetry the mixed form
         // forms the depth h = zeta + zb of the source in FP64
         R hs = h;
@@ -1295,9 +1307,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
     for (int i = 0; i < N; ++i) S0[i] = S1[i] = 0;
     if (member && t < Q) {
-      const int64_t so0 = a.sd0 ? cell_data(a.err, a.sdo0, cell, a.n_sd[0], 5 * Q * Q) : 0;
-      const double *sd0 = a.sd0 ? a.sd0 + so0 : nullptr;
-      const float *sd0e = a.sd0e ? a.sd0e + so0 : nullptr;
+      const int64_t so0 = sd0_p ? cell_data(a.err, a.sdo0, cell, a.n_sd[0], 5 * Q * Q) : 0;
+      const double *sd0 = sd0_p ? sd0_p + so0 : nullptr;
+      const float *sd0e = sd0e_p ? sd0e_p + so0 : nullptr;
 #pragma unroll
       for (int qy = 0; qy < Q; ++qy) {
         R z = 0, q0 = 0, q1 = 0;
@@ -1314,7 +1326,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         R v0, v1, fr0 = 0, fr1 = 0;
         if constexpr (MIX) velocity<R>(z, rf.qr0 + q0, rf.qr1 + q1, zb, cu4, v0, v1);
         else velocity<R>(z, q0, q1, zb, cu4, v0, v1);
-        if (a.friction) friction<R>(a.friction, g, v0, v1, cf, depth<R>(z, zb), fr0, fr1);
+        if (friction_m) friction<R>(friction_m, g, v0, v1, cf, depth<R>(z, zb), fr0, fr1);
         const R w = tb.wQ[t] * tb.wQ[qy] * det;
         const R st0 = -fr0 * w, st1 = -fr1 * w;
 #pragma unroll
@@ -1429,7 +1441,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         const DegTables<R> &tn = gt[pn - 1];
         if (side == 1 && sub >= 0) len *= R(0.5);  // coarse side: the fine half-face
         const R n0 = side ? -on0 : on0, n1 = side ? -on1 : on1;  // minus normal
-        const int sdo = a.cfsdo ? w_sdo[8 * team + sl] : 0;
+        const int sdo = cfsdo_p ? w_sdo[8 * team + sl] : 0;
         nfo = nf;
         tsel = side ? sub + 1 : 0;
         if (reg_path) {  // same degree: nf == G <= T, point k on both sides
@@ -1468,15 +1480,15 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
             const R zm = side ? zn : zo_, qm0 = side ? qn0 : qo0, qm1 = side ? qn1 : qo1;
             const R zp = side ? zo_ : zn, qp0 = side ? qo0 : qn0, qp1 = side ? qo1 : qn1;
             R zbm = MIX ? zbe_flat : R(0), zbp = zbm;
-            if (!MIX && a.sdf) {
-              zbm = (R)a.sdf[sdo + 2 * k]; zbp = (R)a.sdf[sdo + 2 * k + 1];
+            if (!MIX && sdf_p) {
+              zbm = (R)sdf_p[sdo + 2 * k]; zbp = (R)sdf_p[sdo + 2 * k + 1];
             }
             R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
             if constexpr (MIX) {
-              if (a.sdf)  // bathymetry: well-balanced differences in FP64
+              if (sdf_p)  // bathymetry: well-balanced differences in FP64
                 face_flux_dev_wb_call<R>(rf, g, cu4, zref, zm, qm0, qm1, zp, qp0, qp1, n0, n1,
-                                    a.sdf[sdo + 2 * k], a.sdf[sdo + 2 * k + 1],
-                                    a.sdfe[sdo + 2 * k], a.sdfe[sdo + 2 * k + 1], F, Fa0, Fa1,
+                                    sdf_p[sdo + 2 * k], sdf_p[sdo + 2 * k + 1],
+                                    sdfe_p[sdo + 2 * k], sdfe_p[sdo + 2 * k + 1], F, Fa0, Fa1,
                                     Pm0, Pm1, Pp0, Pp1);
               else
                 face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F,
@@ -1516,15 +1528,15 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           const R zm = side ? zn : zo_, qm0 = side ? qn0 : qo0, qm1 = side ? qn1 : qo1;
           const R zp = side ? zo_ : zn, qp0 = side ? qo0 : qn0, qp1 = side ? qo1 : qn1;
           R zbm = MIX ? zbe_flat : R(0), zbp = zbm;
-          if (!MIX && a.sdf) {
-            zbm = (R)a.sdf[sdo + 2 * k]; zbp = (R)a.sdf[sdo + 2 * k + 1];
+          if (!MIX && sdf_p) {
+            zbm = (R)sdf_p[sdo + 2 * k]; zbp = (R)sdf_p[sdo + 2 * k + 1];
           }
           R F, Fa0, Fa1, Pm0, Pm1, Pp0, Pp1;
           if constexpr (MIX) {
-            if (a.sdf)  // bathymetry: well-balanced differences in FP64
+            if (sdf_p)  // bathymetry: well-balanced differences in FP64
               face_flux_dev_wb_call<R>(rf, g, cu4, zref, zm, qm0, qm1, zp, qp0, qp1, n0, n1,
-                                  a.sdf[sdo + 2 * k], a.sdf[sdo + 2 * k + 1],
-                                  a.sdfe[sdo + 2 * k], a.sdfe[sdo + 2 * k + 1], F, Fa0, Fa1, Pm0,
+                                  sdf_p[sdo + 2 * k], sdf_p[sdo + 2 * k + 1],
+                                  sdfe_p[sdo + 2 * k], sdfe_p[sdo + 2 * k + 1], F, Fa0, Fa1, Pm0,
                                   Pm1, Pp0, Pp1);
             else
               face_flux_dev<R>(rf, g, cu4, zm, qm0, qm1, zp, qp0, qp1, n0, n1, zbm, zbp, F, Fa0,
@@ -1548,7 +1560,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         const int bid = r.bid();
         const int bkind = a.bc_kind[bid];
         if (bkind == 0 && t == 0) atomicOr(a.err, ERR_UNKNOWN_BID);
-        const int sdo = a.cfsdo ? w_sdo[8 * team + sl] : 0;
+        const int sdo = cfsdo_p ? w_sdo[8 * team + sl] : 0;
         const R n0 = on0, n1 = on1;
         nfo = Q;
         tsel = -1;
@@ -1662,9 +1674,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 
   // independent instances with their own step size (time-step path): the cell's
   // residual scaled by dt_c / dt, so that every later sum f_j k_j carries it
-  if (a.cscale) {
+  if (cscale_p) {
     if (member && t < N) {
-      const R sc = MIX ? (R)__ldg(a.cscalef + cell) : (R)__ldg(a.cscale + cell);
+      const R sc = MIX ? (R)__ldg(cscalef_p + cell) : (R)__ldg(cscale_p + cell);
 #pragma unroll
       for (int e = 0; e < 3; ++e)
 #pragma unroll
@@ -1692,7 +1704,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     // |zeta - zeta_ref| stay below (zb + zeta_ref - threshold) / Lambda (Lambda: the
     // Lebesgue constant of the nodal basis at those points, with a margin for the
     // FP32 evaluation); only warps where that bound fails evaluate the points.
-    const bool flat_zb = a.sd1e == nullptr;
+    const bool flat_zb = sd1e_p == nullptr;
     const R wet_lim = flat_zb ? (zbe_flat - wet_thr) / tb.lebG * R(0.999) : R(0);
     auto bound_wet = [&](const R *vals) {  // team-uniform
       bool ok = flat_zb;
@@ -1715,7 +1727,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       }
     }
     __syncwarp();
-    const float *zb1e = a.sd1e ? a.sd1e + cell_data(a.err, a.sdo1, cell, a.n_sd[1], G * G) : nullptr;
+    const float *zb1e = sd1e_p ? sd1e_p + cell_data(a.err, a.sdo1, cell, a.n_sd[1], G * G) : nullptr;
     if (exact0 && !sure0 && member && t < G) {
 #pragma unroll
       for (int gy = 0; gy < G; ++gy) {
@@ -1805,7 +1817,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     double rhs[N], dummy[N];
     {
       const double det_d = geo[10];
-      const double *zb1 = a.sd1 ? a.sd1 + cell_data(a.err, a.sdo1, cell, a.n_sd[1], G * G) : nullptr;
+      const double *zb1 = sd1_p ? sd1_p + cell_data(a.err, a.sdo1, cell, a.n_sd[1], G * G) : nullptr;
       const DegTables<double> &td = tab<double>(P);
       gl_eval_apply_integrate<P>(
           DZ, DX, t, work,
@@ -1843,7 +1855,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         }
       }
     }
-    if (!a.ark && a.out_q) {
+    if (!ark && a.out_q) {
 #pragma unroll
       for (int i = 0; i < EQ; ++i) {
         const int e = lane + 32 * i;
@@ -1887,7 +1899,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         }
     }
     __syncwarp();
-  } else if (a.ark) {  // ARK last stage: b = f0 kex0 + sum_j (f_j kex_j + f_{j-1} kim_{j-1})
+  } else if (ark) {  // ARK last stage: b = f0 kex0 + sum_j (f_j kex_j + f_{j-1} kim_{j-1})
     if (member && t < N) {
 #pragma unroll
       for (int e = 0; e < 2; ++e)
@@ -1947,9 +1959,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
     for (int i = 0; i < N; ++i) m0[i] = m1[i] = 0;
     if (member && t < N) {
-      const int64_t so2 = a.sd2 ? cell_data(a.err, a.sdo2, cell, a.n_sd[2], 2 * NN) : 0;
-      const double *sd2 = a.sd2 ? a.sd2 + so2 : nullptr;
-      const float *sd2e = a.sd2e ? a.sd2e + so2 : nullptr;
+      const int64_t so2 = sd2_p ? cell_data(a.err, a.sdo2, cell, a.n_sd[2], 2 * NN) : 0;
+      const double *sd2 = sd2_p ? sd2_p + so2 : nullptr;
+      const float *sd2e = sd2e_p ? sd2e_p + so2 : nullptr;
 #pragma unroll
       for (int qy = 0; qy < N; ++qy) {
         R vz = 0, v0 = 0, v1 = 0, n0 = 0, n1 = 0;
@@ -1969,7 +1981,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         R u0, u1;
         if constexpr (MIX) velocity<R>(vz, rf.qr0 + v0, rf.qr1 + v1, zb, cu4, u0, u1);
         else velocity<R>(vz, v0, v1, zb, cu4, u0, u1);
-        const R jf = friction_jac<R>(a.friction, g, u0, u1, cf, depth<R>(vz, zb));
+        const R jf = friction_jac<R>(friction_m, g, u0, u1, cf, depth<R>(vz, zb));
         const R jxw = tb.wM[t] * tb.wM[qy] * det;
         coef[qy] = R(1) / jxw;
         coef[qy] *= R(1) / (R(1) + fmR * jf);
@@ -2118,8 +2130,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       if (MIX && a.out_rz) a.out_rz[gz] = (float)(zn - zref);
     }
   }
-  const bool wkq = !a.ark && (!a.last || a.write_kq_last);
-  if (fast && !a.ark) {
+  const bool wkq = !ark && (!a.last || a.write_kq_last);
+  if (fast && !ark) {
     // delta = sum_j f_j k_q[j+1] in FP32 (kept in smem for the FP64 loop)
 #pragma unroll 2
     for (int e = lane; e < nvalid * 2 * NN; e += 32) {
@@ -2155,7 +2167,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     const int64_t gq = 2 * (int64_t)w_off[j] + d;
     const R v = Rreg(j)[4 * NN + d];  // RES[NN + d] of team j
     double nxt;
-    if (!a.ark) {
+    if (!ark) {
       // ERK: k_q[s+1] = M^-1 L_h q; next = q^n + sum_j f_j k_q[j+1]
       const double kc = (double)(KT)v;
       if (wkq) static_cast<KT *>(a.kq[s + 1])[gq] = (KT)v;
@@ -2200,10 +2212,11 @@ static cudaError_t launch_programmatic(K kernel, int grid, int threads, int smem
 }
 
 // One degree group per launch.
-template <int P, typename R, typename KT, bool MIX, typename RIN>
+template <int P, typename R, typename KT, bool MIX, typename RIN, bool LEAN>
 __global__ void __launch_bounds__(128, MIX ? OC_MIXED_MIN_BLOCKS : 1) stage_kernel(const StageArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_body<P, R, KT, MIX, RIN>(a, smem_raw, blockIdx.x, a.n_group, a.group_cells, a.group_first);
+  stage_body<P, R, KT, MIX, RIN, LEAN>(a, smem_raw, blockIdx.x, a.n_group, a.group_cells,
+                                       a.group_first);
 }
 
 // Every degree group of an hp mesh in one launch: the grid is the concatenation
@@ -2212,14 +2225,14 @@ __global__ void __launch_bounds__(128, MIX ? OC_MIXED_MIN_BLOCKS : 1) stage_kern
 #ifndef OC_HP_MIN_BLOCKS
 #define OC_HP_MIN_BLOCKS 4
 #endif
-template <typename R, typename KT, bool MIX, typename RIN>
+template <typename R, typename KT, bool MIX, typename RIN, bool LEAN>
 __global__ void __launch_bounds__(128, MIX ? OC_HP_MIN_BLOCKS : 1) stage_kernel_hp(const StageArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int b = blockIdx.x;
 #define OC_HP_CASE(P)                                                                          \
   if (b >= a.hp_first_block[P] && b < a.hp_first_block[P] + a.hp_blocks[P]) {                 \
-    stage_body<P, R, KT, MIX, RIN>(a, smem_raw, b - a.hp_first_block[P], a.hp_n[P],           \
-                                   a.hp_cells[P], 0);                                          \
+    stage_body<P, R, KT, MIX, RIN, LEAN>(a, smem_raw, b - a.hp_first_block[P], a.hp_n[P],     \
+                                         a.hp_cells[P], 0);                                    \
     return;                                                                                    \
   }
   OC_HP_CASE(4)

@@ -2,7 +2,8 @@
 // compiled once per kernel variant with -DOC_HP_VARIANT=v so that the variants
 // build in parallel:
 //   0: FP64 form; 1: mixed time step, FP32 stage input; 2: mixed time step,
-//   FP64 stage input (stage 0).
+//   FP64 stage input (stage 0).  The mixed variants also come as a lean kernel
+//   (no static data, friction, per-cell time scale or ARK scheme).
 // Each translation unit owns its copy of the constant-bank shape tables.
 #include "oc_kernels.cuh"
 
@@ -37,15 +38,23 @@ static constexpr int hp_warp_bytes() {
 }
 
 cudaError_t OC_CAT(configure_stage_hp_v, OC_HP_VARIANT)() {
-  return cudaFuncSetAttribute(stage_kernel_hp<HpR, HpKT, kHpMix, HpRIN>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              kMaxWarpsPerBlock * hp_warp_bytes());
+  cudaError_t e = cudaFuncSetAttribute(stage_kernel_hp<HpR, HpKT, kHpMix, HpRIN, false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       kMaxWarpsPerBlock * hp_warp_bytes());
+  if (e == cudaSuccess && kHpMix)
+    e = cudaFuncSetAttribute(stage_kernel_hp<HpR, HpKT, kHpMix, HpRIN, kHpMix>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kMaxWarpsPerBlock * hp_warp_bytes());
+  return e;
 }
 
 cudaError_t OC_CAT(launch_stage_hp_v, OC_HP_VARIANT)(const StageArgs &a, int grid, int wpb,
-                                                     cudaStream_t st) {
+                                                     bool lean, cudaStream_t st) {
   if (wpb > kMaxWarpsPerBlock) return cudaErrorInvalidValue;
-  return launch_programmatic(stage_kernel_hp<HpR, HpKT, kHpMix, HpRIN>, grid, wpb * 32,
+  if (kHpMix && lean)
+    return launch_programmatic(stage_kernel_hp<HpR, HpKT, kHpMix, HpRIN, kHpMix>, grid, wpb * 32,
+                               wpb * hp_warp_bytes(), st, a);
+  return launch_programmatic(stage_kernel_hp<HpR, HpKT, kHpMix, HpRIN, false>, grid, wpb * 32,
                              wpb * hp_warp_bytes(), st, a);
 }
 
