@@ -997,11 +997,11 @@ static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, doub
 }
 
 // kernel variant of the time-step path: 0 FP64; 1 mixed; 3 the mixed kernel
-// compiled without static data, friction, per-cell time scale and ARK scheme,
-// for workloads that use none of them
+// compiled without static data, friction and ARK scheme, for workloads that
+// use none of them
 static int step_variant(const oc_op *op, const Scheme &sc) {
   if (op->prm.precision != OC_PREC_MIXED) return 0;
-  bool lean = !sc.ark && op->prm.friction_model == 0 && !op->d_cscale;
+  bool lean = !sc.ark && op->prm.friction_model == 0;
   for (int k = 0; k < 5; ++k) lean = lean && !op->d_sd[k];
   return lean ? 3 : 1;
 }

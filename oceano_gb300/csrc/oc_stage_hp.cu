@@ -3,7 +3,7 @@
 // build in parallel:
 //   0: FP64 form; 1: mixed time step, FP32 stage input; 2: mixed time step,
 //   FP64 stage input (stage 0).  The mixed variants also come as a lean kernel
-//   (no static data, friction, per-cell time scale or ARK scheme).
+//   (no static data, friction or ARK scheme).
 // Each translation unit owns its copy of the constant-bank shape tables.
 #include "oc_kernels.cuh"
 

@@ -43,8 +43,8 @@ cudaError_t OC_CAT(configure_stage_p, OC_DEGREE)() {
 
 // variant 0: FP64; 1: mixed time step with FP32 registers (FP64 stage input at
 // stage 0, FP32 afterwards); 2: mixed reference-ABI stage (FP64 registers and
-// vectors); 3: variant 1 compiled without static data, friction, per-cell time
-// scale and ARK scheme (the lean kernel of workloads that use none of them)
+// vectors); 3: variant 1 compiled without static data, friction and ARK scheme
+// (the lean kernel of workloads that use none of them)
 cudaError_t OC_CAT(launch_stage_p, OC_DEGREE)(const StageArgs &a, int variant, int grid, int wpb,
                                                cudaStream_t st) {
   switch (variant) {
