@@ -23,6 +23,8 @@ roofline : dominant kernel = the fused stage kernel; algorithmic bytes per step
            names it); a bench run does not run under ncu.
 cpu_baseline / --impl reference: the FP64 C oracle (CPU restatement; the
            reference itself needs deal.II + MPI) with OpenMP on all host cores.
+secondary_quadrature: the same vortex under the config's secondary cell rule
+           (4x4 Gauss points per cell at p = 3), mixed and FP64 timed, error.
 
 Secondary workloads (--workload; same JSON keys, not the headline line):
   hp        the vortex on the seeded random hp mesh (about 60k cells, degrees
@@ -313,6 +315,36 @@ def time_device(op, mesh, z0, q0, steps, warmup, dt, flush, scheme="ssp33"):
     torch.cuda.synchronize()
     ms = [a.elapsed_time(b) for a, b in times]
     return ms, z.cpu().numpy(), q.cpu().numpy(), launches
+
+
+def secondary_quadrature(args, flush):
+    """The same vortex under the config's secondary cell rule: 4x4 Gauss points
+    per cell at p = 3 (n_points_1d = p + 1; the mass rules are fixed in the
+    reference).  Mixed and FP64 steps timed like the main legs (fewer steps), the
+    mixed state's error against the FP64 one under the same rule."""
+    mesh, vx = workload()
+    from oceano_gb300.workloads import vortex_operator
+    op_m = vortex_operator(mesh, "mixed", vx, cell_quadrature="p+1")
+    op_d = vortex_operator(mesh, "fp64", vx, cell_quadrature="p+1")
+    n = op_d.n_dofs
+    z0, q0 = np.zeros(n), np.zeros(2 * n)
+    op_d.project_vortex(0.0, z0, q0)
+    dt = CFL_VORTEX / op_d.compute_cell_transport_speed(z0, q0)
+    steps = max(5, args.steps // 4)
+    ms_m, zm, qm, _ = time_device(op_m, mesh, z0, q0, steps, args.warmup, dt, flush)
+    ms_d, zd, qd, _ = time_device(op_d, mesh, z0, q0, steps, args.warmup, dt, flush)
+    units = 3 * n * 3 * steps
+    out = {"rule": "cell and boundary faces: Gauss p+1 = 4 points per direction at p = 3 "
+                   "(n_points_1d); mass: Gauss-Lobatto 5 (zeta), Gauss 4 (discharge)",
+           "steps": steps,
+           "mixed": {"value": units / (sum(ms_m) / 1e3), "ms_per_step": sum(ms_m) / steps},
+           "fp64": {"value": units / (sum(ms_d) / 1e3), "ms_per_step": sum(ms_d) / steps},
+           "l2_error_vs_fp64": {"zeta": rel(zm, zd), "hu_hv": rel(qm, qd),
+                                "after_steps": args.warmup + steps}}
+    out["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    op_m.close()
+    op_d.close()
+    return out
 
 
 def time_e2e(op, z0, q0, steps, warmup, dt, scheme="ssp33"):
@@ -733,6 +765,8 @@ def main():
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    if vortex and {"mixed", "fp64"} <= legs:
+        out["secondary_quadrature"] = secondary_quadrature(args, flush)
     if rank == 0 and not args.no_cpu:
         v, cores, el = cpu_baseline(wl, args.cpu_steps)
         out["cpu_baseline"] = {"value": v, "unit": "DoF-stage/s", "cores": cores, "kind": "port",

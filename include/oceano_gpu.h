@@ -108,7 +108,17 @@ typedef struct {
   int32_t batch_width;         /* SIMD lanes of a cell batch for the zeta stop rule */
   int32_t precision;           /* OC_PREC_FP64 or OC_PREC_MIXED */
   double zeta_reference;       /* mixed form: FP32 free surface is stored as zeta - this */
+  int32_t cell_quadrature;     /* Gauss points per direction of the cell integrals, boundary
+                                  faces, cell/boundary static data and errors (the reference's
+                                  n_points_1d, main.cc:216): OC_CELL_RULE_DEFAULT or
+                                  OC_CELL_RULE_P1 */
 } oc_params;
+
+/* cell Gauss rules (oc_params.cell_quadrature) */
+enum {
+  OC_CELL_RULE_DEFAULT = 0, /* floor(1.5 p) + 1 points per direction (main.cc:216) */
+  OC_CELL_RULE_P1 = 1       /* p + 1 points per direction (4x4 at p = 3) */
+};
 
 /* Replaces OceanoOperator::OceanoOperator + reinit + initialize_data_at_quadrature
  * (OceanDG.h:387-470, :497-569): uploads geometry and face tables. */

@@ -22,6 +22,7 @@ OC_PREC_FP64, OC_PREC_MIXED = 0, 1
 BC_KIND = {"none": 0, "wall": 1, "supercritical_inflow": 2, "supercritical_outflow": 3,
            "height_inflow": 4, "discharge_inflow": 5, "absorbing_outflow": 6}
 LAUNCH_MODE = {"auto": 0, "per_group": 1, "one": 2}
+CELL_RULE = {"default": 0, "p+1": 1}  # oc_params.cell_quadrature
 SCHEME = {"forward_euler": 0, "ssp22": 1, "ssp33": 2, "rk4": 3, "stage3_order2": 4,
           "ark_stage3_order2": 5}
 
@@ -38,7 +39,8 @@ class Params(C.Structure):
     _fields_ = [("g", C.c_double), ("threshold_wetdry", C.c_double),
                 ("horizontal_viscosity", C.c_double), ("friction_model", C.c_int32),
                 ("max_iteration_height", C.c_int32), ("batch_width", C.c_int32),
-                ("precision", C.c_int32), ("zeta_reference", C.c_double)]
+                ("precision", C.c_int32), ("zeta_reference", C.c_double),
+                ("cell_quadrature", C.c_int32)]
 
 
 class StageVectors(C.Structure):

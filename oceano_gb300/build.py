@@ -32,11 +32,14 @@ def _nvcc() -> str:
 
 def _sources():
     units = []
-    for p in (1, 2, 3, 4):
-        # FP32 bulk of the mixed form: flush-to-zero and approximate division and
-        # square root (affects single precision only; the FP64 form is IEEE)
-        units.append((os.path.join(CSRC, "oc_stage_inst.cu"), f"oc_stage_p{p}.o",
-                      [f"-DOC_DEGREE={p}", "-ftz=true", "-prec-div=false", "-prec-sqrt=false"]))
+    for rule in (0, 1):  # cell Gauss rule: floor(1.5 p) + 1 or p + 1 points per direction
+        for p in (1, 2, 3, 4):
+            # FP32 bulk of the mixed form: flush-to-zero and approximate division and
+            # square root (affects single precision only; the FP64 form is IEEE)
+            units.append((os.path.join(CSRC, "oc_stage_inst.cu"),
+                          f"oc_stage_p{p}" + ("_r1" if rule else "") + ".o",
+                          [f"-DOC_DEGREE={p}", f"-DOC_CELL_RULE={rule}", "-ftz=true",
+                           "-prec-div=false", "-prec-sqrt=false"]))
     for v in (0, 1, 2):
         units.append((os.path.join(CSRC, "oc_stage_hp.cu"), f"oc_stage_hp_v{v}.o",
                       [f"-DOC_HP_VARIANT={v}", "-ftz=true", "-prec-div=false",
@@ -76,7 +79,7 @@ def build(force: bool = False, verbose: bool = False, extra=(), bounds_check: bo
         r = subprocess.run(cmd, capture_output=True, text=True)
         return cmd, r
 
-    with cf.ThreadPoolExecutor(max_workers=min(10, os.cpu_count() or 2)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 2)) as ex:
         for cmd, r in ex.map(run, jobs):
             if verbose or r.returncode:
                 print(" ".join(cmd))

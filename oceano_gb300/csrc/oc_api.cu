@@ -32,6 +32,23 @@ cudaError_t upload_tables_p1(const DegTables<double> *, const DegTables<float> *
 cudaError_t upload_tables_p2(const DegTables<double> *, const DegTables<float> *);
 cudaError_t upload_tables_p3(const DegTables<double> *, const DegTables<float> *);
 cudaError_t upload_tables_p4(const DegTables<double> *, const DegTables<float> *);
+// the same entry points for the cell Gauss rule p + 1 (OC_CELL_RULE_P1)
+cudaError_t launch_stage_p1_r1(const StageArgs &, int, int, int, cudaStream_t);
+cudaError_t configure_stage_p1_r1();
+int stage_cells_per_warp_p1_r1();
+cudaError_t upload_tables_p1_r1(const DegTables<double> *, const DegTables<float> *);
+cudaError_t launch_stage_p2_r1(const StageArgs &, int, int, int, cudaStream_t);
+cudaError_t configure_stage_p2_r1();
+int stage_cells_per_warp_p2_r1();
+cudaError_t upload_tables_p2_r1(const DegTables<double> *, const DegTables<float> *);
+cudaError_t launch_stage_p3_r1(const StageArgs &, int, int, int, cudaStream_t);
+cudaError_t configure_stage_p3_r1();
+int stage_cells_per_warp_p3_r1();
+cudaError_t upload_tables_p3_r1(const DegTables<double> *, const DegTables<float> *);
+cudaError_t launch_stage_p4_r1(const StageArgs &, int, int, int, cudaStream_t);
+cudaError_t configure_stage_p4_r1();
+int stage_cells_per_warp_p4_r1();
+cudaError_t upload_tables_p4_r1(const DegTables<double> *, const DegTables<float> *);
 
 cudaError_t configure_stage_hp_v0();
 cudaError_t configure_stage_hp_v1();
@@ -274,7 +291,23 @@ static int n_groups(const oc_op *op) {
   return k;
 }
 
-static int cells_per_warp(int p) {
+// the one-launch hp kernel: several degree groups, built for the default cell rule only
+static bool hp_possible(const oc_op *op) {
+  return n_groups(op) > 1 && op->prm.cell_quadrature == OC_CELL_RULE_DEFAULT;
+}
+
+// Gauss points per direction of the cell integrals and boundary faces of degree p
+static int cell_q(const oc_op *op, int p) {
+  return op->prm.cell_quadrature == OC_CELL_RULE_P1 ? p + 1 : (3 * p) / 2 + 1;
+}
+
+static int cells_per_warp(const oc_op *op, int p) {
+  if (op->prm.cell_quadrature == OC_CELL_RULE_P1) switch (p) {
+      case 1: return stage_cells_per_warp_p1_r1();
+      case 2: return stage_cells_per_warp_p2_r1();
+      case 3: return stage_cells_per_warp_p3_r1();
+      default: return stage_cells_per_warp_p4_r1();
+    }
   switch (p) {
     case 1: return stage_cells_per_warp_p1();
     case 2: return stage_cells_per_warp_p2();
@@ -283,8 +316,14 @@ static int cells_per_warp(int p) {
   }
 }
 
-static cudaError_t launch_stage(int p, const StageArgs &a, int variant, int grid, int wpb,
-                                cudaStream_t s) {
+static cudaError_t launch_stage(const oc_op *op, int p, const StageArgs &a, int variant, int grid,
+                                int wpb, cudaStream_t s) {
+  if (op->prm.cell_quadrature == OC_CELL_RULE_P1) switch (p) {
+      case 1: return launch_stage_p1_r1(a, variant, grid, wpb, s);
+      case 2: return launch_stage_p2_r1(a, variant, grid, wpb, s);
+      case 3: return launch_stage_p3_r1(a, variant, grid, wpb, s);
+      default: return launch_stage_p4_r1(a, variant, grid, wpb, s);
+    }
   switch (p) {
     case 1: return launch_stage_p1(a, variant, grid, wpb, s);
     case 2: return launch_stage_p2(a, variant, grid, wpb, s);
@@ -327,7 +366,7 @@ oc_status oc_set_launch_mode(oc_op *op, int32_t mode) {
     return fail(op, OC_ERR_INVALID_ARG, "unknown launch mode");
   op->launch_mode = mode;
   op->tuned = 0;
-  op->use_hp = mode == OC_LAUNCH_ONE && n_groups(op) > 1;
+  op->use_hp = mode == OC_LAUNCH_ONE && hp_possible(op);
   if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
   return OC_OK;
 }
@@ -375,6 +414,8 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   };
   if (prm->horizontal_viscosity != 0.0)
     return bad(OC_ERR_UNSUPPORTED, "horizontal_viscosity != 0 is not implemented on the GPU");
+  if (prm->cell_quadrature != OC_CELL_RULE_DEFAULT && prm->cell_quadrature != OC_CELL_RULE_P1)
+    return bad(OC_ERR_INVALID_ARG, "unknown cell quadrature rule");
   if (prm->precision != OC_PREC_FP64 && prm->precision != OC_PREC_MIXED)
     return bad(OC_ERR_INVALID_ARG, "unknown precision");
   // cells: degree, offsets, affine geometry
@@ -389,7 +430,7 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
     const int p = m->degree[c];
     if (p < 1 || p > OC_MAXDEG) return bad(OC_ERR_UNSUPPORTED, "degree must be 1..4");
     uniform = uniform && p == first_deg;
-    const int Q = (3 * p) / 2 + 1;
+    const int Q = cell_q(op, p);
     op->off[c] = (int)off;
     op->sdo[0][c] = (int)s0; op->sdo[1][c] = (int)s1; op->sdo[2][c] = (int)s2;
     off += (p + 1) * (p + 1);
@@ -455,7 +496,7 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
       op->bbid[b] = bid;
       op->fpack[f] = fm;
       op->fsd[f] = (int)sb;
-      sb += (3 * m->degree[cm]) / 2 + 1;
+      sb += cell_q(op, m->degree[cm]);
       int *sm = &op->slots[8 * (size_t)cm + 2 * fm];
       if (sm[0] != -1) return bad(OC_ERR_INVALID_ARG, "cell face listed twice (boundary)");
       sm[0] = -(b + 2);
@@ -473,7 +514,7 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   op->fofs.resize(nf);
   int64_t fo_total = 0;
   for (int f = 0; f < nf; ++f) {
-    const int npt = f < ni ? (op->fpack[f] >> 16) & 15 : (3 * op->deg[op->fcm[f]]) / 2 + 1;
+    const int npt = f < ni ? (op->fpack[f] >> 16) & 15 : cell_q(op, op->deg[op->fcm[f]]);
     op->fofs[f] = (int)fo_total;
     fo_total += (f < ni ? 6 : 3) * npt;
   }
@@ -549,7 +590,7 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
     // rounded up to whole blocks of at most kWarpsPerBlock warps)
     size_t warps = 0;
     for (int p = 1; p <= OC_MAXDEG; ++p) {
-      const int cpw = (cells_per_warp(p) / op->prm.batch_width) * op->prm.batch_width;
+      const int cpw = (cells_per_warp(op, p) / op->prm.batch_width) * op->prm.batch_width;
       if (op->group_n[p] == 0 || cpw == 0) continue;
       warps += (op->group_n[p] + cpw - 1) / cpw + kWarpsPerBlock;
     }
@@ -567,6 +608,10 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   OC_TRY(upload_tables_p2(td.data(), tf.data()));
   OC_TRY(upload_tables_p3(td.data(), tf.data()));
   OC_TRY(upload_tables_p4(td.data(), tf.data()));
+  OC_TRY(upload_tables_p1_r1(td.data(), tf.data()));
+  OC_TRY(upload_tables_p2_r1(td.data(), tf.data()));
+  OC_TRY(upload_tables_p3_r1(td.data(), tf.data()));
+  OC_TRY(upload_tables_p4_r1(td.data(), tf.data()));
   OC_TRY(upload(op, &op->d_tabd, td.data(), td.size()));
   OC_TRY(upload(op, &op->d_tabf, tf.data(), tf.size()));
   OC_TRY(upload_tables_hp_v0(td.data(), tf.data()));
@@ -582,6 +627,10 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   OC_TRY(configure_stage_p2());
   OC_TRY(configure_stage_p3());
   OC_TRY(configure_stage_p4());
+  OC_TRY(configure_stage_p1_r1());
+  OC_TRY(configure_stage_p2_r1());
+  OC_TRY(configure_stage_p3_r1());
+  OC_TRY(configure_stage_p4_r1());
   OC_TRY(configure_stage_hp_v0());
   OC_TRY(configure_stage_hp_v1());
   OC_TRY(configure_stage_hp_v2());
@@ -631,7 +680,7 @@ oc_status oc_quadrature_points(const oc_op *op, int32_t which, double *xy) {
   if (which <= 2) {
     for (int c = 0; c < op->n_cells; ++c) {
       const int p = op->deg[c];
-      const int n = which == 0 ? (3 * p) / 2 + 1 : which == 1 ? p + 2 : p + 1;
+      const int n = which == 0 ? cell_q(op, p) : which == 1 ? p + 2 : p + 1;
       if (which == 1) lobatto_rule(n, x, w); else gauss_rule(n, x, w);
       for (int qy = 0; qy < n; ++qy)
         for (int qx = 0; qx < n; ++qx) { map(c, x[qx], x[qy], xy + 2 * k); ++k; }
@@ -652,7 +701,7 @@ oc_status oc_quadrature_points(const oc_op *op, int32_t which, double *xy) {
   } else {
     for (int b = 0; b < op->n_bnd; ++b) {
       const int f = op->n_inner + b, c = op->fcm[f], fm = op->fpack[f] & 15;
-      const int n = (3 * op->deg[c]) / 2 + 1;
+      const int n = cell_q(op, op->deg[c]);
       gauss_rule(n, x, w);
       for (int q = 0; q < n; ++q) {
         double e0, e1;
@@ -711,6 +760,7 @@ static void fill_common(oc_op *op, StageArgs &a) {
   a.cfofs = op->d_cfofs;
   a.n_bnd_faces = op->n_bnd; a.fofs = op->d_fofs;
   a.fout = op->d_fout;
+  a.cell_rule = op->prm.cell_quadrature;
   a.n_dofs = op->n_dofs; a.n_fout = op->n_fout;
   for (int k = 0; k < 5; ++k) a.n_sd[k] = op->sd_size[k];
   a.geof = op->prm.precision == OC_PREC_MIXED ? op->d_geof : nullptr;
@@ -760,7 +810,7 @@ static oc_status check_boundaries(oc_op *op) {
 static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
   const int batch = op->prm.batch_width;
   for (int p = 1; p <= OC_MAXDEG; ++p)
-    if (op->group_n[p] && (cells_per_warp(p) / batch) * batch == 0)
+    if (op->group_n[p] && (cells_per_warp(op, p) / batch) * batch == 0)
       return fail(op, OC_ERR_UNSUPPORTED, "batch_width larger than the cells of a warp");
   // face pass of the FP64 stage: every face's flux once, both sides' values (the
   // mixed stage kernels evaluate their faces themselves)
@@ -773,7 +823,7 @@ static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
     int b0 = 0;
     for (int p = OC_MAXDEG; p >= 1; --p) {
       const int n = op->group_n[p];
-      const int cpw = (cells_per_warp(p) / batch) * batch;
+      const int cpw = (cells_per_warp(op, p) / batch) * batch;
       a.hp_first_block[p] = b0;
       a.hp_n[p] = n;
       a.hp_cells[p] = op->d_group[p];
@@ -788,13 +838,13 @@ static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
   for (int p = 1; p <= OC_MAXDEG; ++p) {
     const int n = op->group_n[p];
     if (n == 0) continue;
-    const int cpw = (cells_per_warp(p) / batch) * batch;
+    const int cpw = (cells_per_warp(op, p) / batch) * batch;
     const int wpb = op->wpb[p];
     a.n_group = n;
     a.group_cells = op->uniform_deg ? nullptr : op->d_group[p];
     a.group_first = 0;
     const int grid = (n + wpb * cpw - 1) / (wpb * cpw);
-    OC_TRY(launch_stage(p, a, variant, grid, wpb, op->stream));
+    OC_TRY(launch_stage(op, p, a, variant, grid, wpb, op->stream));
     op->launches++;
   }
   return OC_OK;
@@ -1098,7 +1148,7 @@ static oc_status autotune(oc_op *op, const Scheme &sc, const double *z, const do
   }
   op->tune_ms[0] = per_group;
   float one = 3.4e38f;
-  if (st == OC_OK && op->launch_mode != OC_LAUNCH_PER_GROUP && n_groups(op) > 1) {
+  if (st == OC_OK && op->launch_mode != OC_LAUNCH_PER_GROUP && hp_possible(op)) {
     op->use_hp = 1;
     int bw = 4;
     for (int c = 1; c < 3 && st == OC_OK; ++c) {
@@ -1110,9 +1160,9 @@ static oc_status autotune(oc_op *op, const Scheme &sc, const double *z, const do
     op->hp_wpb = bw;
     op->tune_ms[1] = one;
   }
-  op->use_hp = op->launch_mode == OC_LAUNCH_ONE ? (n_groups(op) > 1)
+  op->use_hp = op->launch_mode == OC_LAUNCH_ONE ? hp_possible(op)
                : op->launch_mode == OC_LAUNCH_PER_GROUP ? 0
-               : (n_groups(op) > 1 && one < per_group);
+               : (hp_possible(op) && one < per_group);
   op->launches = launches;
   cudaStreamSynchronize(op->stream);
   cudaFree(tz);
@@ -1224,6 +1274,7 @@ static AuxArgs aux_args(oc_op *op) {
   for (int k = 0; k < 8; ++k) a.vortex[k] = op->vortex[k];
   a.n_dofs = op->n_dofs;
   for (int k = 0; k < 5; ++k) a.n_sd[k] = op->sd_size[k];
+  a.cell_rule = op->prm.cell_quadrature;
   a.err = op->d_err;
   return a;
 }

@@ -225,8 +225,12 @@ __global__ void errors_kernel(const AuxArgs a, double time, const double *sd0, c
                               const double *z, const double *q, double *part) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.n_cells) return;
-  const int p = checked_degree(a.err, a.deg[c]), N = p + 1, n = N * N, Q = (3 * p) / 2 + 1;
+  const int p = checked_degree(a.err, a.deg[c]), N = p + 1, n = N * N;
+  const int Q = a.cell_rule ? p + 1 : (3 * p) / 2 + 1;
   const DegTables<double> &tb = tab<double>(p);
+  // the cell Gauss rule's tables: floor(1.5 p) + 1 points, or the Gauss p+1 ones
+  const double(*BQ)[OC_MAXN] = a.cell_rule ? tb.BM : tb.BQ;
+  const double *xQ = a.cell_rule ? tb.xM : tb.xQ, *wQ = a.cell_rule ? tb.wM : tb.wQ;
   const double *J = a.geo + 11 * (int64_t)c;
   const int64_t zo = checked(a.err, a.off[c], a.n_dofs - n + 1, BS_OFFSET);
   const double *zc = z + zo, *q0 = q + 2 * zo, *q1 = q + 2 * zo + n;
@@ -238,17 +242,17 @@ __global__ void errors_kernel(const AuxArgs a, double time, const double *sd0, c
       double zv = 0., a0 = 0., a1 = 0.;
       for (int iy = 0; iy < N; ++iy)
         for (int ix = 0; ix < N; ++ix) {
-          const double b = tb.BQ[qy][iy] * tb.BQ[qx][ix];
+          const double b = BQ[qy][iy] * BQ[qx][ix];
           zv += b * zc[iy * N + ix];
           a0 += b * q0[iy * N + ix];
           a1 += b * q1[iy * N + ix];
         }
-      const double x = J[0] + J[2] * tb.xQ[qx] + J[3] * tb.xQ[qy];
-      const double y = J[1] + J[4] * tb.xQ[qx] + J[5] * tb.xQ[qy];
+      const double x = J[0] + J[2] * xQ[qx] + J[3] * xQ[qy];
+      const double y = J[1] + J[4] * xQ[qx] + J[5] * xQ[qy];
       const double zb = sd ? sd[5 * (qy * Q + qx)] : 0.;
       const double f0 = vortex_value(vp, a.g, x, y, time, 0);
       const double hq = depth<double>(f0, zb);
-      const double jxw = tb.wQ[qx] * tb.wQ[qy] * J[10];
+      const double jxw = wQ[qx] * wQ[qy] * J[10];
       const double d0 = hq - depth<double>(zv, zb);
       const double u = vortex_value(vp, a.g, x, y, time, 1) * hq - a0;
       const double v = vortex_value(vp, a.g, x, y, time, 2) * hq - a1;

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(128) face_kernel(const StageArgs a) {
       a.n_dofs - Nm * Nm + 1, BS_OFFSET);
   const bool inner = f < a.n_inner;
   const int nf = P ? P + 2 : (fpk >> 16) & 15;  // points of an inner face
-  const int Qm = (3 * pm) / 2 + 1;              // points of a boundary face
+  const int Qm = a.cell_rule ? pm + 1 : (3 * pm) / 2 + 1;  // points of a boundary face
 #ifdef OC_BOUNDS_CHECK
   if (inner && (nf < 2 || nf > OC_MAXF || ((fpk >> 8) & 15) > 2)) {  // pack word: nf, subface
     checked(a.err, fpk, 0, BS_RECORD);
@@ -162,7 +162,10 @@ __global__ void __launch_bounds__(128) face_kernel(const StageArgs a) {
     }
     const int Q = Qm;
     const DegTables<R> &tm = gt[pm - 1];
-    const DegTables<double> &td = reinterpret_cast<const DegTables<double> *>(a.gtabd)[pm - 1];
+    // the cell Gauss rule's rows: floor(1.5 p) + 1 points, or the Gauss p+1 tables
+    const R(*BQ)[OC_MAXN] = a.cell_rule ? tm.BM : tm.BQ;
+    const R *wQ = a.cell_rule ? tm.wM : tm.wQ;
+    const R *xQ = a.cell_rule ? tm.xM : tm.xQ;
     const double *geo = a.geo + 11 * (int64_t)cm;
 #pragma unroll 1
     for (int k = 0; k < Q; ++k) {
@@ -170,14 +173,14 @@ __global__ void __launch_bounds__(128) face_kernel(const StageArgs a) {
 #pragma unroll
       for (int n = 0; n < NMAX; ++n) {
         if (P || n < Nm) {
-          const R l = __ldg(&tm.BQ[k][n]);
+          const R l = __ldg(&BQ[k][n]);
           zm += l * zmn[n]; qm0 += l * qm0n[n]; qm1 += l * qm1n[n];
         }
       }
       R F, Fa0, Fa1;
-      boundary_flux<R, false>(a, bid, bkind, fm, __ldg(&td.xQ[k]), geo, 0.0, fsd + k, g, cu4, zm,
-                            qm0, qm1, n0, n1, F, Fa0, Fa1);
-      const R jxw = __ldg(&tm.wQ[k]) * len;
+      boundary_flux<R, false>(a, bid, bkind, fm, __ldg(&xQ[k]), geo, 0.0, fsd + k, g, cu4, zm,
+                              qm0, qm1, n0, n1, F, Fa0, Fa1);
+      const R jxw = __ldg(&wQ[k]) * len;
       out[k] = -F * jxw;
       out[Q + k] = -Fa0 * jxw;
       out[2 * Q + k] = -Fa1 * jxw;

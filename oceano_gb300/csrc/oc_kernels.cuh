@@ -467,9 +467,11 @@ __device__ __forceinline__ KT ldro(const void *p, int64_t i) {
 // stride of the per-variable face point values (>= OC_MAXF and OC_MAXQ)
 constexpr int FVS = 8;
 
-template <int P>
+// QR: the cell Gauss rule (the reference's n_points_1d, main.cc:216 /
+// OceanDG.h:448): 0 floor(1.5 P) + 1 points per direction, 1 P + 1 points
+template <int P, int QR = 0>
 struct Dims {
-  static constexpr int N = P + 1, Q = (3 * P) / 2 + 1, G = P + 2;
+  static constexpr int N = P + 1, Q = QR ? P + 1 : (3 * P) / 2 + 1, G = P + 2;
   static constexpr int T = Q > G ? Q : G;
   static constexpr int NN = N * N, NT = N * T;
   static constexpr int CPW = 32 / T;
@@ -544,11 +546,11 @@ __device__ __forceinline__ double team_max(double *red, int t, bool member, doub
 // Evaluate the FP64 tile DZ at the Gauss-Lobatto (p+2)^2 points, call
 // fn(qx, qy, value, o0, o1) per point, integrate o0, o1 back against the basis
 // into out0/out1 (rows of thread t < N).  All lanes call; `work` gates arithmetic.
-template <int P, class Fn>
+template <int P, int QR, class Fn>
 __device__ __forceinline__ void gl_eval_apply_integrate(const double *DZ, double *DX, int t,
                                                         bool work, Fn fn, double *out0,
                                                         double *out1) {
-  using D = Dims<P>;
+  using D = Dims<P, QR>;
   constexpr int N = D::N, G = D::G, T = D::T, NT = D::NT;
   const DegTables<double> &tb = tab<double>(P);
   if (work && t < N) {
@@ -607,11 +609,11 @@ __device__ __forceinline__ void gl_eval_apply_integrate(const double *DZ, double
 // stopped when the l1 norm of the update summed over the cell batch is <= 1e-12.
 // DZ holds the initial guess on entry and the result on exit; rhs are the
 // rows of thread t < N.  All lanes call; `work` selects the participating teams.
-template <int P>
+template <int P, int QR>
 __device__ void zeta_iteration_fp64(const StageArgs &a, int cell, double *DZ, double *DX,
                                     double *DRED, double *warp_norm, int team, int cpw, int t,
                                     bool member, bool work, const double *rhs) {
-  using D = Dims<P>;
+  using D = Dims<P, QR>;
   constexpr int N = D::N, G = D::G, T = D::T;
   const DegTables<double> &tb = tab<double>(P);
   const double *geo = a.geo + 11 * (int64_t)cell;
@@ -622,7 +624,7 @@ __device__ void zeta_iteration_fp64(const StageArgs &a, int cell, double *DZ, do
     int ndry = 0;
     double zbmax = -1.7976931348623157e308;
     double d0[N], d1[N];
-    gl_eval_apply_integrate<P>(
+    gl_eval_apply_integrate<P, QR>(
         DZ, DX, t, work,
         [&](int qx, int qy, double v, double &o0, double &o1) {
           const double zb = zb1 ? zb1[qy * G + qx] : 0.;
@@ -646,7 +648,7 @@ __device__ void zeta_iteration_fp64(const StageArgs &a, int cell, double *DZ, do
     if (!__any_sync(OC_FULL, active)) break;
     int ndry = 0;
     double r[N], m[N];
-    gl_eval_apply_integrate<P>(
+    gl_eval_apply_integrate<P, QR>(
         DZ, DX, t, active,
         [&](int qx, int qy, double v, double &o0, double &o1) {
           const double zb = zb1 ? zb1[qy * G + qx] : 0.;
@@ -796,11 +798,11 @@ struct FaceRec {
 };
 
 #ifdef OC_BOUNDS_CHECK
-// Face record of a slot of a cell of degree p (bounds-checked build): packed
+// Face record of a slot of a cell with q boundary-face points (bounds-checked build): packed
 // fields in range, the neighbour's DoFs or the boundary face, the static face
 // data (sdo) and the face-pass values (fo) of the slot inside their arrays.  A
 // malformed record becomes an empty slot; a bad offset becomes 0.
-static __device__ __noinline__ void check_record(const StageArgs &a, FaceRec &r, int p,
+static __device__ __noinline__ void check_record(const StageArgs &a, FaceRec &r, int q,
                                                  int *sdo, int *fo) {
   const int kind = r.kind();
   if (kind == 0) return;
@@ -814,7 +816,7 @@ static __device__ __noinline__ void check_record(const StageArgs &a, FaceRec &r,
     r.other = 0;
     return;
   }
-  const int nfo = kind == 1 ? r.nf() : (3 * p) / 2 + 1;
+  const int nfo = kind == 1 ? r.nf() : q;
   if (kind == 1) {
     const int nn = (r.nb_deg() + 1) * (r.nb_deg() + 1);
     r.other = (int)checked(a.err, r.other, a.n_dofs - nn + 1, BS_NEIGHBOUR);
@@ -867,15 +869,20 @@ __device__ __forceinline__ void report_nonfinite(const StageArgs &a, bool bad) {
 // One block of the stage: `blk` is the block index within the degree group of
 // n_group cells (listed by group_cells, or group_first + i when NULL); the FP64
 // work-area slots of the mixed form are indexed by the launch-wide block index.
-template <int P, typename R, typename KT, bool MIX, typename RIN, bool LEAN>
+template <int P, typename R, typename KT, bool MIX, typename RIN, bool LEAN, int QR>
 __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *smem_raw,
                                            const int blk, const int n_group,
                                            const int *group_cells, const int group_first) {
-  using D = Dims<P>;
+  using D = Dims<P, QR>;
   constexpr int N = D::N, Q = D::Q, G = D::G, T = D::T, NN = D::NN, NT = D::NT;
   constexpr int CPWMAX = D::CPW;
   static_assert(CPWMAX <= OC_MAXCPW, "cells per warp above the work-area slot stride");
   const DegTables<R> &tb = tab<R>(P);
+  // cell Gauss rule: the floor(1.5 P) + 1 point tables, or (QR = 1) the P + 1 point
+  // tables of the discharge mass
+  const auto &cBQ = QR ? tb.BM : tb.BQ;
+  const auto &cDQ = QR ? tb.DM : tb.DQ;
+  const auto &cwQ = QR ? tb.wM : tb.wQ;
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int team_raw = lane / T, t = lane - team_raw * T;
@@ -984,7 +991,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #ifdef OC_BOUNDS_CHECK
   __syncwarp();
   for (int e = lane; e < nvalid * 8; e += 32)
-    check_record(a, reinterpret_cast<FaceRec *>(w_rec)[e], P, cfsdo_p ? w_sdo + e : nullptr,
+    check_record(a, reinterpret_cast<FaceRec *>(w_rec)[e], Q, cfsdo_p ? w_sdo + e : nullptr,
                  FPASS ? w_fo + e : nullptr);
 #endif
   // Everything above reads only the mesh (written before the stream's first stage
@@ -1129,7 +1136,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           c1 += pcol[k] * FV[2 * FVS + k];
         }
       } else {
-        const R *col = tsel < 0 ? &ptb.BQ[0][t] : &ptb.F[tsel][nfo][0][t];  // stride OC_MAXN
+        const R *col = tsel < 0 ? (QR ? &ptb.BM[0][t] : &ptb.BQ[0][t]) : &ptb.F[tsel][nfo][0][t];  // stride OC_MAXN
 #pragma unroll
         for (int k = 0; k < (Q > OC_MAXF ? Q : OC_MAXF); ++k) {  // nfo <= max(Q, OC_MAXF)
           if (k < nfo) {
@@ -1164,8 +1171,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       R b0 = 0, d0 = 0, a0 = 0, a1 = 0;
 #pragma unroll
       for (int ix = 0; ix < N; ++ix) {
-        fma2(b0, a0, tb.BQ[qx][ix], z[ix], tb.BQ[qx][ix], q0[ix]);
-        fma2(d0, a1, tb.DQ[qx][ix], z[ix], tb.BQ[qx][ix], q1[ix]);
+        fma2(b0, a0, cBQ[qx][ix], z[ix], cBQ[qx][ix], q0[ix]);
+        fma2(d0, a1, cDQ[qx][ix], z[ix], cBQ[qx][ix], q1[ix]);
       }
       X[0 * NT + t * T + qx] = b0;
       X[1 * NT + t * T + qx] = d0;
@@ -1192,10 +1199,10 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
         for (int iy = 0; iy < N; ++iy) {
           const R xb = X[0 * NT + iy * T + t], xd = X[1 * NT + iy * T + t];
-          const R b = tb.BQ[qy][iy];
+          const R b = cBQ[qy][iy];
           fma2(z, zx, b, xb, b, xd);
           fma2(q0, q1, b, X[2 * NT + iy * T + t], b, X[3 * NT + iy * T + t]);
-          zy += tb.DQ[qy][iy] * xb;
+          zy += cDQ[qy][iy] * xb;
         }
         const int k = qy * Q + t;
         R zb = MIX ? zbe_flat : R(0), cf = 0, w0 = 0, w1 = 0, fc = 0;
@@ -1206,7 +1213,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           zb = (R)sd0[5 * k]; cf = (R)sd0[5 * k + 1]; w0 = (R)sd0[5 * k + 2];
           w1 = (R)sd0[5 * k + 3]; fc = (R)sd0[5 * k + 4];
         }
-        const R w = tb.wQ[t] * tb.wQ[qy] * det;
+        const R w = cwQ[t] * cwQ[qy] * det;
         // height: int q . grad(phi)   (mass_flux = q, ShallowWater.h:349-357)
         const R gz0 = (Ji00 * q0 + Ji01 * q1) * w, gz1 = (Ji10 * q0 + Ji11 * q1) * w;
         // discharge: advective flux (ShallowWater.h:378-403, nu = 0) and sources (:405-472)
@@ -1240,7 +1247,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         const R sv0 = s0 * w, sv1 = s1 * w;
 #pragma unroll
         for (int iy = 0; iy < N; ++iy) {
-          const R b = tb.BQ[qy][iy], d = tb.DQ[qy][iy];
+          const R b = cBQ[qy][iy], d = cDQ[qy][iy];
           fma2(Az[iy], Cz[iy], b, gz0, d, gz1);
           fma2(A0[iy], A1[iy], b, g00, b, g10);
           fma2(C0[iy], C1[iy], d, g01, d, g11);
@@ -1267,7 +1274,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         R rz = 0, r0 = 0, r1 = 0;
 #pragma unroll
         for (int qx = 0; qx < Q; ++qx) {
-          const R b = tb.BQ[qx][ix], d = tb.DQ[qx][ix];
+          const R b = cBQ[qx][ix], d = cDQ[qx][ix];
           fma2(r0, r1, d, X[2 * NT + t * T + qx], d, X[4 * NT + t * T + qx]);
           fma2(r0, r1, b, X[3 * NT + t * T + qx], b, X[5 * NT + t * T + qx]);
           rz += d * X[0 * NT + t * T + qx];
@@ -1294,9 +1301,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         R b0 = 0, a0 = 0, a1 = 0;
 #pragma unroll
         for (int ix = 0; ix < N; ++ix) {
-          b0 += tb.BQ[qx][ix] * z[ix];
-          a0 += tb.BQ[qx][ix] * q0[ix];
-          a1 += tb.BQ[qx][ix] * q1[ix];
+          b0 += cBQ[qx][ix] * z[ix];
+          a0 += cBQ[qx][ix] * q0[ix];
+          a1 += cBQ[qx][ix] * q1[ix];
         }
         X[2 * NT + t * T + qx] = b0;
         X[3 * NT + t * T + qx] = a0;
@@ -1316,9 +1323,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         R z = 0, q0 = 0, q1 = 0;
 #pragma unroll
         for (int iy = 0; iy < N; ++iy) {
-          z += tb.BQ[qy][iy] * X[2 * NT + iy * T + t];
-          q0 += tb.BQ[qy][iy] * X[3 * NT + iy * T + t];
-          q1 += tb.BQ[qy][iy] * X[4 * NT + iy * T + t];
+          z += cBQ[qy][iy] * X[2 * NT + iy * T + t];
+          q0 += cBQ[qy][iy] * X[3 * NT + iy * T + t];
+          q1 += cBQ[qy][iy] * X[4 * NT + iy * T + t];
         }
         const int k = qy * Q + t;
         R zb = MIX ? zbe_flat : R(0), cf = 0;
@@ -1328,12 +1335,12 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         if constexpr (MIX) velocity<R>(z, rf.qr0 + q0, rf.qr1 + q1, zb, cu4, v0, v1);
         else velocity<R>(z, q0, q1, zb, cu4, v0, v1);
         if (friction_m) friction<R>(friction_m, g, v0, v1, cf, depth<R>(z, zb), fr0, fr1);
-        const R w = tb.wQ[t] * tb.wQ[qy] * det;
+        const R w = cwQ[t] * cwQ[qy] * det;
         const R st0 = -fr0 * w, st1 = -fr1 * w;
 #pragma unroll
         for (int iy = 0; iy < N; ++iy) {
-          S0[iy] += tb.BQ[qy][iy] * st0;
-          S1[iy] += tb.BQ[qy][iy] * st1;
+          S0[iy] += cBQ[qy][iy] * st0;
+          S1[iy] += cBQ[qy][iy] * st1;
         }
       }
     }
@@ -1352,8 +1359,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         R r0 = 0, r1 = 0;
 #pragma unroll
         for (int qx = 0; qx < Q; ++qx) {
-          r0 += tb.BQ[qx][ix] * X[0 * NT + t * T + qx];
-          r1 += tb.BQ[qx][ix] * X[1 * NT + t * T + qx];
+          r0 += cBQ[qx][ix] * X[0 * NT + t * T + qx];
+          r1 += cBQ[qx][ix] * X[1 * NT + t * T + qx];
         }
         RST[t * N + ix] = r0;
         RST[NN + t * N + ix] = r1;
@@ -1572,15 +1579,15 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
           for (int i = 0; i < N; ++i) {
             const int d = face_dof(N, fo, i);
-            const R l = tb.BQ[k][i];
+            const R l = cBQ[k][i];
             zm += l * U[d];
             qm0 += l * U[NN + d];
             qm1 += l * U[2 * NN + d];
           }
           R F, Fa0, Fa1;
-          boundary_flux<R, MIX>(a, bid, bkind, fo, tab<double>(P).xQ[k], geo, zref, sdo + k, g, cu4,
+          boundary_flux<R, MIX>(a, bid, bkind, fo, (QR ? tab<double>(P).xM[k] : tab<double>(P).xQ[k]), geo, zref, sdo + k, g, cu4,
                                 zm, qm0, qm1, n0, n1, F, Fa0, Fa1);
-          const R jxw = tb.wQ[k] * len;
+          const R jxw = cwQ[k] * len;
           FV[k] = -F * jxw;
           FV[FVS + k] = -Fa0 * jxw;
           FV[2 * FVS + k] = -Fa1 * jxw;
@@ -1602,7 +1609,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           c1 += fcol[k] * FV[2 * FVS + k];
         }
       } else {
-        const R *col = tsel < 0 ? &tbg.BQ[0][t] : &tbg.F[tsel][nfo][0][t];  // stride OC_MAXN
+        const R *col = tsel < 0 ? (QR ? &tbg.BM[0][t] : &tbg.BQ[0][t]) : &tbg.F[tsel][nfo][0][t];  // stride OC_MAXN
 #pragma unroll
         for (int k = 0; k < (Q > OC_MAXF ? Q : OC_MAXF); ++k) {  // nfo <= max(Q, OC_MAXF)
           if (k < nfo) {
@@ -1820,7 +1827,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       const double det_d = geo[10];
       const double *zb1 = sd1_p ? sd1_p + cell_data(a.err, a.sdo1, cell, a.n_sd[1], G * G) : nullptr;
       const DegTables<double> &td = tab<double>(P);
-      gl_eval_apply_integrate<P>(
+      gl_eval_apply_integrate<P, QR>(
           DZ, DX, t, work,
           [&](int qx, int qy, double v, double &o0, double &o1) {
             const double zb = zb1 ? zb1[qy * G + qx] : 0.;
@@ -1832,7 +1839,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
         for (int ix = 0; ix < N; ++ix) rhs[ix] = (double)BZ[t * N + ix] + rhs[ix];
     }
-    zeta_iteration_fp64<P>(a, cell, DZ, DX, DRED, warp_norm, team, cpw, t, member, work, rhs);
+    zeta_iteration_fp64<P, QR>(a, cell, DZ, DX, DRED, warp_norm, team, cpw, t, member, work, rhs);
     if (work && t == 0) w_flag[team] = 1;
   }
   if (MIX && member && t < N && !need_fp64) {  // wet: keep delta (FP32) in BZ
@@ -2215,11 +2222,11 @@ static cudaError_t launch_programmatic(K kernel, int grid, int threads, int smem
 }
 
 // One degree group per launch.
-template <int P, typename R, typename KT, bool MIX, typename RIN, bool LEAN>
+template <int P, typename R, typename KT, bool MIX, typename RIN, bool LEAN, int QR>
 __global__ void __launch_bounds__(128, MIX ? OC_MIXED_MIN_BLOCKS : 1) stage_kernel(const StageArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_body<P, R, KT, MIX, RIN, LEAN>(a, smem_raw, blockIdx.x, a.n_group, a.group_cells,
-                                       a.group_first);
+  stage_body<P, R, KT, MIX, RIN, LEAN, QR>(a, smem_raw, blockIdx.x, a.n_group, a.group_cells,
+                                           a.group_first);
 }
 
 // Every degree group of an hp mesh in one launch: the grid is the concatenation
@@ -2234,7 +2241,7 @@ __global__ void __launch_bounds__(128, MIX ? OC_HP_MIN_BLOCKS : 1) stage_kernel_
   const int b = blockIdx.x;
 #define OC_HP_CASE(P)                                                                          \
   if (b >= a.hp_first_block[P] && b < a.hp_first_block[P] + a.hp_blocks[P]) {                 \
-    stage_body<P, R, KT, MIX, RIN, LEAN>(a, smem_raw, b - a.hp_first_block[P], a.hp_n[P],     \
+    stage_body<P, R, KT, MIX, RIN, LEAN, 0>(a, smem_raw, b - a.hp_first_block[P], a.hp_n[P],  \
                                          a.hp_cells[P], 0);                                    \
     return;                                                                                    \
   }

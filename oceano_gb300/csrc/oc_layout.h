@@ -43,7 +43,10 @@ template <typename R>
 struct DegTables {
   R BQ[OC_MAXQ][OC_MAXN], DQ[OC_MAXQ][OC_MAXN], wQ[OC_MAXQ], xQ[OC_MAXQ];  // Gauss floor(1.5p)+1
   R BG[OC_MAXF][OC_MAXN], wG[OC_MAXF];                        // Gauss-Lobatto p+2
-  R BM[OC_MAXN][OC_MAXN], Sinv[OC_MAXN][OC_MAXN], wM[OC_MAXN], xM[OC_MAXN];  // Gauss p+1
+  // Gauss p+1: mass of the discharge and, with DM, the cell rule n_points_1d = p + 1
+  // (rows sized like the BQ rows so that a kernel selects either rule's arrays)
+  R BM[OC_MAXQ][OC_MAXN], DM[OC_MAXQ][OC_MAXN], wM[OC_MAXQ], xM[OC_MAXQ];
+  R Sinv[OC_MAXN][OC_MAXN];
   R F[3][OC_MAXF + 1][OC_MAXF][OC_MAXN];  // [0 full face | 1,2 subface 0,1][nf][k][node]
   R wF[OC_MAXF + 1][OC_MAXF];             // Gauss-Lobatto nf weights
   R lump[OC_MAXN];                        // 1D lumped GL(p+2) mass
@@ -108,6 +111,7 @@ struct StageArgs {
   int n_bnd_faces;
   const int *fofs;
   void *fout;
+  int cell_rule;  // Gauss points of boundary faces: 0 floor(1.5 p) + 1, 1 p + 1
   // static data (NULL = zero); *e arrays are FP32 copies with zeta_reference folded into zb
   const double *sd0, *sd1, *sd2, *sdf, *sdb;
   const float *sd0e, *sd1e, *sd2e, *sdfe, *sdbe;
@@ -179,5 +183,6 @@ struct AuxArgs {
   double g, cu4;
   double vortex[8];
   int64_t n_dofs, n_sd[5];  // extents checked by the bounds-checked build
+  int cell_rule;            // cell Gauss rule of the errors: 0 floor(1.5 p) + 1, 1 p + 1
   int *err;
 };

@@ -191,6 +191,7 @@ inline void fill_tables(int p, int max_iter, DegTables<double> &t) {
     for (int i = 0; i < N; ++i) {
       S[q * N + i] = lag(N, xN, i, xM[q]);
       t.BM[q][i] = S[q * N + i];
+      t.DM[q][i] = lag_d(N, xN, i, xM[q]);
     }
   }
   invert_small(N, S, Si);

@@ -52,7 +52,10 @@ class OceanoOperator:
 
     def __init__(self, mesh, g=9.81, threshold_wetdry=0.1, horizontal_viscosity=0.0,
                  friction="none", max_iteration_height=15, batch_width=1, precision="fp64",
-                 zeta_reference=0.0):
+                 zeta_reference=0.0, cell_quadrature="default"):
+        """cell_quadrature: Gauss points per direction of the cell integrals, boundary
+        faces, cell/boundary static data and errors (the reference's n_points_1d,
+        main.cc:216): "default" = floor(1.5 p) + 1, "p+1" = p + 1 (4x4 at p = 3)."""
         self.mesh = mesh
         self.precision = precision
         self._keep = [np.ascontiguousarray(a) for a in (
@@ -67,7 +70,8 @@ class OceanoOperator:
                              _ptr(k[7]), _ptr(k[8]))
         prm = _lib.Params(g, threshold_wetdry, horizontal_viscosity, FRICTION[friction],
                           max_iteration_height, batch_width, PRECISION[precision],
-                          zeta_reference)
+                          zeta_reference, _lib.CELL_RULE[cell_quadrature])
+        self.cell_quadrature = cell_quadrature
         h = C.c_void_p()
         st = lib().oc_create(C.byref(desc), C.byref(prm), C.byref(h))
         self.h = h

@@ -47,13 +47,14 @@ def apply_bcs(op, bcs):
             op.set_boundary(bid, kind, "constant", spec[1] if len(spec) > 1 else (0, 0, 0))
 
 
-def vortex_operator(mesh, precision, vx=None):
+def vortex_operator(mesh, precision, vx=None, cell_quadrature="default"):
     """Operator of the vortex runs: walls (id 0), the vortex data; the mixed form
     measures zeta and q from the undisturbed background (depth h0, discharge
     h0 u_inf)."""
     vx = vx or vortex_params()
     op = OceanoOperator(mesh, precision=precision,
-                        zeta_reference=vx[0] if precision == "mixed" else 0.0)
+                        zeta_reference=vx[0] if precision == "mixed" else 0.0,
+                        cell_quadrature=cell_quadrature)
     if precision == "mixed":
         op.set_reference_state(vx[0], (vx[0] * vx[1], 0.0))
     op.set_wall_boundary(0)

@@ -176,10 +176,11 @@ typedef struct {
   double xM[MAXN], wM[MAXN], BM[MAXN * MAXN], BMinv[MAXN * MAXN];
 } shape_t;
 
-static void shape_init(shape_t *s, int p)
+static void shape_init(shape_t *s, int p, int cell_rule)
 {
   double w[MAXF];
-  s->p = p; s->N = p + 1; s->Q = (int)floor(1.5 * p) + 1; s->G = p + 2; s->M = p + 1;
+  s->p = p; s->N = p + 1; s->Q = cell_rule ? p + 1 : (int)floor(1.5 * p) + 1; s->G = p + 2;
+  s->M = p + 1;
   rule_lobatto(s->N, s->xN, w);
   rule_gauss(s->Q, s->xQ, s->wQ);
   rule_lobatto(s->G, s->xG, s->wG);
@@ -261,6 +262,8 @@ typedef struct {
   int friction; /* 0 none, 1 linear, 2 manning (BottomFriction.h) */
   int max_iter; /* max_iteration_height, main.cc */
   int batch;    /* SIMD lanes per cell batch for the stop rule */
+  int cell_rule; /* Gauss points per direction of the cell integrals and boundary faces
+                    (n_points_1d, main.cc:216 / OceanDG.h:448): 0 floor(1.5 p) + 1, 1 p + 1 */
 } params_t;
 
 typedef struct {
@@ -289,7 +292,6 @@ typedef struct {
 } oracle_t;
 
 static int64_t nd_of(int p) { return (int64_t)(p + 1) * (p + 1); }
-static int nq_of(int p) { return (int)floor(1.5 * p) + 1; }
 
 static double max_d(double a, double b) { return a < b ? b : a; } /* std::max */
 static double min_d(double a, double b) { return b < a ? b : a; } /* std::min */
@@ -469,13 +471,14 @@ void *oc_oracle_create(int n_cells, const int *degree, const double *vertices, i
   o->prm.friction = params_i[0];
   o->prm.max_iter = params_i[1];
   o->prm.batch = params_i[2] > 0 ? params_i[2] : 1;
+  o->prm.cell_rule = params_i[3];
   for (int b = 0; b < MAXBID; ++b) {
     o->bc_kind[b] = bc_kind ? bc_kind[b] : 0;
     o->bc_fn[b] = bc_fn ? bc_fn[b] : 0;
     for (int k = 0; k < 3; ++k) o->bc_c[b][k] = bc_const ? bc_const[3 * b + k] : 0;
   }
   for (int k = 0; k < 8; ++k) o->vortex[k] = vortex ? vortex[k] : 0;
-  for (int p = 1; p < MAXN; ++p) shape_init(&o->sh[p], p);
+  for (int p = 1; p < MAXN; ++p) shape_init(&o->sh[p], p, o->prm.cell_rule);
   for (int p = 1; p < MAXN; ++p) {
     for (int nf = 2; nf <= MAXF; ++nf) {
       double xf[MAXF], wf[MAXF];
@@ -502,7 +505,7 @@ void *oc_oracle_create(int n_cells, const int *degree, const double *vertices, i
     const int p = degree[c];
     o->deg[c] = p;
     o->off[c] = off; off += nd_of(p);
-    o->sdo0[c] = s0; s0 += 5 * nq_of(p) * nq_of(p);
+    o->sdo0[c] = s0; s0 += 5 * o->sh[p].Q * o->sh[p].Q;
     o->sdo1[c] = s1; s1 += (p + 2) * (p + 2);
     o->sdo2[c] = s2; s2 += 2 * (p + 1) * (p + 1);
     const double *v = vertices + 8 * c;
@@ -558,7 +561,7 @@ void *oc_oracle_create(int n_cells, const int *degree, const double *vertices, i
       o->sdof[f] = sf; sf += 2 * o->fnf[f];
       count[cm]++; count[cell_p[f]]++;
     } else {
-      o->fnf[f] = nq_of(degree[cm]);
+      o->fnf[f] = o->sh[degree[cm]].Q;
       o->sdob[f - n_inner] = sb; sb += o->fnf[f];
       count[cm]++;
     }
@@ -1409,7 +1412,7 @@ void oc_oracle_vorticity(void *h, const double *u, int n_q_1d, float *out)
 /* OceanDG.h:2380-2459 compute_errors_hydro with the travelling vortex as the
    exact solution: out[0] = sqrt(sum_cells int (depth(f0, zb) - depth(zeta_h, zb))^2),
    out[1] = sqrt(sum_cells int sum_d (f_{d+1} depth(f0, zb) - q_h,d)^2), on the
-   cell Gauss rule (n_points_1d = floor(1.5 p) + 1), zb from the cell static data
+   cell Gauss rule (n_points_1d points per direction), zb from the cell static data
    (data_quadrature_cell_0, component 0); cells summed in order. */
 void oc_oracle_errors_vortex(void *h, double t, const double *z, const double *q, double *out)
 {

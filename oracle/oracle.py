@@ -83,7 +83,9 @@ class Oracle:
     """FP64 oracle bound to one mesh, parameter set and boundary-condition table."""
 
     def __init__(self, mesh, g=9.81, cu=0.1, nu=0.0, friction=0, max_iter=15, batch=1,
-                 bcs=None, vortex=None):
+                 bcs=None, vortex=None, cell_rule=0):
+        """cell_rule: Gauss points per direction of the cell integrals and boundary
+        faces (the reference's n_points_1d, main.cc:216): 0 floor(1.5 p) + 1, 1 p + 1."""
         L = lib()
         self.mesh = mesh
         bc_kind = np.zeros(16, np.int32)
@@ -103,7 +105,8 @@ class Oracle:
             mesh.subface if mesh.n_inner else np.zeros(1, np.int8),
             mesh.orient if mesh.n_inner else np.zeros(1, np.int8),
             mesh.bid if mesh.n_bnd else np.zeros(1, np.int32),
-            np.array([g, cu, nu], np.float64), np.array([friction, max_iter, batch], np.int32),
+            np.array([g, cu, nu], np.float64),
+            np.array([friction, max_iter, batch, cell_rule], np.int32),
             bc_kind, bc_fn, bc_c, vx)
         self.n = int(L.oc_oracle_n_dofs(self.h))
         self._static = None

@@ -20,13 +20,17 @@ def rel(a, b):
     return np.linalg.norm(a - b) / (n if n > 0 else 1.0)
 
 
-def setup(name, precision="fp64", batch=1, zeta_reference=0.0, reference_state=None):
+def setup(name, precision="fp64", batch=1, zeta_reference=0.0, reference_state=None,
+          cell_quadrature="default"):
+    from oceano_gb300 import _lib
     from oceano_gb300.operator import OceanoOperator
     mesh_f, bcs, pdata, friction = CASES[name]
     mesh = mesh_f()
-    orc = O.Oracle(mesh, friction=friction, bcs=bcs, vortex=VORTEX + [0, 0], batch=batch)
+    orc = O.Oracle(mesh, friction=friction, bcs=bcs, vortex=VORTEX + [0, 0], batch=batch,
+                   cell_rule=_lib.CELL_RULE[cell_quadrature])
     op = OceanoOperator(mesh, friction=["none", "linear", "manning"][friction],
-                        precision=precision, batch_width=batch, zeta_reference=zeta_reference)
+                        precision=precision, batch_width=batch, zeta_reference=zeta_reference,
+                        cell_quadrature=cell_quadrature)
     for b, spec in bcs.items():
         if len(spec) > 1 and spec[1] == "vortex":
             op.set_boundary(b, spec[0], "vortex")

@@ -5,7 +5,9 @@ pinned by properties the reference's scheme must have: free-stream
 preservation (also across hanging faces and degree jumps), the lake at rest to
 machine precision (well-balancing of OceanDG.h's hydrostatic reconstruction),
 global mass conservation of a stage, consistency of the explicit and additive
-stage drivers, and convergence to the analytic travelling vortex.
+stage drivers, and convergence to the analytic travelling vortex.  The
+properties that hold for any cell quadrature are checked for both rules of
+n_points_1d (floor(1.5 p) + 1 and p + 1).
 """
 import numpy as np
 import pytest
@@ -37,11 +39,12 @@ def residuals(orc, z, q, t=0.0):
     return kz[1], kq[0], nz, nq
 
 
+@pytest.mark.parametrize("rule", [0, 1])
 @pytest.mark.parametrize("mesh_f", [lambda: vortex_mesh(0, 1), lambda: vortex_mesh(0, 4),
                                     lambda: hanging_mesh(3), lambda: mixed_degree(hanging_mesh(2))])
-def test_free_stream_preserved(mesh_f):
+def test_free_stream_preserved(mesh_f, rule):
     mesh = mesh_f()
-    orc = O.Oracle(mesh, bcs={0: ("wall",)})
+    orc = O.Oracle(mesh, bcs={0: ("wall",)}, cell_rule=rule)
     z, q = uniform_state(mesh)
     rz, rq, nz, nq = residuals(orc, z, q)
     assert np.abs(rz).max() < 1e-13 and np.abs(rq).max() < 1e-12
@@ -53,11 +56,12 @@ def bump(x, y):
     return np.stack([zb, 0.03 + 0 * x, 0 * x, 0 * x, 0 * x])
 
 
+@pytest.mark.parametrize("rule", [0, 1])
 @pytest.mark.parametrize("degree", [1, 3])
-def test_lake_at_rest(degree):
+def test_lake_at_rest(degree, rule):
     from cases import static_arrays
     mesh = uniform_mesh(8, 4, (0.0, 2.0, 0.0, 1.0), False, degree)
-    orc = O.Oracle(mesh, friction=2, bcs={b: ("wall",) for b in (0, 1, 2)})
+    orc = O.Oracle(mesh, friction=2, bcs={b: ("wall",) for b in (0, 1, 2)}, cell_rule=rule)
     orc.set_static(*static_arrays(orc, bump))
     z, q = uniform_state(mesh, z=0.25, q=(0.0, 0.0))
     rz, rq, nz, nq = residuals(orc, z, q)
@@ -79,10 +83,11 @@ def cell_integrals(mesh, z):
     return tot
 
 
+@pytest.mark.parametrize("rule", [0, 1])
 @pytest.mark.parametrize("mesh_f", [lambda: vortex_mesh(0, 2), lambda: hanging_mesh(2)])
-def test_mass_conserved(mesh_f):
+def test_mass_conserved(mesh_f, rule):
     mesh = mesh_f()
-    orc = O.Oracle(mesh, bcs={0: ("wall",)}, vortex=VORTEX + [0, 0])
+    orc = O.Oracle(mesh, bcs={0: ("wall",)}, vortex=VORTEX + [0, 0], cell_rule=rule)
     z, q = orc.project_vortex(0.0)
     m0 = cell_integrals(mesh, z)
     tb = O.TABLEAUX["ssp33"]
@@ -90,6 +95,25 @@ def test_mass_conserved(mesh_f):
     for it in range(3):
         O.erk_step(orc, tb["a"], tb["b"], tb["c"], it * dt, dt, z, q)
     assert abs(cell_integrals(mesh, z) - m0) < 1e-13 * abs(m0)
+
+
+def test_cell_rules_coincide_at_degree_1_and_differ_at_3():
+    """floor(1.5 p) + 1 = p + 1 at p = 1: the two rules give the same stage; at
+    p = 3 (5 against 4 points) the nonlinear flux integrals differ, the static
+    data sizes follow the rule (5 values per cell point, one per boundary point)."""
+    for degree, same in ((1, True), (3, False)):
+        mesh = vortex_mesh(0, degree)
+        out = []
+        for rule in (0, 1):
+            orc = O.Oracle(mesh, bcs={0: ("wall",)}, vortex=VORTEX + [0, 0], cell_rule=rule)
+            z, q = orc.project_vortex(0.0)
+            out.append((residuals(orc, z, q), orc.static_sizes()))
+        (r0, s0), (r1, s1) = out
+        nq0, nq1 = 3 * degree // 2 + 1, degree + 1
+        assert s0[0] == 5 * nq0 * nq0 * mesh.n_cells and s1[0] == 5 * nq1 * nq1 * mesh.n_cells
+        assert s0[4] == nq0 * mesh.n_bnd and s1[4] == nq1 * mesh.n_bnd
+        d = max(np.abs(r1[0] - r0[0]).max(), np.abs(r1[3] - r0[3]).max())  # L_h zeta, q^{n+1}
+        assert (d == 0.0) if same else (d > 1e-10), (degree, d)
 
 
 def test_erk_ark_same_height_residual():
