@@ -29,50 +29,9 @@ constexpr int OW1 = 0, OB1 = OW1 + NH * NF, OW2 = OB1 + NH, OB2 = OW2 + NH * NH,
               OB3 = OW3 + NH;
 static_assert(OB3 + 1 == NP, "parameter layout");
 
-constexpr int kThreads = 128;      // samples per tile = threads per block
 constexpr int kGradBlocks = 304;   // persistent gradient grid (2 per SM)
 
 __device__ __forceinline__ float bf(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
-
-// Weights as FP32 values of their BF16 roundings, biases FP32, normalisation.
-struct SmemWeights {
-  float w1[NH * NF], b1[NH], w2[NH * NH], b2[NH], w3[NH], b3, mean[NF], istd[NF];
-};
-
-__device__ void load_weights(SmemWeights &s, const float *w, const float *norm) {
-  for (int i = threadIdx.x; i < NH * NF; i += blockDim.x) s.w1[i] = bf(w[OW1 + i]);
-  for (int i = threadIdx.x; i < NH * NH; i += blockDim.x) s.w2[i] = bf(w[OW2 + i]);
-  for (int i = threadIdx.x; i < NH; i += blockDim.x) {
-    s.b1[i] = w[OB1 + i];
-    s.b2[i] = w[OB2 + i];
-    s.w3[i] = bf(w[OW3 + i]);
-  }
-  for (int i = threadIdx.x; i < NF; i += blockDim.x) {
-    s.mean[i] = norm[i];
-    s.istd[i] = norm[NF + i];
-  }
-  if (threadIdx.x == 0) s.b3 = w[OB3];
-}
-
-// normalised, BF16-rounded input and first hidden layer of one sample
-__device__ __forceinline__ void layer1(const SmemWeights &s, const float *x, float *xh, float *h1) {
-#pragma unroll
-  for (int i = 0; i < NF; ++i) xh[i] = bf((x[i] - s.mean[i]) * s.istd[i]);
-#pragma unroll
-  for (int k = 0; k < NH; ++k) {
-    float a = s.b1[k];
-#pragma unroll
-    for (int i = 0; i < NF; ++i) a = fmaf(s.w1[k * NF + i], xh[i], a);
-    h1[k] = bf(fmaxf(a, 0.f));
-  }
-}
-
-__device__ __forceinline__ float layer2_row(const SmemWeights &s, const float *h1, int j) {
-  float a = s.b2[j];
-#pragma unroll
-  for (int k = 0; k < NH; ++k) a = fmaf(s.w2[j * NH + k], h1[k], a);
-  return bf(fmaxf(a, 0.f));
-}
 
 // ---------------------------------------------------------------------------
 // Forward pass on the BF16 tensor cores (mma.sync m16n8k16, FP32 accumulation).
@@ -186,122 +145,323 @@ __global__ void __launch_bounds__(32 * kMmaWarps) mlp_forward_mma_kernel(
   }
 }
 
-// Per-tile activations of the gradient kernel (one row per sample).
-struct SmemTile {
-  float xh[kThreads][NF + 1];
-  float h1[kThreads][NH + 1];
-  float h2[kThreads][NH + 1];
-  float d2[kThreads][NH + 1];  // dL/da2
-  float d1[kThreads][NH + 1];  // dL/da1
-  float dz[kThreads];
+// ---------------------------------------------------------------------------
+// Gradient on the BF16 tensor cores (mma.sync m16n8k16, FP32 accumulation).
+// A block of 4 warps takes 64 samples per tile.
+// Phase 1, warp w on samples 16w .. 16w+15 of the tile: the forward pass as in
+// mlp_forward_mma_kernel, the loss and dz = dL/dz, d2 = [h2 > 0] dz w3 and
+// d1 = [h1 > 0] W2^T d2 (MMAs: d2 as A operand, W2 as B; the accumulator
+// fragments of d2 are the A fragments, as in the forward pass).  The
+// back-propagated signals enter every MMA as two BF16 terms, hi = bf16(d) and
+// lo = bf16(d - hi), which keeps about 16 bits of their FP32 values; xh, h1
+// and the BF16 weights are exact in BF16.  Phase 1 leaves xh, h1, d2 and d1
+// transposed in shared memory ([column][sample], rows padded against bank
+// conflicts).  Phase 2, warp w owning rows 16w .. 16w+15 of dW2 and of dW1:
+// dW2 += d2^T h1 and dW1 += d1^T xh over the tile's 64 samples (4 k-steps of
+// 16), accumulators in registers across the block's tiles.  Bias, w3 and b3
+// sums come from phase 1's registers.  The block's partial gradient and loss go
+// to part[block][NP + 1] (summed in a fixed order by mlp_reduce_kernel).
+// ---------------------------------------------------------------------------
+constexpr int kGradWarps = 4;
+constexpr int kTile = 16 * kGradWarps;  // samples per block tile
+constexpr int kTS = kTile + 8;          // row stride (BF16) of the transposed buffers
+
+struct GradSmem {
+  uint32_t B1[8][2][32];      // layer-1 B fragments (per lane)
+  uint32_t B2[4][8][2][32];   // layer-2 B fragments: W2^T
+  uint32_t BW2[4][8][2][32];  // back-propagation B fragments: W2
+  __nv_bfloat16 xhT[16][kTS];  // [feature (12 + padding)][sample]
+  __nv_bfloat16 h1T[NH][kTS];
+  __nv_bfloat16 d2T[2][NH][kTS];  // hi, lo
+  __nv_bfloat16 d1T[2][NH][kTS];
+  float bias1[NH], bias2[NH], w3[NH];  // w3 rounded to BF16
+  float colsum[kGradWarps][3][NH];  // per warp: d1, d2 and dz h2 column sums
+  float b3sum[kGradWarps];
+  double loss[kGradWarps];
 };
 
-// Persistent gradient kernel: each block walks tiles of kThreads samples;
-// thread t owns parameter entries e = t + kThreads * r and accumulates their
-// sums over the tiles in registers; the block's partial gradient and loss go
-// to part[block][NP + 1] (summed in a fixed order by mlp_reduce_kernel).
-constexpr int kOwn = (NP + kThreads - 1) / kThreads;
+__device__ __forceinline__ uint32_t ld_pair(const __nv_bfloat16 *p) {
+  return *reinterpret_cast<const uint32_t *>(p);
+}
 
-__global__ void __launch_bounds__(kThreads, 1) mlp_grad_kernel(const float *w, const float *norm,
-                                                                const float *feat,
-                                                                const float *label, int64_t n,
-                                                                float pos_weight, float inv_n,
-                                                                float *part) {
+// hi and lo BF16 terms of v (v ~= hi + lo)
+__device__ __forceinline__ void split_bf16(float v, float &hi, float &lo) {
+  hi = bf(v);
+  lo = bf(v - hi);
+}
+
+__global__ void __launch_bounds__(32 * kGradWarps) mlp_grad_mma_kernel(
+    const float *w, const float *norm, const float *feat, const float *label, int64_t n,
+    float pos_weight, float inv_n, float *part) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemWeights &s = *reinterpret_cast<SmemWeights *>(smem_raw);
-  SmemTile &T = *reinterpret_cast<SmemTile *>(smem_raw + ((sizeof(SmemWeights) + 15) / 16) * 16);
-  load_weights(s, w, norm);
-  const int t = threadIdx.x;
-  float acc[kOwn];
+  GradSmem &S = *reinterpret_cast<GradSmem *>(smem_raw);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
+  // B fragments (the lane's entries), as in the forward kernel; BW2: B[k = j][n = k']
+  // = W2[j][k'], rows j = 16kk + 2t (+1 | +8, +9), column k' = 8nk + g
+  for (int idx = warp; idx < 8; idx += kGradWarps) {
+    const int j = idx;
+    const float *r1 = w + OW1 + (8 * j + g) * NF;
+    S.B1[j][0][lane] = pack_bf16(r1[2 * t], r1[2 * t + 1]);
+    S.B1[j][1][lane] = t < 2 ? pack_bf16(r1[2 * t + 8], r1[2 * t + 9]) : 0u;
+    const float *r2 = w + OW2 + (8 * j + g) * NH;
+    for (int kk = 0; kk < 4; ++kk) {
+      S.B2[kk][j][0][lane] = pack_bf16(r2[16 * kk + 2 * t], r2[16 * kk + 2 * t + 1]);
+      S.B2[kk][j][1][lane] = pack_bf16(r2[16 * kk + 2 * t + 8], r2[16 * kk + 2 * t + 9]);
+      const float *c2 = w + OW2 + 8 * j + g;  // column 8j + g of W2, rows j'
+      S.BW2[kk][j][0][lane] =
+          pack_bf16(c2[(16 * kk + 2 * t) * NH], c2[(16 * kk + 2 * t + 1) * NH]);
+      S.BW2[kk][j][1][lane] =
+          pack_bf16(c2[(16 * kk + 2 * t + 8) * NH], c2[(16 * kk + 2 * t + 9) * NH]);
+    }
+  }
+  for (int e = threadIdx.x; e < 4 * kTS; e += blockDim.x)  // feature rows 12..15 stay 0
+    S.xhT[12 + e / kTS][e % kTS] = __float2bfloat16_rn(0.f);
+  for (int c = threadIdx.x; c < NH; c += blockDim.x) {
+    S.bias1[c] = w[OB1 + c];
+    S.bias2[c] = w[OB2 + c];
+    S.w3[c] = bf(w[OW3 + c]);
+  }
+  const float b3 = w[OB3];
+  const int fc[4] = {2 * t, 2 * t + 1, 2 * t + 8, 2 * t + 9};
+  float mu[4], is[4];
 #pragma unroll
-  for (int r = 0; r < kOwn; ++r) acc[r] = 0.f;
+  for (int e = 0; e < 4; ++e) {
+    mu[e] = fc[e] < NF ? norm[fc[e]] : 0.f;
+    is[e] = fc[e] < NF ? norm[NF + fc[e]] : 0.f;
+  }
+  float acc2[8][4], acc1[2][4];  // dW2 rows 16w + g (+8) x 64; dW1 rows 16w + g (+8) x 16
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) acc2[j][e] = 0.f;
+#pragma unroll
+  for (int j = 0; j < 2; ++j)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) acc1[j][e] = 0.f;
+  float sd1[8][2], sd2[8][2], sw3[8][2], sb3 = 0.f;  // column sums of rows g and g + 8
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+#pragma unroll
+    for (int e = 0; e < 2; ++e) sd1[j][e] = sd2[j][e] = sw3[j][e] = 0.f;
   double loss = 0.0;
   __syncthreads();
-  const int64_t tiles = (n + kThreads - 1) / kThreads;
+
+  const int64_t tiles = (n + kTile - 1) / kTile;
   for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    const int64_t c = tile * kThreads + t;
-    const bool ok = c < n;
-    // forward, keeping the activations of the tile
-    {
-      float x[NF], xh[NF], h1[NH];
+    // ---- phase 1: warp w, samples s0 = 16w + g and s1 = s0 + 8 of the tile
+    const int s0 = 16 * warp + g, s1 = s0 + 8;
+    const int64_t r0 = tile * kTile + s0, r1 = tile * kTile + s1;
+    float x0[4], x1[4];
 #pragma unroll
-      for (int i = 0; i < NF; ++i) x[i] = ok ? feat[c * NF + i] : 0.f;
-      layer1(s, x, xh, h1);
-#pragma unroll
-      for (int i = 0; i < NF; ++i) T.xh[t][i] = xh[i];
-#pragma unroll
-      for (int k = 0; k < NH; ++k) T.h1[t][k] = h1[k];
-      float z = s.b3;
-#pragma unroll 1
-      for (int j = 0; j < NH; ++j) {
-        const float h2 = layer2_row(s, h1, j);
-        T.h2[t][j] = h2;
-        z = fmaf(s.w3[j], h2, z);
+    for (int e = 0; e < 4; ++e) {
+      const bool col = fc[e] < NF;
+      x0[e] = (col && r0 < n) ? bf((feat[r0 * NF + fc[e]] - mu[e]) * is[e]) : 0.f;
+      x1[e] = (col && r1 < n) ? bf((feat[r1 * NF + fc[e]] - mu[e]) * is[e]) : 0.f;
+      if (col) {
+        S.xhT[fc[e]][s0] = __float2bfloat16_rn(x0[e]);
+        S.xhT[fc[e]][s1] = __float2bfloat16_rn(x1[e]);
       }
-      // weighted BCE with logits: wt * (softplus(z) - y z); dL/dz = wt (sigmoid(z) - y) / n
-      const float y = ok ? label[c] : 0.f;
+    }
+    const uint32_t a0 = pack_bf16(x0[0], x0[1]), a1 = pack_bf16(x1[0], x1[1]);
+    const uint32_t a2 = pack_bf16(x0[2], x0[3]), a3 = pack_bf16(x1[2], x1[3]);
+    uint32_t H[4][4];
+    uint32_t m1 = 0u;  // h1 > 0: bit 4j + e (e: c0..c3 of n-tile j)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const float ba = S.bias1[8 * j + 2 * t], bb = S.bias1[8 * j + 2 * t + 1];
+      float c[4] = {ba, bb, ba, bb};
+      mma_bf16(c, a0, a1, a2, a3, S.B1[j][0][lane], S.B1[j][1][lane]);
+      float h[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        h[e] = bf(fmaxf(c[e], 0.f));
+        m1 |= (h[e] > 0.f ? 1u : 0u) << (4 * j + e);
+      }
+      H[j >> 1][(j & 1) * 2 + 0] = pack_bf16(h[0], h[1]);
+      H[j >> 1][(j & 1) * 2 + 1] = pack_bf16(h[2], h[3]);
+      const int col = 8 * j + 2 * t;
+      S.h1T[col][s0] = __float2bfloat16_rn(h[0]);
+      S.h1T[col + 1][s0] = __float2bfloat16_rn(h[1]);
+      S.h1T[col][s1] = __float2bfloat16_rn(h[2]);
+      S.h1T[col + 1][s1] = __float2bfloat16_rn(h[3]);
+    }
+    float h2[8][4], z0 = 0.f, z1 = 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const float ba = S.bias2[8 * j + 2 * t], bb = S.bias2[8 * j + 2 * t + 1];
+      float c[4] = {ba, bb, ba, bb};
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk)
+        mma_bf16(c, H[kk][0], H[kk][1], H[kk][2], H[kk][3], S.B2[kk][j][0][lane],
+                 S.B2[kk][j][1][lane]);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) h2[j][e] = bf(fmaxf(c[e], 0.f));
+      const float wa = S.w3[8 * j + 2 * t], wb = S.w3[8 * j + 2 * t + 1];
+      z0 = fmaf(wa, h2[j][0], z0);
+      z0 = fmaf(wb, h2[j][1], z0);
+      z1 = fmaf(wa, h2[j][2], z1);
+      z1 = fmaf(wb, h2[j][3], z1);
+    }
+    z0 += __shfl_xor_sync(0xffffffffu, z0, 1);
+    z0 += __shfl_xor_sync(0xffffffffu, z0, 2);
+    z1 += __shfl_xor_sync(0xffffffffu, z1, 1);
+    z1 += __shfl_xor_sync(0xffffffffu, z1, 2);
+    z0 += b3;
+    z1 += b3;
+    // weighted BCE with logits: wt (softplus(z) - y z); dL/dz = wt (sigmoid(z) - y) / n
+    float dz[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int64_t r = h ? r1 : r0;
+      const float z = h ? z1 : z0;
+      const bool ok = r < n;
+      const float y = ok ? label[r] : 0.f;
       const float wt = ok ? (y > 0.5f ? pos_weight : 1.f) : 0.f;
-      const float sp = fmaxf(z, 0.f) + log1pf(expf(-fabsf(z)));
-      loss += (double)(wt * (sp - y * z));
-      const float sg = 1.f / (1.f + expf(-z));
-      const float dz = wt * (sg - y) * inv_n;
-      T.dz[t] = dz;
-#pragma unroll 1
-      for (int j = 0; j < NH; ++j) T.d2[t][j] = T.h2[t][j] > 0.f ? dz * s.w3[j] : 0.f;
+      if (t == 0) loss += (double)(wt * (fmaxf(z, 0.f) + log1pf(expf(-fabsf(z))) - y * z));
+      dz[h] = wt * (1.f / (1.f + expf(-z)) - y) * inv_n;
+    }
+    if (t == 0) sb3 += dz[0] + dz[1];
+    // d2 = [h2 > 0] dz w3 (accumulator layout), its A fragments (hi, lo) and its
+    // transposed copy for phase 2
+    uint32_t D2[2][4][4];
 #pragma unroll
-      for (int k = 0; k < NH; ++k) {  // dL/da1 = [h1 > 0] W2^T dL/da2
-        float a = 0.f;
-#pragma unroll 1
-        for (int j = 0; j < NH; ++j) a = fmaf(s.w2[j * NH + k], T.d2[t][j], a);
-        T.d1[t][k] = h1[k] > 0.f ? a : 0.f;
+    for (int j = 0; j < 8; ++j) {
+      float hi[4], lo[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float d = h2[j][e] > 0.f ? dz[e >> 1] * S.w3[8 * j + 2 * t + (e & 1)] : 0.f;
+        sd2[j][e & 1] += d;
+        sw3[j][e & 1] += dz[e >> 1] * h2[j][e];
+        split_bf16(d, hi[e], lo[e]);
+      }
+      D2[0][j >> 1][(j & 1) * 2 + 0] = pack_bf16(hi[0], hi[1]);
+      D2[0][j >> 1][(j & 1) * 2 + 1] = pack_bf16(hi[2], hi[3]);
+      D2[1][j >> 1][(j & 1) * 2 + 0] = pack_bf16(lo[0], lo[1]);
+      D2[1][j >> 1][(j & 1) * 2 + 1] = pack_bf16(lo[2], lo[3]);
+      const int col = 8 * j + 2 * t;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int cc = col + (e & 1), ss = (e >> 1) ? s1 : s0;
+        S.d2T[0][cc][ss] = __float2bfloat16_rn(hi[e]);
+        S.d2T[1][cc][ss] = __float2bfloat16_rn(lo[e]);
+      }
+    }
+    // d1 = [h1 > 0] W2^T d2
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+        for (int p = 0; p < 2; ++p)
+          mma_bf16(c, D2[p][kk][0], D2[p][kk][1], D2[p][kk][2], D2[p][kk][3],
+                   S.BW2[kk][j][0][lane], S.BW2[kk][j][1][lane]);
+      const int col = 8 * j + 2 * t;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float d = ((m1 >> (4 * j + e)) & 1u) ? c[e] : 0.f;
+        sd1[j][e & 1] += d;
+        float hi, lo;
+        split_bf16(d, hi, lo);
+        const int cc = col + (e & 1), ss = (e >> 1) ? s1 : s0;
+        S.d1T[0][cc][ss] = __float2bfloat16_rn(hi);
+        S.d1T[1][cc][ss] = __float2bfloat16_rn(lo);
       }
     }
     __syncthreads();
-    // parameter sums over the tile's samples
-    const int64_t left = n - tile * kThreads;
-    const int cnt = left < kThreads ? (int)left : kThreads;  // samples in the tile
+    // ---- phase 2: warp w owns rows 16w + g, 16w + g + 8 of dW2 (j) and dW1 (k)
+    const int ra = 16 * warp + g, rb = ra + 8;
 #pragma unroll
-    for (int r = 0; r < kOwn; ++r) {
-      const int e = t + kThreads * r;
-      if (e >= NP) break;
-      float v = 0.f;
-      if (e < OB1) {
-        const int k = e / NF, i = e - k * NF;
-        for (int q = 0; q < cnt; ++q) v = fmaf(T.d1[q][k], T.xh[q][i], v);
-      } else if (e < OW2) {
-        const int k = e - OB1;
-        for (int q = 0; q < cnt; ++q) v += T.d1[q][k];
-      } else if (e < OB2) {
-        const int j = (e - OW2) / NH, k = (e - OW2) - j * NH;
-        for (int q = 0; q < cnt; ++q) v = fmaf(T.d2[q][j], T.h1[q][k], v);
-      } else if (e < OW3) {
-        const int j = e - OB2;
-        for (int q = 0; q < cnt; ++q) v += T.d2[q][j];
-      } else if (e < OB3) {
-        const int j = e - OW3;
-        for (int q = 0; q < cnt; ++q) v = fmaf(T.dz[q], T.h2[q][j], v);
-      } else {
-        for (int q = 0; q < cnt; ++q) v += T.dz[q];
+    for (int ks = 0; ks < kGradWarps; ++ks) {  // samples 16 ks .. 16 ks + 15
+      const int sc = 16 * ks + 2 * t;
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        const uint32_t e0 = ld_pair(&S.d2T[p][ra][sc]), e1 = ld_pair(&S.d2T[p][rb][sc]);
+        const uint32_t e2 = ld_pair(&S.d2T[p][ra][sc + 8]), e3 = ld_pair(&S.d2T[p][rb][sc + 8]);
+#pragma unroll
+        for (int nk = 0; nk < 8; ++nk)
+          mma_bf16(acc2[nk], e0, e1, e2, e3, ld_pair(&S.h1T[8 * nk + g][sc]),
+                   ld_pair(&S.h1T[8 * nk + g][sc + 8]));
+        const uint32_t f0 = ld_pair(&S.d1T[p][ra][sc]), f1 = ld_pair(&S.d1T[p][rb][sc]);
+        const uint32_t f2 = ld_pair(&S.d1T[p][ra][sc + 8]), f3 = ld_pair(&S.d1T[p][rb][sc + 8]);
+#pragma unroll
+        for (int ni = 0; ni < 2; ++ni)
+          mma_bf16(acc1[ni], f0, f1, f2, f3, ld_pair(&S.xhT[8 * ni + g][sc]),
+                   ld_pair(&S.xhT[8 * ni + g][sc + 8]));
       }
-      acc[r] += v;
     }
     __syncthreads();
   }
+  // ---- block partial gradient: dW2, dW1 from the accumulators; column sums over
+  // the lanes of equal t (shuffles across g), then over the warps in order
   float *out = part + (int64_t)blockIdx.x * (NP + 1);
+  const int ra = 16 * warp + g, rb = ra + 8;
 #pragma unroll
-  for (int r = 0; r < kOwn; ++r) {
-    const int e = t + kThreads * r;
-    if (e < NP) out[e] = acc[r];
+  for (int nk = 0; nk < 8; ++nk)
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      out[OW2 + ra * NH + 8 * nk + 2 * t + e] = acc2[nk][e];
+      out[OW2 + rb * NH + 8 * nk + 2 * t + e] = acc2[nk][2 + e];
+    }
+#pragma unroll
+  for (int ni = 0; ni < 2; ++ni)
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int i = 8 * ni + 2 * t + e;
+      if (i < NF) {
+        out[OW1 + ra * NF + i] = acc1[ni][e];
+        out[OW1 + rb * NF + i] = acc1[ni][2 + e];
+      }
+    }
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      float v1 = sd1[j][e], v2 = sd2[j][e], v3 = sw3[j][e];
+#pragma unroll
+      for (int o = 4; o < 32; o <<= 1) {
+        v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+        v2 += __shfl_xor_sync(0xffffffffu, v2, o);
+        v3 += __shfl_xor_sync(0xffffffffu, v3, o);
+      }
+      if (g == 0) {
+        const int col = 8 * j + 2 * t + e;
+        S.colsum[warp][0][col] = v1;
+        S.colsum[warp][1][col] = v2;
+        S.colsum[warp][2][col] = v3;
+      }
+    }
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    sb3 += __shfl_xor_sync(0xffffffffu, sb3, o);
+    loss += __shfl_xor_sync(0xffffffffu, loss, o);
   }
-  // block loss: the samples' terms summed over the threads
-  __shared__ double red[kThreads];
-  red[t] = loss;
+  if (lane == 0) {
+    S.b3sum[warp] = sb3;
+    S.loss[warp] = loss;
+  }
   __syncthreads();
-  for (int h = kThreads / 2; h > 0; h >>= 1) {
-    if (t < h) red[t] += red[t + h];
-    __syncthreads();
+  for (int c = threadIdx.x; c < NH; c += blockDim.x) {
+    float v1 = 0.f, v2 = 0.f, v3 = 0.f;
+    for (int q = 0; q < kGradWarps; ++q) {
+      v1 += S.colsum[q][0][c];
+      v2 += S.colsum[q][1][c];
+      v3 += S.colsum[q][2][c];
+    }
+    out[OB1 + c] = v1;
+    out[OB2 + c] = v2;
+    out[OW3 + c] = v3;
   }
-  if (t == 0) out[NP] = (float)red[0];
+  if (threadIdx.x == 0) {
+    float vb = 0.f;
+    double vl = 0.0;
+    for (int q = 0; q < kGradWarps; ++q) {
+      vb += S.b3sum[q];
+      vl += S.loss[q];
+    }
+    out[OB3] = vb;
+    out[NP] = (float)vl;
+  }
 }
 
 __global__ void mlp_reduce_kernel(const float *part, int nb, float *grad, double *loss) {
@@ -368,9 +528,7 @@ struct oc_mlp {
     }                                                                         \
   } while (0)
 
-static size_t grad_smem() {
-  return ((sizeof(SmemWeights) + 15) / 16) * 16 + sizeof(SmemTile);
-}
+static size_t grad_smem() { return sizeof(GradSmem); }
 
 // splitmix64 (Steele, Lea, Flood 2014) for the seeded initialisation
 static uint64_t splitmix64(uint64_t &x) {
@@ -395,7 +553,7 @@ oc_status oc_mlp_create(uint64_t seed, oc_mlp **out) {
   MLP_TRY(cudaMalloc((void **)&m->d_part, (size_t)kGradBlocks * (NP + 1) * 4));
   MLP_TRY(cudaMalloc((void **)&m->d_loss, 8));
   MLP_TRY(cudaMalloc((void **)&m->d_stats, 2 * NF * 8));
-  MLP_TRY(cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  MLP_TRY(cudaFuncSetAttribute(mlp_grad_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)grad_smem()));
   // He-uniform weights U(-sqrt(6/fan_in), +sqrt(6/fan_in)), zero biases
   std::vector<float> w(NP, 0.f);
@@ -496,9 +654,9 @@ oc_status oc_mlp_forward(oc_mlp *m, const float *features, int64_t n, float *log
 oc_status oc_mlp_gradient(oc_mlp *m, const float *features, const float *labels, int64_t n,
                           float pos_weight, float *grad, double *loss) {
   if (!m || !features || !labels || n <= 0) return OC_ERR_INVALID_ARG;
-  const int64_t tiles = (n + kThreads - 1) / kThreads;
+  const int64_t tiles = (n + kTile - 1) / kTile;
   const int grid = (int)std::min<int64_t>(kGradBlocks, tiles);
-  mlp_grad_kernel<<<grid, kThreads, grad_smem(), m->stream>>>(
+  mlp_grad_mma_kernel<<<grid, 32 * kGradWarps, grad_smem(), m->stream>>>(
       m->d_w, m->d_norm, features, labels, n, pos_weight, (float)(1.0 / (double)n), m->d_part);
   MLP_TRY(cudaGetLastError());
   mlp_reduce_kernel<<<(NP + 1 + 255) / 256, 256, 0, m->stream>>>(m->d_part, grid, m->d_g,

@@ -87,14 +87,15 @@ def _bf16_boundary_distance(v):
     return 0.5 * ulp - np.abs(v - b)
 
 
-def forward_tensor_core(params, norm, X, margin=1e-6):
+def forward_tensor_core(params, norm, X, margin=1e-6, activations=False):
     """The forward pass of the tensor-core kernel: BF16 weights, inputs and
     activations as forward(), each layer's sum of exact BF16 products formed
     at FP32 precision or better (here exactly, in FP64) before the BF16
     rounding.  Returns (logits, flip_prone): flip_prone marks the samples with
     a hidden activation whose exact value lies within `margin` x (sum of
     |terms|) of a BF16 rounding boundary, where a different summation order of
-    the hardware may round the activation to the neighbouring BF16 value."""
+    the hardware may round the activation to the neighbouring BF16 value.
+    activations=True also returns (xh, h1, h2)."""
     W1, b1, W2, b2, w3, b3 = unpack(params)
     mean, istd = np.asarray(norm[:NF]), np.asarray(norm[NF:])
     W1b, W2b, w3b = (bf16(a).astype(f64) for a in (W1, W2, w3))
@@ -113,13 +114,20 @@ def forward_tensor_core(params, norm, X, margin=1e-6):
     h1, p1 = layer(xh, W1b, b1)
     h2, p2 = layer(h1, W2b, b2)
     z = h2 @ w3b + f64(b3)
+    if activations:
+        return z, p1 | p2, (xh, h1, h2)
     return z, p1 | p2
 
 
-def loss_and_grad(params, norm, X, y, pos_weight, exact=False):
-    """Mean weighted BCE-with-logits and its gradient (FP64 accumulation)."""
+def loss_and_grad(params, norm, X, y, pos_weight, exact=False, tensor_core=False):
+    """Mean weighted BCE-with-logits and its gradient (FP64 accumulation).
+    tensor_core=True takes the activations of forward_tensor_core (the GPU's
+    tensor-core forward pass; compare on samples that are not flip-prone)."""
     W1, b1, W2, b2, w3, b3 = unpack(params)
-    z, (xh, h1, h2) = forward(params, norm, X, exact)
+    if tensor_core:
+        z, _, (xh, h1, h2) = forward_tensor_core(params, norm, X, activations=True)
+    else:
+        z, (xh, h1, h2) = forward(params, norm, X, exact)
     z, xh, h1, h2 = (np.asarray(a, f64) for a in (z, xh, h1, h2))
     if not exact:  # the GPU multiplies by the BF16 weights in the backward pass as well
         W2, w3 = bf16(W2).astype(f64), bf16(w3).astype(f64)

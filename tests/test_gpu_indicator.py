@@ -90,11 +90,19 @@ def test_mlp_forward_matches_oracle(gpu_lib, n):
 
 @pytest.mark.parametrize("n", [100, 1000, 70000])
 def test_mlp_gradient_matches_oracle(gpu_lib, n):
+    """The tensor-core gradient (forward, back-propagation and parameter sums on
+    BF16 MMAs, back-propagated signals as two BF16 terms) against the oracle's
+    gradient over the tensor-core forward's activations, on the samples that are
+    not flip-prone (a different summation order may round a hidden activation
+    of those to the neighbouring BF16 value): loss 1e-5, gradient 1e-4 of its
+    norm (the two-term signals keep about 16 bits)."""
     import torch
     p, norm, X, y = random_net(2, n)
+    _, prone = IO.forward_tensor_core(p, norm, X)
+    X, y = np.ascontiguousarray(X[~prone]), np.ascontiguousarray(y[~prone])
     m = model_with(p, norm)
     loss, g = m.gradient(torch.from_numpy(X).cuda(), torch.from_numpy(y).cuda(), 3.0)
-    lo, go = IO.loss_and_grad(p, norm, X, y, 3.0)
+    lo, go = IO.loss_and_grad(p, norm, X, y, 3.0, tensor_core=True)
     assert abs(loss - lo) <= 1e-5 * abs(lo)
     assert np.linalg.norm(g - go) <= 1e-4 * np.linalg.norm(go)
 

@@ -131,3 +131,14 @@ def test_degree_transfer_round_trip_and_conservation():
     assert np.allclose(z2.reshape(nc, 9) @ w2, zc.reshape(nc, 4) @ w1, atol=1e-13)
     qa, qb2 = q2.reshape(nc, 2, 9), qc.reshape(nc, 2, 4)
     assert np.allclose(qa @ w2, qb2 @ w1, atol=1e-13)
+
+
+def test_tensor_core_gradient_close_to_the_fp32_order_one():
+    """The gradient over the tensor-core forward's activations (what the GPU's
+    tensor-core gradient is checked against) and over the FP32-order forward
+    agree up to the activations' BF16 rounding differences."""
+    p, norm, X, y = random_net(4)
+    l0, g0 = IO.loss_and_grad(p, norm, X, y, 3.0)
+    l1, g1 = IO.loss_and_grad(p, norm, X, y, 3.0, tensor_core=True)
+    assert abs(l1 - l0) <= 1e-3 * abs(l0)
+    assert np.linalg.norm(g1 - g0) <= 2e-2 * np.linalg.norm(g0)
