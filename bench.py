@@ -621,6 +621,22 @@ def run_indicator(args):
     e1.synchronize()
     t_fwd = e0.elapsed_time(e1) / 1e3 / reps
     flops_fwd = 2 * (12 * 64 + 64 * 64 + 64)
+    # gradient kernels alone (forward, back-propagation W2^T d2 and the parameter
+    # sums d2^T h1, d1^T xh on the tensor cores, then the fixed-order block
+    # reduction) on the first 2^20 training samples; no host copy in the loop
+    ng = min(int(X.shape[0]), 1 << 20)
+    Xg, Yg = X[:ng].contiguous(), Y[:ng].contiguous()
+    for _ in range(3):
+        oclib().oc_mlp_gradient(model.h, C.c_void_p(Xg.data_ptr()), C.c_void_p(Yg.data_ptr()),
+                                ng, C.c_float(pos), None, None)
+    e0.record(stream)
+    for _ in range(reps):
+        oclib().oc_mlp_gradient(model.h, C.c_void_p(Xg.data_ptr()), C.c_void_p(Yg.data_ptr()),
+                                ng, C.c_float(pos), None, None)
+    e1.record(stream)
+    e1.synchronize()
+    t_grad = e0.elapsed_time(e1) / 1e3 / reps
+    flops_grad = flops_fwd + 2 * (64 * 64 + 64 * 64 + 64 * 12)  # + W2^T d2, d2^T h1, d1^T xh
     # remeshing runs: 16 independent members (own mesh, operator and time step),
     # p-adaptive degree map (1 outside / 2 inside the refined set) with state
     # transfer, 40 steps, under the three policies
@@ -647,6 +663,11 @@ def run_indicator(args):
                              "kernel": "mlp_forward_mma_kernel (mma.sync m16n8k16 bf16)",
                              "flop_per_cell": flops_fwd},
         "train_samples_per_s": X.shape[0] * INDICATOR_EPOCHS / t_train,
+        "gradient_kernel": {"samples_per_s": ng / t_grad, "tflops": ng * flops_grad / t_grad / 1e12,
+                            "frac_of_bf16_peak": ng * flops_grad / t_grad / 1e12 / bf16_peak(),
+                            "flop_per_sample": flops_grad, "samples": ng,
+                            "kernel": "mlp_grad_mma_kernel (mma.sync m16n8k16 bf16; "
+                                      "back-propagated signals as two BF16 terms)"},
         "loss_first_last": [losses[0], losses[-1]],
         "eval": res,
         "remesh_runs": remesh,
