@@ -1141,8 +1141,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         for (int k = 0; k < (Q > OC_MAXF ? Q : OC_MAXF); ++k) {  // nfo <= max(Q, OC_MAXF)
           if (k < nfo) {
             const R l = __ldg(col + k * OC_MAXN);
-            cz += l * FV[k];
-            c0 += l * FV[FVS + k];
+            fma2(cz, c0, l, FV[k], l, FV[FVS + k]);
             c1 += l * FV[2 * FVS + k];
           }
         }
@@ -1478,12 +1477,10 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 #pragma unroll
             for (int i = 0; i < N; ++i) {
               const int d = fbase + i * fstride;
-              zo_ += lo[i] * U[d];
-              qo0 += lo[i] * U[NN + d];
-              qo1 += lo[i] * U[2 * NN + d];
-              zn += ln[i] * NB[(sl * 3 + 0) * OC_MAXN + i];
-              qn0 += ln[i] * NB[(sl * 3 + 1) * OC_MAXN + i];
-              qn1 += ln[i] * NB[(sl * 3 + 2) * OC_MAXN + i];
+              fma2(zo_, qo0, lo[i], U[d], lo[i], U[NN + d]);
+              fma2(qo1, zn, lo[i], U[2 * NN + d], ln[i], NB[(sl * 3 + 0) * OC_MAXN + i]);
+              fma2(qn0, qn1, ln[i], NB[(sl * 3 + 1) * OC_MAXN + i], ln[i],
+                   NB[(sl * 3 + 2) * OC_MAXN + i]);
             }
             const R zm = side ? zn : zo_, qm0 = side ? qn0 : qo0, qm1 = side ? qn1 : qo1;
             const R zp = side ? zo_ : zn, qp0 = side ? qo0 : qn0, qp1 = side ? qo1 : qn1;
@@ -1519,8 +1516,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           for (int i = 0; i < N; ++i) {  // own trace
             const int d = face_dof(N, fo, i);
             const R l = __ldg(&tbg.F[tsel][nf][ko][i]);
-            zo_ += l * U[d];
-            qo0 += l * U[NN + d];
+            fma2(zo_, qo0, l, U[d], l, U[NN + d]);
             qo1 += l * U[2 * NN + d];
           }
           const int nsel = side ? 0 : sub + 1;
@@ -1528,8 +1524,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           for (int i = 0; i < OC_MAXN; ++i) {  // neighbour trace (Nn <= OC_MAXN nodes)
             if (i < Nn) {
               const R l = __ldg(&tn.F[nsel][nf][kn][i]);
-              zn += l * NB[(sl * 3 + 0) * OC_MAXN + i];
-              qn0 += l * NB[(sl * 3 + 1) * OC_MAXN + i];
+              fma2(zn, qn0, l, NB[(sl * 3 + 0) * OC_MAXN + i], l, NB[(sl * 3 + 1) * OC_MAXN + i]);
               qn1 += l * NB[(sl * 3 + 2) * OC_MAXN + i];
             }
           }
@@ -1604,8 +1599,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       if (reg_cols) {
 #pragma unroll
         for (int k = 0; k < G; ++k) {
-          cz += fcol[k] * FV[k];
-          c0 += fcol[k] * FV[FVS + k];
+          fma2(cz, c0, fcol[k], FV[k], fcol[k], FV[FVS + k]);
           c1 += fcol[k] * FV[2 * FVS + k];
         }
       } else {
@@ -1614,8 +1608,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         for (int k = 0; k < (Q > OC_MAXF ? Q : OC_MAXF); ++k) {  // nfo <= max(Q, OC_MAXF)
           if (k < nfo) {
             const R l = __ldg(col + k * OC_MAXN);
-            cz += l * FV[k];
-            c0 += l * FV[FVS + k];
+            fma2(cz, c0, l, FV[k], l, FV[FVS + k]);
             c1 += l * FV[2 * FVS + k];
           }
         }
@@ -1746,43 +1739,66 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         wet = wet && (v + zb > wet_thr);
       }
     }
-    // closed form of max_iter sweeps on fully wet cells: delta = A_K b
+    // closed form of max_iter sweeps on fully wet cells: delta = A_K b (the 1D
+    // factors applied to two output rows at a time in packed FMAs)
     if (member && t < N) {
 #pragma unroll
-      for (int ap = 0; ap < N; ++ap) {
-        R v = 0;
+      for (int ap = 0; ap < N; ap += 2) {
+        R v0 = 0, v1 = 0;
 #pragma unroll
-        for (int ix = 0; ix < N; ++ix) v += tb.W1[ap][ix] * BZ[t * N + ix];
-        X[t * T + ap] = v;
+        for (int ix = 0; ix < N; ++ix) {
+          const R b = BZ[t * N + ix];
+          if (ap + 1 < N) fma2(v0, v1, tb.W1[ap][ix], b, tb.W1[ap + 1][ix], b);
+          else v0 += tb.W1[ap][ix] * b;
+        }
+        X[t * T + ap] = v0;
+        if (ap + 1 < N) X[t * T + ap + 1] = v1;
       }
     }
     __syncwarp();
     if (member && t < N) {
       R c[N];
 #pragma unroll
-      for (int aa = 0; aa < N; ++aa) {
-        R v = 0;
+      for (int aa = 0; aa < N; aa += 2) {
+        R v0 = 0, v1 = 0;
 #pragma unroll
-        for (int iy = 0; iy < N; ++iy) v += tb.W1[aa][iy] * X[iy * T + t];
-        c[aa] = v * tb.Gk[aa][t] / det;
+        for (int iy = 0; iy < N; ++iy) {
+          const R x = X[iy * T + t];
+          if (aa + 1 < N) fma2(v0, v1, tb.W1[aa][iy], x, tb.W1[aa + 1][iy], x);
+          else v0 += tb.W1[aa][iy] * x;
+        }
+        c[aa] = v0 * tb.Gk[aa][t] / det;
+        if (aa + 1 < N) c[aa + 1] = v1 * tb.Gk[aa + 1][t] / det;
       }
 #pragma unroll
-      for (int iy = 0; iy < N; ++iy) {
-        R v = 0;
+      for (int iy = 0; iy < N; iy += 2) {
+        R v0 = 0, v1 = 0;
 #pragma unroll
-        for (int aa = 0; aa < N; ++aa) v += tb.W2[iy][aa] * c[aa];
-        X[2 * NT + iy * T + t] = v;
+        for (int aa = 0; aa < N; ++aa) {
+          if (iy + 1 < N) fma2(v0, v1, tb.W2[iy][aa], c[aa], tb.W2[iy + 1][aa], c[aa]);
+          else v0 += tb.W2[iy][aa] * c[aa];
+        }
+        X[2 * NT + iy * T + t] = v0;
+        if (iy + 1 < N) X[2 * NT + (iy + 1) * T + t] = v1;
       }
     }
     __syncwarp();
     if (member && t < N) {  // delta rows into tile 3, zeta' of the result into tile 4
 #pragma unroll
-      for (int ix = 0; ix < N; ++ix) {
-        R dl = 0;
+      for (int ix = 0; ix < N; ix += 2) {
+        R d0 = 0, d1 = 0;
 #pragma unroll
-        for (int ap = 0; ap < N; ++ap) dl += tb.W2[ix][ap] * X[2 * NT + t * T + ap];
-        X[3 * NT + t * N + ix] = dl;
-        X[4 * NT + t * N + ix] = ZN[t * N + ix] + dl;
+        for (int ap = 0; ap < N; ++ap) {
+          const R x = X[2 * NT + t * T + ap];
+          if (ix + 1 < N) fma2(d0, d1, tb.W2[ix][ap], x, tb.W2[ix + 1][ap], x);
+          else d0 += tb.W2[ix][ap] * x;
+        }
+        X[3 * NT + t * N + ix] = d0;
+        X[4 * NT + t * N + ix] = ZN[t * N + ix] + d0;
+        if (ix + 1 < N) {
+          X[3 * NT + t * N + ix + 1] = d1;
+          X[4 * NT + t * N + ix + 1] = ZN[t * N + ix + 1] + d1;
+        }
       }
     }
     __syncwarp();
@@ -2030,50 +2046,54 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     }
     __syncwarp();
   }
-  // S^-1 diag(coef) S^-T applied to the two discharge components of RES (in place)
+  // S^-1 diag(coef) S^-T applied to the two discharge components of RES (in place);
+  // both components in one pass, their sums paired in packed FMAs
   if (member && t < N) {  // x-pass: A[iy][qx] = sum_ix Sinv[ix][qx] in[iy][ix]
-#pragma unroll 1  // component loop kept rolled (instruction footprint)
-    for (int e = 0; e < 2; ++e)
 #pragma unroll
-      for (int qx = 0; qx < N; ++qx) {
-        R v = 0;
+    for (int qx = 0; qx < N; ++qx) {
+      R v0 = 0, v1 = 0;
 #pragma unroll
-        for (int ix = 0; ix < N; ++ix) v += tb.Sinv[ix][qx] * RES[(1 + e) * NN + t * N + ix];
-        X[e * NT + t * T + qx] = v;
-      }
+      for (int ix = 0; ix < N; ++ix)
+        fma2(v0, v1, tb.Sinv[ix][qx], RES[NN + t * N + ix], tb.Sinv[ix][qx],
+             RES[2 * NN + t * N + ix]);
+      X[0 * NT + t * T + qx] = v0;
+      X[1 * NT + t * T + qx] = v1;
+    }
   }
   __syncwarp();
   if (member && t < N) {  // y on column qx = t: scale, back-transform in y
-#pragma unroll 1  // component loop kept rolled (instruction footprint)
-    for (int e = 0; e < 2; ++e) {
-      R bq[N];
+    R b0[N], b1[N];
 #pragma unroll
-      for (int qy = 0; qy < N; ++qy) {
-        R v = 0;
+    for (int qy = 0; qy < N; ++qy) {
+      R v0 = 0, v1 = 0;
 #pragma unroll
-        for (int iy = 0; iy < N; ++iy) v += tb.Sinv[iy][qy] * X[e * NT + iy * T + t];
-        bq[qy] = v * coef[qy];
-      }
+      for (int iy = 0; iy < N; ++iy)
+        fma2(v0, v1, tb.Sinv[iy][qy], X[0 * NT + iy * T + t], tb.Sinv[iy][qy],
+             X[1 * NT + iy * T + t]);
+      b0[qy] = v0 * coef[qy];
+      b1[qy] = v1 * coef[qy];
+    }
 #pragma unroll
-      for (int iy = 0; iy < N; ++iy) {
-        R v = 0;
+    for (int iy = 0; iy < N; ++iy) {
+      R v0 = 0, v1 = 0;
 #pragma unroll
-        for (int qy = 0; qy < N; ++qy) v += tb.Sinv[iy][qy] * bq[qy];
-        X[(2 + e) * NT + iy * T + t] = v;
-      }
+      for (int qy = 0; qy < N; ++qy) fma2(v0, v1, tb.Sinv[iy][qy], b0[qy], tb.Sinv[iy][qy], b1[qy]);
+      X[2 * NT + iy * T + t] = v0;
+      X[3 * NT + iy * T + t] = v1;
     }
   }
   __syncwarp();
   if (member && t < N) {  // x back-transform into RES_q
-#pragma unroll 1  // component loop kept rolled (instruction footprint)
-    for (int e = 0; e < 2; ++e)
 #pragma unroll
-      for (int ix = 0; ix < N; ++ix) {
-        R v = 0;
+    for (int ix = 0; ix < N; ++ix) {
+      R v0 = 0, v1 = 0;
 #pragma unroll
-        for (int qx = 0; qx < N; ++qx) v += tb.Sinv[ix][qx] * X[(2 + e) * NT + t * T + qx];
-        RES[(1 + e) * NN + t * N + ix] = v;
-      }
+      for (int qx = 0; qx < N; ++qx)
+        fma2(v0, v1, tb.Sinv[ix][qx], X[2 * NT + t * T + qx], tb.Sinv[ix][qx],
+             X[3 * NT + t * T + qx]);
+      RES[NN + t * N + ix] = v0;
+      RES[2 * NN + t * N + ix] = v1;
+    }
   }
   __syncwarp();
 
