@@ -106,3 +106,23 @@ def test_vortex_p3_320x160_rule_p1(gpu_lib):
         assert rel(zd.cpu().numpy(), z) < TOL_FP64 and rel(qd.cpu().numpy(), q) < TOL_FP64
         em = rel(zm.cpu().numpy(), z), rel(qm.cpu().numpy(), q)
         assert em[0] < 1e-6 and em[1] < 1e-6, em
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_time_steps_rule_p1_mixed_degrees(gpu_lib, precision):
+    """Whole SSP-RK3 steps on a mixed-degree hanging mesh under the p + 1 rule
+    (per-group launches: the one-launch hp kernel is built for the default rule):
+    FP64 within 1e-12, mixed within 1e-6 of the oracle."""
+    _, orc, op = setup("mixed_degree", precision=precision, cell_quadrature=RULE,
+                       **({"zeta_reference": 1.0, "reference_state": (1.0, (1.0, 0.0))}
+                          if precision == "mixed" else {}))
+    z, q = orc.project_vortex(0.0)
+    zg, qg = z.copy(), q.copy()
+    dt = 0.075 / orc.transport_speed(z, q)
+    tb = O.TABLEAUX["ssp33"]
+    for it in range(2):
+        O.erk_step(orc, tb["a"], tb["b"], tb["c"], it * dt, dt, z, q)
+        op.perform_time_step("ssp33", it * dt, dt, zg, qg)
+    assert op.launch_config["one_launch"] is False
+    tol = TOL_FP64 if precision == "fp64" else 1e-6
+    assert rel(zg, z) < tol and rel(qg, q) < tol
