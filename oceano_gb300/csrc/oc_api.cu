@@ -156,6 +156,7 @@ struct oc_op {
   int group_n[OC_MAXDEG + 1] = {0, 0, 0, 0, 0};
   int *d_group[OC_MAXDEG + 1] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   int uniform_deg = 0;
+  int conforming = 0;  // uniform degree, no hanging face, standard orientation
   // boundary conditions
   int bc_kind[OC_MAXBID] = {0}, bc_fn[OC_MAXBID] = {0};
   double bc_c[OC_MAXBID][3] = {{0}};
@@ -459,6 +460,7 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
   op->fnrm.resize(2 * (size_t)nf); op->flen.resize(nf);
   op->slots.assign(8 * (size_t)nc, -1);
   int64_t sf = 0, sb = 0;
+  bool nonconforming = false;
   static const double rn[4][2] = {{-1, 0}, {1, 0}, {0, -1}, {0, 1}};
   for (int f = 0; f < nf; ++f) {
     const int cm = m->cell_m[f];
@@ -480,6 +482,7 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
       const int nfq = std::max(m->degree[cm], m->degree[cp]) + 2;
       op->fcp[f] = cp;
       op->fpack[f] = fm | (fp << 4) | ((sub + 1) << 8) | (orient << 12) | (nfq << 16);
+      if (sub >= 0 || orient != 0) nonconforming = true;
       op->fsd[f] = (int)sf;
       sf += 2 * nfq;
       int *sm = &op->slots[8 * (size_t)cm + 2 * fm];
@@ -510,6 +513,7 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
       if (sl[0] == -1) return bad(OC_ERR_INVALID_ARG, "hanging face without subface 0");
     }
   op->sd_size[3] = sf; op->sd_size[4] = sb;
+  op->conforming = op->uniform_deg != 0 && !nonconforming;
   // face pass: output offset of every face
   op->fofs.resize(nf);
   int64_t fo_total = 0;
@@ -831,7 +835,7 @@ static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
       b0 += a.hp_blocks[p];
     }
     const int hv = variant == 0 ? 0 : (a.r_is_float ? 1 : 2);
-    OC_TRY(launch_stage_hp(hv, a, b0, wpb, variant == 3, op->stream));
+    OC_TRY(launch_stage_hp(hv, a, b0, wpb, variant >= 3, op->stream));
     op->launches++;
     return OC_OK;
   }
@@ -1048,12 +1052,12 @@ static void step_stage_args(oc_op *op, const Scheme &sc, int st, double *z, doub
 
 // kernel variant of the time-step path: 0 FP64; 1 mixed; 3 the mixed kernel
 // compiled without static data, friction and ARK scheme, for workloads that
-// use none of them
+// use none of them; 4 the same on a conforming single-degree mesh
 static int step_variant(const oc_op *op, const Scheme &sc) {
   if (op->prm.precision != OC_PREC_MIXED) return 0;
   bool lean = !sc.ark && op->prm.friction_model == 0;
   for (int k = 0; k < 5; ++k) lean = lean && !op->d_sd[k];
-  return lean ? 3 : 1;
+  return lean ? (op->conforming ? 4 : 3) : 1;
 }
 
 // enqueue the stages of one time step on op->stream (capturable)

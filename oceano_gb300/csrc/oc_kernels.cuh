@@ -869,7 +869,7 @@ __device__ __forceinline__ void report_nonfinite(const StageArgs &a, bool bad) {
 // One block of the stage: `blk` is the block index within the degree group of
 // n_group cells (listed by group_cells, or group_first + i when NULL); the FP64
 // work-area slots of the mixed form are indexed by the launch-wide block index.
-template <int P, typename R, typename KT, bool MIX, typename RIN, bool LEAN, int QR>
+template <int P, typename R, typename KT, bool MIX, typename RIN, bool LEAN, int QR, bool CONF>
 __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *smem_raw,
                                            const int blk, const int n_group,
                                            const int *group_cells, const int group_first) {
@@ -917,6 +917,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   const float *sd0e_p = LEAN ? nullptr : a.sd0e, *sd1e_p = LEAN ? nullptr : a.sd1e,
               *sd2e_p = LEAN ? nullptr : a.sd2e, *sdfe_p = LEAN ? nullptr : a.sdfe;
   const int *cfsdo_p = LEAN ? nullptr : a.cfsdo;
+  // CONF: every cell of degree P, no hanging face, standard orientation (the host
+  // checks this): every inner face takes the register-row path
   const double *cscale_p = a.cscale;
   const float *cscalef_p = a.cscalef;
   static_assert(MIX == (sizeof(R) == 4), "the scratch layout assumes FP32 exactly in the mixed form");
@@ -1384,7 +1386,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       if (e >= 8 * OC_MAXN) break;
       const int sl = e / OC_MAXN, i = e - sl * OC_MAXN;
       const FaceRec r = recs[sl];
-      const int Nn = r.nb_deg() + 1;
+      const int Nn = CONF ? N : r.nb_deg() + 1;
       if (r.kind() == 1 && i < Nn) {
         const int d = face_dof(Nn, r.nb_face(), i);
         const int64_t oz = r.other, oq = 2 * (int64_t)r.other;
@@ -1427,7 +1429,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     // orientation, else the table path for all of them (one path per warp: on hp
     // meshes the teams of a warp meet different neighbour degrees, and two paths
     // would run one after the other)
-    const bool reg_path = __all_sync(OC_FULL, kind != 1 || (r.nb_deg() == P && r.orient() == 0));
+    const bool reg_path =
+        CONF || __all_sync(OC_FULL, kind != 1 || (r.nb_deg() == P && r.orient() == 0));
     const int fo = r.own_face();
     // DoF of node i on face fo: fbase + i * fstride (face_dof)
     const int fbase = fo == 0 ? 0 : fo == 1 ? N - 1 : fo == 2 ? 0 : (N - 1) * N;
@@ -1443,8 +1446,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       const R tx = fo < 2 ? J01 : J00, ty = fo < 2 ? J11 : J10;
       R len = m_sqrt(tx * tx + ty * ty);
       if (kind == 1) {
-        const int side = r.side(), sub = r.sub(), orient = r.orient(), nf = r.nf();
-        const int pn = r.nb_deg(), Nn = pn + 1;
+        const int side = r.side(), sub = CONF ? -1 : r.sub(), orient = r.orient(), nf = r.nf();
+        const int pn = CONF ? P : r.nb_deg(), Nn = pn + 1;
         const DegTables<R> &tn = gt[pn - 1];
         if (side == 1 && sub >= 0) len *= R(0.5);  // coarse side: the fine half-face
         const R n0 = side ? -on0 : on0, n1 = side ? -on1 : on1;  // minus normal
@@ -2242,11 +2245,11 @@ static cudaError_t launch_programmatic(K kernel, int grid, int threads, int smem
 }
 
 // One degree group per launch.
-template <int P, typename R, typename KT, bool MIX, typename RIN, bool LEAN, int QR>
+template <int P, typename R, typename KT, bool MIX, typename RIN, bool LEAN, int QR, bool CONF>
 __global__ void __launch_bounds__(128, MIX ? OC_MIXED_MIN_BLOCKS : 1) stage_kernel(const StageArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_body<P, R, KT, MIX, RIN, LEAN, QR>(a, smem_raw, blockIdx.x, a.n_group, a.group_cells,
-                                           a.group_first);
+  stage_body<P, R, KT, MIX, RIN, LEAN, QR, CONF>(a, smem_raw, blockIdx.x, a.n_group,
+                                                 a.group_cells, a.group_first);
 }
 
 // Every degree group of an hp mesh in one launch: the grid is the concatenation
@@ -2261,8 +2264,8 @@ __global__ void __launch_bounds__(128, MIX ? OC_HP_MIN_BLOCKS : 1) stage_kernel_
   const int b = blockIdx.x;
 #define OC_HP_CASE(P)                                                                          \
   if (b >= a.hp_first_block[P] && b < a.hp_first_block[P] + a.hp_blocks[P]) {                 \
-    stage_body<P, R, KT, MIX, RIN, LEAN, 0>(a, smem_raw, b - a.hp_first_block[P], a.hp_n[P],  \
-                                         a.hp_cells[P], 0);                                    \
+    stage_body<P, R, KT, MIX, RIN, LEAN, 0, false>(a, smem_raw, b - a.hp_first_block[P],      \
+                                                   a.hp_n[P], a.hp_cells[P], 0);               \
     return;                                                                                    \
   }
   OC_HP_CASE(4)

@@ -25,21 +25,21 @@ namespace oc {
 static const int kMaxWarpsPerBlock = 4;
 static constexpr int kRule = OC_CELL_RULE;
 
-template <typename R, typename KT, bool MIX, typename RIN, bool LEAN = false>
+template <typename R, typename KT, bool MIX, typename RIN, bool LEAN = false, bool CONF = false>
 static cudaError_t configure_one() {
   constexpr int P = OC_DEGREE;
   const int smem = kMaxWarpsPerBlock * Dims<P, kRule>::template warp_bytes<R>();
-  return cudaFuncSetAttribute(stage_kernel<P, R, KT, MIX, RIN, LEAN, kRule>,
+  return cudaFuncSetAttribute(stage_kernel<P, R, KT, MIX, RIN, LEAN, kRule, CONF>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
-template <typename R, typename KT, bool MIX, typename RIN, bool LEAN = false>
+template <typename R, typename KT, bool MIX, typename RIN, bool LEAN = false, bool CONF = false>
 static cudaError_t launch_one(const StageArgs &a, int grid, int wpb, cudaStream_t st) {
   constexpr int P = OC_DEGREE;
   if (wpb > kMaxWarpsPerBlock) return cudaErrorInvalidValue;
   const int smem = wpb * Dims<P, kRule>::template warp_bytes<R>();
-  return launch_programmatic(stage_kernel<P, R, KT, MIX, RIN, LEAN, kRule>, grid, wpb * 32,
-                             smem, st, a);
+  return launch_programmatic(stage_kernel<P, R, KT, MIX, RIN, LEAN, kRule, CONF>, grid,
+                             wpb * 32, smem, st, a);
 }
 
 // dynamic shared-memory opt-in, done once at set-up (outside any stream capture)
@@ -50,13 +50,16 @@ cudaError_t OC_NAME(configure_stage_p)() {
   if (e == cudaSuccess) e = configure_one<float, double, true, double>();
   if (e == cudaSuccess) e = configure_one<float, float, true, float, true>();
   if (e == cudaSuccess) e = configure_one<float, float, true, double, true>();
+  if (e == cudaSuccess) e = configure_one<float, float, true, float, true, true>();
+  if (e == cudaSuccess) e = configure_one<float, float, true, double, true, true>();
   return e;
 }
 
 // variant 0: FP64; 1: mixed time step with FP32 registers (FP64 stage input at
 // stage 0, FP32 afterwards); 2: mixed reference-ABI stage (FP64 registers and
 // vectors); 3: variant 1 compiled without static data, friction and ARK scheme
-// (the lean kernel of workloads that use none of them)
+// (the lean kernel of workloads that use none of them); 4: variant 3 for a
+// conforming mesh of this degree alone (no hanging face, standard orientation)
 cudaError_t OC_NAME(launch_stage_p)(const StageArgs &a, int variant, int grid, int wpb,
                                     cudaStream_t st) {
   switch (variant) {
@@ -68,6 +71,9 @@ cudaError_t OC_NAME(launch_stage_p)(const StageArgs &a, int variant, int grid, i
     case 3:
       return a.r_is_float ? launch_one<float, float, true, float, true>(a, grid, wpb, st)
                           : launch_one<float, float, true, double, true>(a, grid, wpb, st);
+    case 4:
+      return a.r_is_float ? launch_one<float, float, true, float, true, true>(a, grid, wpb, st)
+                          : launch_one<float, float, true, double, true, true>(a, grid, wpb, st);
     default: return cudaErrorInvalidValue;
   }
 }
