@@ -609,10 +609,13 @@ __device__ __forceinline__ void gl_eval_apply_integrate(const double *DZ, double
 // stopped when the l1 norm of the update summed over the cell batch is <= 1e-12.
 // DZ holds the initial guess on entry and the result on exit; rhs are the
 // rows of thread t < N.  All lanes call; `work` selects the participating teams.
+// (out of line: the mixed form runs it only for cells that are not fully wet,
+// and a smaller kernel body keeps the common path in the instruction cache)
 template <int P, int QR>
-__device__ void zeta_iteration_fp64(const StageArgs &a, int cell, double *DZ, double *DX,
-                                    double *DRED, double *warp_norm, int team, int cpw, int t,
-                                    bool member, bool work, const double *rhs) {
+__device__ __noinline__ void zeta_iteration_fp64(const StageArgs &a, int cell, double *DZ,
+                                                 double *DX, double *DRED, double *warp_norm,
+                                                 int team, int cpw, int t, bool member, bool work,
+                                                 const double *rhs) {
   using D = Dims<P, QR>;
   constexpr int N = D::N, G = D::G, T = D::T;
   const DegTables<double> &tb = tab<double>(P);
@@ -682,6 +685,80 @@ __device__ void zeta_iteration_fp64(const StageArgs &a, int cell, double *DZ, do
     __syncwarp();
     active = active && bn > 1e-12;
   }
+}
+
+// Mixed form's exact wetness check of one cell (all lanes of the warp call): the
+// nodal values vals ([row][node], FP32 deviations from zeta_ref) at the
+// Gauss-Lobatto (p+2)^2 points, through the scratch tile Xs; lane t < G of a
+// team with `check` set tests column t: zeta + zb > threshold at every point.
+// Out of line: it runs only where the Lebesgue bound cannot prove wetness.
+template <int P, int QR, typename R>
+__device__ __noinline__ bool gl_wet(const R *vals, R *Xs, int t, bool member, bool check,
+                                    const float *zb1e, R zbe_flat, R wet_thr) {
+  using D = Dims<P, QR>;
+  constexpr int N = D::N, G = D::G, T = D::T;
+  const DegTables<R> &tb = tab<R>(P);
+  if (member && t < N) {
+#pragma unroll
+    for (int gx = 0; gx < G; ++gx) {
+      R v = 0;
+#pragma unroll
+      for (int ix = 0; ix < N; ++ix) v += tb.BG[gx][ix] * vals[t * N + ix];
+      Xs[t * T + gx] = v;
+    }
+  }
+  __syncwarp();
+  bool wet = true;
+  if (check && member && t < G) {
+#pragma unroll
+    for (int gy = 0; gy < G; ++gy) {
+      R v = 0;
+#pragma unroll
+      for (int iy = 0; iy < N; ++iy) v += tb.BG[gy][iy] * Xs[iy * T + t];
+      const R zb = zb1e ? (R)zb1e[gy * G + t] : zbe_flat;
+      wet = wet && (v + zb > wet_thr);
+    }
+  }
+  __syncwarp();
+  return wet;
+}
+
+// The zeta solve of a stage literally in FP64 (all lanes of the warp call; `work`
+// selects the teams): zeta^n into DZ, rhs = b + int depth(zeta^n) phi over
+// Gauss-Lobatto p+2 (OceanDG.h:828-855), then zeta_iteration_fp64.  The FP64
+// form runs it for every cell, the mixed form only for cells that are not fully
+// wet; out of line, so that the mixed kernel's common path stays small in the
+// instruction cache.
+template <int P, int QR, typename R>
+__device__ __noinline__ void zeta_literal_fp64(const StageArgs &a, int cell, int64_t zo,
+                                               const R *BZ, const double *sd1_p, double *DZ,
+                                               double *DX, double *DRED, double *warp_norm,
+                                               int team, int cpw, int t, bool member, bool work) {
+  using D = Dims<P, QR>;
+  constexpr int N = D::N, G = D::G;
+  if (member && t < N) {
+#pragma unroll
+    for (int ix = 0; ix < N; ++ix) DZ[t * N + ix] = a.un_z[zo + t * N + ix];
+  }
+  __syncwarp();
+  double rhs[N], dummy[N];
+  {
+    const double det_d = a.geo[11 * (int64_t)cell + 10];
+    const double *zb1 = sd1_p ? sd1_p + cell_data(a.err, a.sdo1, cell, a.n_sd[1], G * G) : nullptr;
+    const DegTables<double> &td = tab<double>(P);
+    gl_eval_apply_integrate<P, QR>(
+        DZ, DX, t, work,
+        [&](int qx, int qy, double v, double &o0, double &o1) {
+          const double zb = zb1 ? zb1[qy * G + qx] : 0.;
+          o0 = depth<double>(v, zb) * (td.wG[qx] * td.wG[qy] * det_d);
+          o1 = 0;
+        },
+        rhs, dummy);
+    if (work && t < N)
+#pragma unroll
+      for (int ix = 0; ix < N; ++ix) rhs[ix] = (double)BZ[t * N + ix] + rhs[ix];
+  }
+  zeta_iteration_fp64<P, QR>(a, cell, DZ, DX, DRED, warp_norm, team, cpw, t, member, work, rhs);
 }
 
 // Boundary face point (OceanDG.h:1105-1339): ghost state of the boundary kind
@@ -1042,7 +1119,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     // fast ERK path: the discharge part of the update known before this stage,
     // QB = (last stage ? 0 : q^n) + sum_{j<s} f_j k_q[j+1] (RST region, unused by
     // the explicit stage), loaded with the stage input so that the epilogue loads nothing
-    if (fast && !ark && !a.apply_mode) {
+    if (fast && !ark && (LEAN || !a.apply_mode)) {
       R qb0 = 0, qb1 = 0;
 #pragma unroll
       for (int jj = 0; jj < OC_MAXSTAGES; ++jj)
@@ -1057,7 +1134,7 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
       Uj[6 * NN + d] = qb0;
       Uj[7 * NN + d] = qb1;
     }
-    if (!a.apply_mode) {
+    if (LEAN || !a.apply_mode) {
       R bprev = 0;  // sum_{j<s} f_j kz_j in the reference's order
 #pragma unroll
       for (int jj = 0; jj < OC_MAXSTAGES; ++jj)  // compile-time indices: fR stays in registers
@@ -1583,8 +1660,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
             qm1 += l * U[2 * NN + d];
           }
           R F, Fa0, Fa1;
-          boundary_flux<R, MIX>(a, bid, bkind, fo, (QR ? tab<double>(P).xM[k] : tab<double>(P).xQ[k]), geo, zref, sdo + k, g, cu4,
-                                zm, qm0, qm1, n0, n1, F, Fa0, Fa1);
+          const double sx = QR ? tab<double>(P).xM[k] : tab<double>(P).xQ[k];
+          boundary_flux<R, MIX>(a, bid, bkind, fo, sx, geo, zref, sdo + k, g, cu4, zm, qm0, qm1,
+                                n0, n1, F, Fa0, Fa1);
           const R jxw = cwQ[k] * len;
           FV[k] = -F * jxw;
           FV[FVS + k] = -Fa0 * jxw;
@@ -1626,8 +1704,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
 
   }
 
-  // ---- apply(): dst = M^-1 L_h(src), exact Gauss p+1 inverse for all variables ----
-  if (a.apply_mode) {
+  // ---- apply(): dst = M^-1 L_h(src), exact Gauss p+1 inverse for all variables
+  //      (not in the lean variants: apply() launches the general ones) ----
+  if (!LEAN && a.apply_mode) {
     if (member && t < N) {
 #pragma unroll
       for (int e = 0; e < 3; ++e)
@@ -1721,27 +1800,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     bool wet = true;
     const bool sure0 = bound_wet(ZN);
     const bool exact0 = __any_sync(OC_FULL, member && !sure0);
-    if (exact0 && member && t < N) {
-#pragma unroll
-      for (int gx = 0; gx < G; ++gx) {
-        R v = 0;
-#pragma unroll
-        for (int ix = 0; ix < N; ++ix) v += tb.BG[gx][ix] * ZN[t * N + ix];
-        X[NT + t * T + gx] = v;
-      }
-    }
-    __syncwarp();
     const float *zb1e = sd1e_p ? sd1e_p + cell_data(a.err, a.sdo1, cell, a.n_sd[1], G * G) : nullptr;
-    if (exact0 && !sure0 && member && t < G) {
-#pragma unroll
-      for (int gy = 0; gy < G; ++gy) {
-        R v = 0;
-#pragma unroll
-        for (int iy = 0; iy < N; ++iy) v += tb.BG[gy][iy] * X[NT + iy * T + t];
-        const R zb = zb1e ? (R)zb1e[gy * G + t] : zbe_flat;
-        wet = wet && (v + zb > wet_thr);
-      }
-    }
+    if (exact0) wet = gl_wet<P, QR, R>(ZN, X + NT, t, member, !sure0, zb1e, zbe_flat, wet_thr);
     // closed form of max_iter sweeps on fully wet cells: delta = A_K b (the 1D
     // factors applied to two output rows at a time in packed FMAs)
     if (member && t < N) {
@@ -1809,25 +1869,10 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     // check the result too, else redo the cell with the FP64 literal iteration
     const bool sure1 = bound_wet(X + 4 * NT);
     const bool exact1 = __any_sync(OC_FULL, member && !sure1);
-    if (exact1 && member && t < N) {
-#pragma unroll
-      for (int gx = 0; gx < G; ++gx) {
-        R v = 0;
-#pragma unroll
-        for (int ix = 0; ix < N; ++ix) v += tb.BG[gx][ix] * X[4 * NT + t * N + ix];
-        X[5 * NT + t * T + gx] = v;
-      }
-    }
-    __syncwarp();
-    if (exact1 && !sure1 && member && t < G) {
-#pragma unroll
-      for (int gy = 0; gy < G; ++gy) {
-        R v = 0;
-#pragma unroll
-        for (int iy = 0; iy < N; ++iy) v += tb.BG[gy][iy] * X[5 * NT + iy * T + t];
-        const R zb = zb1e ? (R)zb1e[gy * G + t] : zbe_flat;
-        wet = wet && (v + zb > wet_thr);
-      }
+    if (exact1) {  // all lanes call (the helper synchronises the warp)
+      const bool w1 =
+          gl_wet<P, QR, R>(X + 4 * NT, X + 5 * NT, t, member, !sure1, zb1e, zbe_flat, wet_thr);
+      wet = wet && w1;
     }
     const unsigned drym = __ballot_sync(OC_FULL, member && !wet);  // team OR of "not wet"
     need_fp64 = ((drym >> (team * T)) & ((1u << T) - 1u)) != 0u;
@@ -1835,30 +1880,8 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
   if (__any_sync(OC_FULL, valid && need_fp64)) {
     // literal FP64 iteration (all lanes; teams with work = valid && need_fp64)
     const bool work = valid && need_fp64;
-    if (member && t < N) {
-#pragma unroll
-      for (int ix = 0; ix < N; ++ix) DZ[t * N + ix] = a.un_z[zo + t * N + ix];
-    }
-    __syncwarp();
-    // rhs = b + int depth(zeta^n) phi over Gauss-Lobatto p+2 (OceanDG.h:828-855)
-    double rhs[N], dummy[N];
-    {
-      const double det_d = geo[10];
-      const double *zb1 = sd1_p ? sd1_p + cell_data(a.err, a.sdo1, cell, a.n_sd[1], G * G) : nullptr;
-      const DegTables<double> &td = tab<double>(P);
-      gl_eval_apply_integrate<P, QR>(
-          DZ, DX, t, work,
-          [&](int qx, int qy, double v, double &o0, double &o1) {
-            const double zb = zb1 ? zb1[qy * G + qx] : 0.;
-            o0 = depth<double>(v, zb) * (td.wG[qx] * td.wG[qy] * det_d);
-            o1 = 0;
-          },
-          rhs, dummy);
-      if (work && t < N)
-#pragma unroll
-        for (int ix = 0; ix < N; ++ix) rhs[ix] = (double)BZ[t * N + ix] + rhs[ix];
-    }
-    zeta_iteration_fp64<P, QR>(a, cell, DZ, DX, DRED, warp_norm, team, cpw, t, member, work, rhs);
+    zeta_literal_fp64<P, QR, R>(a, cell, zo, BZ, sd1_p, DZ, DX, DRED, warp_norm, team, cpw, t,
+                                member, work);
     if (work && t == 0) w_flag[team] = 1;
   }
   if (MIX && member && t < N && !need_fp64) {  // wet: keep delta (FP32) in BZ
