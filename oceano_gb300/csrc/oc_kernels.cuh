@@ -907,6 +907,44 @@ static __device__ __noinline__ void check_record(const StageArgs &a, FaceRec &r,
 }
 #endif
 
+// Boundary face of a cell slot in the mixed form's face phase: lane t < Q of the
+// team evaluates Gauss point t (the own trace, the ghost state of the boundary
+// kind and the fluxes, boundary_flux) and writes the point's values times the
+// outward sign and JxW into FV ([var][FVS]).  Out of line: only the teams of
+// boundary cells run it.
+template <int P, int QR, typename R, bool MIX>
+__device__ __noinline__ void boundary_slot(const StageArgs &a, int bid, int fo, int sdo, R n0,
+                                           R n1, R len, const double *geo, double zref, R g,
+                                           R cu4, const R *U, R *FV, int t) {
+  using D = Dims<P, QR>;
+  constexpr int N = D::N, NN = D::NN, Q = D::Q;
+  const DegTables<R> &tb = tab<R>(P);
+  const auto &cBQ = QR ? tb.BM : tb.BQ;
+  const auto &cwQ = QR ? tb.wM : tb.wQ;
+  const int bkind = a.bc_kind[bid];
+  if (bkind == 0 && t == 0) atomicOr(a.err, ERR_UNKNOWN_BID);
+  if (t < Q) {
+    const int k = t;
+    R zm = 0, qm0 = 0, qm1 = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      const int d = face_dof(N, fo, i);
+      const R l = cBQ[k][i];
+      zm += l * U[d];
+      qm0 += l * U[NN + d];
+      qm1 += l * U[2 * NN + d];
+    }
+    R F, Fa0, Fa1;
+    const double sx = QR ? tab<double>(P).xM[k] : tab<double>(P).xQ[k];
+    boundary_flux<R, MIX>(a, bid, bkind, fo, sx, geo, zref, sdo + k, g, cu4, zm, qm0, qm1, n0, n1,
+                          F, Fa0, Fa1);
+    const R jxw = cwQ[k] * len;
+    FV[k] = -F * jxw;
+    FV[FVS + k] = -Fa0 * jxw;
+    FV[2 * FVS + k] = -Fa1 * jxw;
+  }
+}
+
 // Stage coefficients in the compute type: the FP32 copies for the FP32 bulk (one
 // 16-byte read-only load, no FP64 conversion), the FP64 values otherwise.
 template <typename R>
@@ -1639,35 +1677,11 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
           }
         }
       } else {  // boundary face
-        const int b = r.other;
-        const int bid = r.bid();
-        const int bkind = a.bc_kind[bid];
-        if (bkind == 0 && t == 0) atomicOr(a.err, ERR_UNKNOWN_BID);
         const int sdo = cfsdo_p ? w_sdo[8 * team + sl] : 0;
-        const R n0 = on0, n1 = on1;
         nfo = Q;
         tsel = -1;
-        (void)b;
-        if (t < Q) {
-          const int k = t;
-          R zm = 0, qm0 = 0, qm1 = 0;
-#pragma unroll
-          for (int i = 0; i < N; ++i) {
-            const int d = face_dof(N, fo, i);
-            const R l = cBQ[k][i];
-            zm += l * U[d];
-            qm0 += l * U[NN + d];
-            qm1 += l * U[2 * NN + d];
-          }
-          R F, Fa0, Fa1;
-          const double sx = QR ? tab<double>(P).xM[k] : tab<double>(P).xQ[k];
-          boundary_flux<R, MIX>(a, bid, bkind, fo, sx, geo, zref, sdo + k, g, cu4, zm, qm0, qm1,
-                                n0, n1, F, Fa0, Fa1);
-          const R jxw = cwQ[k] * len;
-          FV[k] = -F * jxw;
-          FV[FVS + k] = -Fa0 * jxw;
-          FV[2 * FVS + k] = -Fa1 * jxw;
-        }
+        boundary_slot<P, QR, R, MIX>(a, r.bid(), fo, sdo, on0, on1, len, geo, zref, g, cu4, U, FV,
+                                     t);
       }
     }
     __syncwarp();
