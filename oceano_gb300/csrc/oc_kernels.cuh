@@ -691,10 +691,9 @@ __device__ __noinline__ void zeta_iteration_fp64(const StageArgs &a, int cell, d
 // nodal values vals ([row][node], FP32 deviations from zeta_ref) at the
 // Gauss-Lobatto (p+2)^2 points, through the scratch tile Xs; lane t < G of a
 // team with `check` set tests column t: zeta + zb > threshold at every point.
-// Out of line: it runs only where the Lebesgue bound cannot prove wetness.
 template <int P, int QR, typename R>
-__device__ __noinline__ bool gl_wet(const R *vals, R *Xs, int t, bool member, bool check,
-                                    const float *zb1e, R zbe_flat, R wet_thr) {
+__device__ __forceinline__ bool gl_wet(const R *vals, R *Xs, int t, bool member, bool check,
+                                       const float *zb1e, R zbe_flat, R wet_thr) {
   using D = Dims<P, QR>;
   constexpr int N = D::N, G = D::G, T = D::T;
   const DegTables<R> &tb = tab<R>(P);
@@ -721,6 +720,16 @@ __device__ __noinline__ bool gl_wet(const R *vals, R *Xs, int t, bool member, bo
   }
   __syncwarp();
   return wet;
+}
+
+// gl_wet out of line, for the lean variants: without bathymetry data the check runs
+// only where the Lebesgue bound cannot prove wetness, so its code stays out of
+// the instruction cache of the common path (with bathymetry it runs every time and
+// stays inline)
+template <int P, int QR, typename R>
+__device__ __noinline__ bool gl_wet_call(const R *vals, R *Xs, int t, bool member, bool check,
+                                         const float *zb1e, R zbe_flat, R wet_thr) {
+  return gl_wet<P, QR, R>(vals, Xs, t, member, check, zb1e, zbe_flat, wet_thr);
 }
 
 // The zeta solve of a stage literally in FP64 (all lanes of the warp call; `work`
@@ -1815,7 +1824,9 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     const bool sure0 = bound_wet(ZN);
     const bool exact0 = __any_sync(OC_FULL, member && !sure0);
     const float *zb1e = sd1e_p ? sd1e_p + cell_data(a.err, a.sdo1, cell, a.n_sd[1], G * G) : nullptr;
-    if (exact0) wet = gl_wet<P, QR, R>(ZN, X + NT, t, member, !sure0, zb1e, zbe_flat, wet_thr);
+    if (exact0)
+      wet = LEAN ? gl_wet_call<P, QR, R>(ZN, X + NT, t, member, !sure0, zb1e, zbe_flat, wet_thr)
+                 : gl_wet<P, QR, R>(ZN, X + NT, t, member, !sure0, zb1e, zbe_flat, wet_thr);
     // closed form of max_iter sweeps on fully wet cells: delta = A_K b (the 1D
     // factors applied to two output rows at a time in packed FMAs)
     if (member && t < N) {
@@ -1885,7 +1896,10 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
     const bool exact1 = __any_sync(OC_FULL, member && !sure1);
     if (exact1) {  // all lanes call (the helper synchronises the warp)
       const bool w1 =
-          gl_wet<P, QR, R>(X + 4 * NT, X + 5 * NT, t, member, !sure1, zb1e, zbe_flat, wet_thr);
+          LEAN ? gl_wet_call<P, QR, R>(X + 4 * NT, X + 5 * NT, t, member, !sure1, zb1e, zbe_flat,
+                                       wet_thr)
+               : gl_wet<P, QR, R>(X + 4 * NT, X + 5 * NT, t, member, !sure1, zb1e, zbe_flat,
+                                  wet_thr);
       wet = wet && w1;
     }
     const unsigned drym = __ballot_sync(OC_FULL, member && !wet);  // team OR of "not wet"
