@@ -34,8 +34,10 @@ def checked_results(tmp_path_factory):
 
 def test_checked_build_flags_nothing_and_matches(gpu_lib, checked_results):
     """Every case and precision: no OC_ERR_BOUNDS (the child would have raised),
-    and the same u^{n+1}, transport speed and velocity as the regular build
-    (relative 1e-14: the checked build compiles the same expressions)."""
+    and the regular build's u^{n+1}, transport speed and velocity: FP64 form
+    within 1e-14 of the scale; mixed form within 1e-7 (the two builds compile the
+    same expressions, but the compiler's FP32 contraction and ordering choices
+    around the extra checks may differ by a rounding)."""
     from bounds_cases import run_all
     assert int(checked_results["_checked"][0]) == 1
     assert gpu_lib.oc_bounds_checked() == 0
@@ -44,7 +46,8 @@ def test_checked_build_flags_nothing_and_matches(gpu_lib, checked_results):
     for k, v in ref.items():
         got = checked_results[k]
         scale = max(np.abs(v).max(), 1e-300)
-        assert np.abs(got - v).max() <= 1e-14 * scale, k
+        tol = 1e-7 if "/mixed/" in k else 1e-14
+        assert np.abs(got - v).max() <= tol * scale, (k, np.abs(got - v).max() / scale)
 
 
 def test_checked_build_reports_a_failed_check(gpu_lib, checked_results):
