@@ -919,12 +919,11 @@ static __device__ __noinline__ void check_record(const StageArgs &a, FaceRec &r,
 // Boundary face of a cell slot in the mixed form's face phase: lane t < Q of the
 // team evaluates Gauss point t (the own trace, the ghost state of the boundary
 // kind and the fluxes, boundary_flux) and writes the point's values times the
-// outward sign and JxW into FV ([var][FVS]).  Out of line: only the teams of
-// boundary cells run it.
+// outward sign and JxW into FV ([var][FVS]).
 template <int P, int QR, typename R, bool MIX>
-__device__ __noinline__ void boundary_slot(const StageArgs &a, int bid, int fo, int sdo, R n0,
-                                           R n1, R len, const double *geo, double zref, R g,
-                                           R cu4, const R *U, R *FV, int t) {
+__device__ __forceinline__ void boundary_slot(const StageArgs &a, int bid, int fo, int sdo, R n0,
+                                              R n1, R len, const double *geo, double zref, R g,
+                                              R cu4, const R *U, R *FV, int t) {
   using D = Dims<P, QR>;
   constexpr int N = D::N, NN = D::NN, Q = D::Q;
   const DegTables<R> &tb = tab<R>(P);
@@ -952,6 +951,15 @@ __device__ __noinline__ void boundary_slot(const StageArgs &a, int bid, int fo, 
     FV[FVS + k] = -Fa0 * jxw;
     FV[2 * FVS + k] = -Fa1 * jxw;
   }
+}
+
+// boundary_slot out of line, for the lean variants (only the teams of boundary
+// cells run it; the common path keeps a smaller instruction footprint)
+template <int P, int QR, typename R, bool MIX>
+__device__ __noinline__ void boundary_slot_call(const StageArgs &a, int bid, int fo, int sdo,
+                                                R n0, R n1, R len, const double *geo, double zref,
+                                                R g, R cu4, const R *U, R *FV, int t) {
+  boundary_slot<P, QR, R, MIX>(a, bid, fo, sdo, n0, n1, len, geo, zref, g, cu4, U, FV, t);
 }
 
 // Stage coefficients in the compute type: the FP32 copies for the FP32 bulk (one
@@ -1689,8 +1697,12 @@ __device__ __forceinline__ void stage_body(const StageArgs &a, unsigned char *sm
         const int sdo = cfsdo_p ? w_sdo[8 * team + sl] : 0;
         nfo = Q;
         tsel = -1;
-        boundary_slot<P, QR, R, MIX>(a, r.bid(), fo, sdo, on0, on1, len, geo, zref, g, cu4, U, FV,
-                                     t);
+        if constexpr (LEAN)
+          boundary_slot_call<P, QR, R, MIX>(a, r.bid(), fo, sdo, on0, on1, len, geo, zref, g, cu4,
+                                            U, FV, t);
+        else
+          boundary_slot<P, QR, R, MIX>(a, r.bid(), fo, sdo, on0, on1, len, geo, zref, g, cu4, U,
+                                       FV, t);
       }
     }
     __syncwarp();
