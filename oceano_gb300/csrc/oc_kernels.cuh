@@ -492,8 +492,12 @@ struct Dims {
   static constexpr int SZD = NN + 3 * NT + T + 2;
   // Team strides: padded so that the 32/T teams of a warp start on different
   // shared-memory banks (stride mod 32 chosen per degree and element size to
-  // keep row, column and node-row accesses at most 2-way conflicted).
-  static constexpr int pad_f = P == 1 ? 29 : P == 2 ? 29 : P == 3 ? 3 : 0;
+  // keep row, column and node-row accesses at most 2-way conflicted).  FP32,
+  // counted over the sum-factorisation rows and columns, the face traces read by
+  // a whole team and the face values: degree 4 (4 teams of 7 lanes) is free of
+  // conflicts with a stride of 24 mod 32 (with 16 mod 32 every access was 2-way),
+  // degree 1 (10 teams of 3) has at most 2-way conflicts with 29 mod 32.
+  static constexpr int pad_f = P == 1 ? 5 : P == 2 ? 29 : P == 3 ? 3 : 8;
   static constexpr int pad_d = P == 1 ? 5 : P == 2 ? 2 : P == 3 ? 3 : 4;
   template <typename R>
   static constexpr int bytes_r() {
