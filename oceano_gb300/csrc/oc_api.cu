@@ -213,6 +213,21 @@ struct oc_op {
   int graph_scheme = -1;
   const void *graph_z = nullptr, *graph_q = nullptr;
   const void *graph_oz = nullptr, *graph_oq = nullptr;  // last-stage outputs of the graph
+  const void *graph_hz = nullptr, *graph_hq = nullptr;  // host vectors the graph copies in
+  // Host-vector time step on a mesh of one degree (mixed form): u^n is copied in
+  // by pieces on a second stream, and stage 0 runs by chunks of cells, each
+  // launched once the DoFs that its cells and their face neighbours read have
+  // arrived, so that the transfer in overlaps stage 0.  Three chunks: the chunk
+  // launches follow one another on the stream, and each lasts at least the
+  // lifetime of one warp (about a third of a stage on the 320x160 degree-3 vortex),
+  // so more chunks lengthen stage 0 again (measured per step: 1 chunk 0.350 ms,
+  // 2 0.335, 3 0.323, 4 0.329, 8 0.373).
+  static constexpr int kChunks = 3;
+  cudaStream_t cstream = nullptr;
+  cudaEvent_t cev[kChunks + 1] = {nullptr};
+  int n_chunks = 0;                    // 0: not set up yet; 1: no chunking
+  int chunk_first[kChunks + 1] = {0};  // cell range [first[k], first[k + 1]) of chunk k
+  int64_t chunk_reach[kChunks] = {0};  // zeta DoFs [0, reach[k]) read by chunks 0..k
 };
 
 #define OC_TRY(call)                                                              \
@@ -392,6 +407,9 @@ void oc_destroy(oc_op *op) {
   if (op->graph) cudaGraphExecDestroy(op->graph);
   for (void *p : op->bufs) cudaFree(p);
   delete[] op->h_dyn;
+  for (cudaEvent_t e : op->cev)
+    if (e) cudaEventDestroy(e);
+  if (op->cstream) cudaStreamDestroy(op->cstream);
   if (op->stream) cudaStreamDestroy(op->stream);
   delete op;
 }
@@ -1061,18 +1079,84 @@ static int step_variant(const oc_op *op, const Scheme &sc) {
 }
 
 // enqueue the stages of one time step on op->stream (capturable)
+// Chunks of the host-vector time step (mixed form, one degree, at least 4 warps of
+// cells per chunk; otherwise n_chunks = 1): kChunks equal cell ranges and, per
+// chunk, the prefix of u^n that chunks 0..k read (own DoFs and those of the
+// inner-face neighbours; the last prefix is every DoF).
+static oc_status setup_chunks(oc_op *op) {
+  if (op->n_chunks) return OC_OK;
+  const int nc = op->n_cells, p = op->uniform_deg, K = oc_op::kChunks;
+  if (!p || op->prm.precision != OC_PREC_MIXED || nc < K * 4 * cells_per_warp(op, p)) {
+    op->n_chunks = 1;
+    return OC_OK;
+  }
+  OC_TRY(cudaStreamCreateWithFlags(&op->cstream, cudaStreamNonBlocking));
+  for (int k = 0; k <= K; ++k) OC_TRY(cudaEventCreateWithFlags(&op->cev[k], cudaEventDisableTiming));
+  const int64_t nn = (int64_t)(p + 1) * (p + 1);
+  int64_t reach = 0;
+  for (int k = 0; k < K; ++k) {
+    op->chunk_first[k] = (int)((int64_t)nc * k / K);
+    op->chunk_first[k + 1] = (int)((int64_t)nc * (k + 1) / K);
+    for (int c = op->chunk_first[k]; c < op->chunk_first[k + 1]; ++c) {
+      reach = std::max(reach, (int64_t)op->off[c] + nn);
+      for (int sl = 0; sl < 8; ++sl) {
+        const int other = op->cfrec[16 * (size_t)c + 2 * sl], pk = op->cfrec[16 * (size_t)c + 2 * sl + 1];
+        if (((pk >> 14) & 3) == 1) reach = std::max(reach, (int64_t)other + nn);
+      }
+    }
+    op->chunk_reach[k] = reach;
+  }
+  op->n_chunks = K;
+  return OC_OK;
+}
+
 static oc_status enqueue_step(oc_op *op, const Scheme &sc, double *z, double *q,
-                              double *oz = nullptr, double *oq = nullptr) {
+                              double *oz = nullptr, double *oq = nullptr,
+                              const double *hz = nullptr, const double *hq = nullptr) {
   const bool mixed = op->prm.precision == OC_PREC_MIXED;
   if (sc.s == 1) {
     const size_t nz = op->n_dofs;
     OC_TRY(cudaMemcpyAsync(op->ts_z0, z, nz * 8, cudaMemcpyDeviceToDevice, op->stream));
     OC_TRY(cudaMemcpyAsync(op->ts_q0, q, 2 * nz * 8, cudaMemcpyDeviceToDevice, op->stream));
   }
+  // host vectors hz, hq (chunked step): copied into z, q by pieces on the second
+  // stream, one event per chunk once its prefix is in
+  const bool chunked = hz && hq && op->n_chunks > 1;
+  if (chunked) {
+    OC_TRY(cudaEventRecord(op->cev[oc_op::kChunks], op->stream));
+    OC_TRY(cudaStreamWaitEvent(op->cstream, op->cev[oc_op::kChunks], 0));
+    int64_t done = 0;
+    for (int k = 0; k < op->n_chunks; ++k) {
+      const int64_t r = op->chunk_reach[k];
+      if (r > done) {
+        OC_TRY(cudaMemcpyAsync(z + done, hz + done, (r - done) * 8, cudaMemcpyHostToDevice,
+                               op->cstream));
+        OC_TRY(cudaMemcpyAsync(q + 2 * done, hq + 2 * done, 2 * (r - done) * 8,
+                               cudaMemcpyHostToDevice, op->cstream));
+        done = r;
+      }
+      OC_TRY(cudaEventRecord(op->cev[k], op->cstream));
+    }
+  }
   for (int st = 0; st < sc.s; ++st) {
     StageArgs a;
     step_stage_args(op, sc, st, z, q, a, oz, oq);
-    oc_status s = launch_groups(op, a, step_variant(op, sc));
+    const int variant = step_variant(op, sc);
+    if (chunked && st == 0) {
+      const int p = op->uniform_deg, batch = op->prm.batch_width;
+      const int cpw = (cells_per_warp(op, p) / batch) * batch, wpb = op->wpb[p];
+      a.group_cells = nullptr;
+      for (int k = 0; k < op->n_chunks; ++k) {
+        OC_TRY(cudaStreamWaitEvent(op->stream, op->cev[k], 0));
+        a.group_first = op->chunk_first[k];
+        a.n_group = op->chunk_first[k + 1] - op->chunk_first[k];
+        OC_TRY(launch_stage(op, p, a, variant, (a.n_group + wpb * cpw - 1) / (wpb * cpw), wpb,
+                            op->stream));
+        op->launches++;
+      }
+      continue;
+    }
+    oc_status s = launch_groups(op, a, variant);
     if (s != OC_OK) return s;
   }
   return OC_OK;
@@ -1205,13 +1289,23 @@ extern "C" oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time
   // both are page-locked host memory the GPU can address (over NVLink-C2C on
   // Grace-Blackwell, overlapping the transfer with the stage), else copied out
   double *oz = nullptr, *oq = nullptr;
+  const double *hz = nullptr, *hq = nullptr;  // copied in by the graph (chunked step)
   if (memory == OC_MEM_HOST) {
     if (ensure(op, &op->ts_z, nz) || ensure(op, &op->ts_q, nq)) return OC_ERR_CUDA;
-    OC_TRY(cudaMemcpyAsync(op->ts_z, z, nz * 8, cudaMemcpyHostToDevice, op->stream));
-    OC_TRY(cudaMemcpyAsync(op->ts_q, q, nq * 8, cudaMemcpyHostToDevice, op->stream));
     dz = op->ts_z; dq = op->ts_q;
     oz = mapped_host(z); oq = mapped_host(q);
     if (!oz || !oq) oz = oq = nullptr;
+    // page-locked vectors on a tuned operator of one degree: the graph copies u^n
+    // in by pieces, overlapped with stage 0 (setup_chunks); otherwise one copy here
+    if (oz && op->tuned && sc.s > 1) {
+      st = setup_chunks(op);
+      if (st != OC_OK) return st;
+      if (op->n_chunks > 1) { hz = z; hq = q; }
+    }
+    if (!hz) {
+      OC_TRY(cudaMemcpyAsync(op->ts_z, z, nz * 8, cudaMemcpyHostToDevice, op->stream));
+      OC_TRY(cudaMemcpyAsync(op->ts_q, q, nq * 8, cudaMemcpyHostToDevice, op->stream));
+    }
   }
   // coefficients: rows a_i[stage] (b_i at the last stage) times dt
   for (int s = 0; s < sc.s; ++s) {
@@ -1233,12 +1327,12 @@ extern "C" oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time
     if (st != OC_OK) return st;
   }
   if (!op->graph || op->graph_scheme != scheme || op->graph_z != dz || op->graph_q != dq ||
-      op->graph_oz != oz || op->graph_oq != oq) {
+      op->graph_oz != oz || op->graph_oq != oq || op->graph_hz != hz || op->graph_hq != hq) {
     if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
     cudaGraph_t g;
     OC_TRY(cudaStreamBeginCapture(op->stream, cudaStreamCaptureModeThreadLocal));
     const int64_t before = op->launches;
-    st = enqueue_step(op, sc, dz, dq, oz, oq);
+    st = enqueue_step(op, sc, dz, dq, oz, oq, hz, hq);
     cudaError_t ce = cudaStreamEndCapture(op->stream, &g);
     op->graph_launches = op->launches - before;
     op->launches = before;
@@ -1248,6 +1342,7 @@ extern "C" oc_status oc_perform_time_step(oc_op *op, int32_t scheme, double time
     cudaGraphDestroy(g);
     op->graph_scheme = scheme; op->graph_z = dz; op->graph_q = dq;
     op->graph_oz = oz; op->graph_oq = oq;
+    op->graph_hz = hz; op->graph_hq = hq;
   }
   {
     TimedScope ts(op, SCOPE_STEP);
