@@ -197,7 +197,9 @@ oc_status oc_perform_stage_hydro(oc_op *op, uint32_t stage, uint32_t n_stages, d
  * height/discharge are updated in place.  With OC_MEM_HOST they are copied in;
  * when both are page-locked (cudaHostAlloc / cudaHostRegister) the last stage
  * writes u^{n+1} into them directly, overlapping the transfer with the stage,
- * else they are copied out.  The call returns when the host vectors hold u^{n+1}
+ * else they are copied out; on a mesh of one degree in the mixed form the copy
+ * in then goes in three pieces, each chunk of stage 0 starting once its cells'
+ * and their neighbours' DoFs have arrived.  The call returns when the host vectors hold u^{n+1}
  * (and reports device-side errors); with OC_MEM_DEVICE it returns once the step
  * is enqueued, and oc_synchronize reports its device-side errors.
  */
