@@ -257,8 +257,7 @@ def test_time_step_host_buffers(gpu_lib, precision, case):
     """oc_perform_time_step on host vectors: page-locked buffers (the last stage
     writes u^{n+1} into them directly) and pageable ones (copied back) give the
     bits of the device-vector run, over several steps and a change of buffers.
-    On the one-degree mesh in the mixed form the page-locked run copies u^n in by
-    pieces and launches stage 0 by chunks of cells (3 chunks of 66-67 cells)."""
+    These meshes are below the size of the chunked copy in: the same launches."""
     import ctypes as C
     import torch
     from oceano_gb300 import _lib
@@ -284,10 +283,8 @@ def test_time_step_host_buffers(gpu_lib, precision, case):
         n1 = _lib.lib().oc_launch_count(op.h)
         a, b = pinned[it % 2]
         host_step(t, a, b)
-        # chunked: stage 0 as 3 launches instead of 1 (after the first, tuning, step)
-        chunked = precision == "mixed" and case == "vortex_p3"
-        if it > 0:
-            assert _lib.lib().oc_launch_count(op.h) - n1 == n1 - n0 + (2 if chunked else 0)
+        if it > 0:  # (the first device step tunes the launches)
+            assert _lib.lib().oc_launch_count(op.h) - n1 == n1 - n0
         if it % 2 == 0:  # the other pair follows with a copy of the state
             pinned[1][0].copy_(a)
             pinned[1][1].copy_(b)
@@ -300,6 +297,39 @@ def test_time_step_host_buffers(gpu_lib, precision, case):
     a, b = pinned[1]
     assert np.array_equal(a.numpy(), zr) and np.array_equal(b.numpy(), qr)
     assert np.array_equal(zp, zr) and np.array_equal(qp, qr)
+
+
+def test_time_step_host_buffers_chunked(gpu_lib):
+    """The 320x160 degree-3 vortex in the mixed form on page-locked host vectors:
+    u^n (19.7 MB) is copied in by three pieces and stage 0 runs by three chunks of
+    cells, each launched once its cells' and their neighbours' DoFs are in; the
+    states are the bits of the device-vector run, step after step."""
+    import ctypes as C
+    import torch
+    from oceano_gb300 import _lib, vortex_mesh
+    from oceano_gb300.icbc import vortex_params
+    from oceano_gb300.workloads import vortex_operator
+    op = vortex_operator(vortex_mesh(4, 3), "mixed", vortex_params())
+    n = op.n_dofs
+    z0, q0 = np.zeros(n), np.zeros(2 * n)
+    op.project_vortex(0.0, z0, q0)
+    dt = 0.05 / op.compute_cell_transport_speed(z0, q0)
+    zd, qd = torch.from_numpy(z0.copy()).cuda(), torch.from_numpy(q0.copy()).cuda()
+    zh, qh = torch.from_numpy(z0.copy()).pin_memory(), torch.from_numpy(q0.copy()).pin_memory()
+    for it in range(4):
+        t = it * dt
+        n0 = _lib.lib().oc_launch_count(op.h)
+        op.perform_time_step("ssp33", t, dt, zd, qd)
+        n1 = _lib.lib().oc_launch_count(op.h)
+        _lib.check(_lib.lib().oc_perform_time_step(op.h, _lib.SCHEME["ssp33"], t, dt,
+                                                   C.c_void_p(zh.data_ptr()),
+                                                   C.c_void_p(qh.data_ptr()), _lib.OC_MEM_HOST),
+                   op.h)
+        if it > 0:  # stage 0 as 3 launches instead of 1
+            assert _lib.lib().oc_launch_count(op.h) - n1 == n1 - n0 + 2
+        torch.cuda.synchronize()
+        assert np.array_equal(zh.numpy(), zd.cpu().numpy())
+        assert np.array_equal(qh.numpy(), qd.cpu().numpy())
 
 
 def test_unknown_boundary_id(gpu_lib):
