@@ -277,8 +277,9 @@ oc_status oc_set_reference_state(oc_op *op, double depth, double qx, double qy);
 /* Launch configuration of the stage kernels (no reference counterpart: deal.II's
  * MatrixFree loops have no launch shape).  OC_LAUNCH_AUTO (default) times, at the
  * first oc_perform_time_step, one launch per degree group with 1, 2 or 4 warps
- * per block against one launch over all groups (hp meshes) with 2 or 4, on a
- * scratch copy of the solution, and keeps the fastest.  The other modes fix the
+ * per block (the groups' launches run concurrently, one stream each) against one
+ * launch over all groups (hp meshes) with 2 or 4, on a scratch copy of the
+ * solution, and keeps the fastest.  The other modes fix the
  * launch shape and tune only the block size.  Setting a mode drops the tuned
  * configuration and the captured step graph. */
 #define OC_LAUNCH_AUTO 0

@@ -225,6 +225,10 @@ struct oc_op {
   static constexpr int kChunks = 3;
   cudaStream_t cstream = nullptr;
   cudaEvent_t cev[kChunks + 1] = {nullptr};
+  // per-group launches on a mesh of several degrees: one stream per degree group,
+  // forked from and joined back into the handle's stream (gev[0]: fork)
+  cudaStream_t gstream[OC_MAXDEG + 1] = {nullptr};
+  cudaEvent_t gev[OC_MAXDEG + 1] = {nullptr};
   int n_chunks = 0;                    // 0: not set up yet; 1: no chunking
   int chunk_first[kChunks + 1] = {0};  // cell range [first[k], first[k + 1]) of chunk k
   int64_t chunk_reach[kChunks] = {0};  // zeta DoFs [0, reach[k]) read by chunks 0..k
@@ -409,6 +413,10 @@ void oc_destroy(oc_op *op) {
   delete[] op->h_dyn;
   for (cudaEvent_t e : op->cev)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : op->gev)
+    if (e) cudaEventDestroy(e);
+  for (cudaStream_t g : op->gstream)
+    if (g) cudaStreamDestroy(g);
   if (op->cstream) cudaStreamDestroy(op->cstream);
   if (op->stream) cudaStreamDestroy(op->stream);
   delete op;
@@ -606,10 +614,10 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
     if (!uniform && !g.empty()) OC_TRY(upload(op, &op->d_group[p], g.data(), g.size()));
   }
   if (op->prm.precision == OC_PREC_MIXED) {
-    // FP64 zeta work area of the mixed kernels: one slot per (warp, team) of the
-    // largest degree-group launch
-    // (the one-launch hp grid is the longest: every group's warps, each group
-    // rounded up to whole blocks of at most kWarpsPerBlock warps)
+    // FP64 zeta work area of the mixed kernels: one slot per (warp, team) of
+    // every group's warps, each group rounded up to whole blocks of at most
+    // kWarpsPerBlock warps: the one-launch hp grid, or the concurrent per-group
+    // launches side by side (launch_groups gives each group its part)
     size_t warps = 0;
     for (int p = 1; p <= OC_MAXDEG; ++p) {
       const int cpw = (cells_per_warp(op, p) / op->prm.batch_width) * op->prm.batch_width;
@@ -857,6 +865,23 @@ static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
     op->launches++;
     return OC_OK;
   }
+  // Per-group launches.  With several groups they run concurrently, one stream
+  // per group (no drain between the groups, each group with its own registers and
+  // block size; each group's launch gets its own part of the FP64 work area,
+  // which the kernels index by block): hp step 0.480 -> 0.388 ms against the
+  // groups one after the other on the handle's stream (A/B).
+  const bool conc = n_groups(op) > 1;
+  if (conc) {
+    if (!op->gstream[1]) {
+      for (int p = 1; p <= OC_MAXDEG; ++p)
+        OC_TRY(cudaStreamCreateWithFlags(&op->gstream[p], cudaStreamNonBlocking));
+      for (int p = 0; p <= OC_MAXDEG; ++p)
+        OC_TRY(cudaEventCreateWithFlags(&op->gev[p], cudaEventDisableTiming));
+    }
+    OC_TRY(cudaEventRecord(op->gev[0], op->stream));
+  }
+  double *const dbase = a.dscratch;
+  size_t woff = 0;  // warps of the work area taken by the groups before (sized in oc_create)
   for (int p = 1; p <= OC_MAXDEG; ++p) {
     const int n = op->group_n[p];
     if (n == 0) continue;
@@ -866,9 +891,20 @@ static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
     a.group_cells = op->uniform_deg ? nullptr : op->d_group[p];
     a.group_first = 0;
     const int grid = (n + wpb * cpw - 1) / (wpb * cpw);
-    OC_TRY(launch_stage(op, p, a, variant, grid, wpb, op->stream));
+    if (conc) {
+      a.dscratch = dbase ? dbase + woff * OC_MAXCPW * OC_DSTRIDE : nullptr;
+      OC_TRY(cudaStreamWaitEvent(op->gstream[p], op->gev[0], 0));
+      OC_TRY(launch_stage(op, p, a, variant, grid, wpb, op->gstream[p]));
+      OC_TRY(cudaEventRecord(op->gev[p], op->gstream[p]));
+    } else {
+      OC_TRY(launch_stage(op, p, a, variant, grid, wpb, op->stream));
+    }
+    woff += (size_t)(n + cpw - 1) / cpw + kWarpsPerBlock;
     op->launches++;
   }
+  if (conc)
+    for (int p = 1; p <= OC_MAXDEG; ++p)
+      if (op->group_n[p]) OC_TRY(cudaStreamWaitEvent(op->stream, op->gev[p], 0));
   return OC_OK;
 }
 
@@ -1236,6 +1272,8 @@ static oc_status autotune(oc_op *op, const Scheme &sc, const double *z, const do
       per_group += best;
     }
     for (int p = 0; p <= OC_MAXDEG; ++p) op->group_n[p] = saved[p];
+    // several groups run concurrently (launch_groups): time them together
+    if (st == OC_OK && n_groups(op) > 1) st = time_stage(op, sc, tz, tq, reps, &per_group);
   }
   op->tune_ms[0] = per_group;
   float one = 3.4e38f;
