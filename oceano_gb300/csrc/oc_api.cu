@@ -610,6 +610,24 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
     std::vector<int> g;
     for (int c = 0; c < nc; ++c)
       if (m->degree[c] == p) g.push_back(c);
+    // Cells of a group in the order of their face records (kind, neighbour degree,
+    // face points, side, subface, orientation, boundary id of each slot; the
+    // neighbour's face number aside): the cells of a warp then mostly take the
+    // same face paths, and fewer lanes idle on divergent branches (random hp mesh
+    // 0.383 -> 0.363 ms, ensemble 3.10 -> 3.00 ms per step, A/B).  Cells are
+    // independent within a stage, so the order changes no result, except through
+    // the batches of the zeta stop rule (batch_width > 1: cells batched in index
+    // order, as the oracle does), where it is kept.
+    if (!uniform && op->prm.batch_width == 1) {
+      auto key = [&](int c, int sl) { return op->cfrec[16 * (size_t)c + 2 * sl + 1] & ~0xC; };
+      std::stable_sort(g.begin(), g.end(), [&](int x, int y) {
+        for (int sl = 0; sl < 8; ++sl) {
+          const int kx = key(x, sl), ky = key(y, sl);
+          if (kx != ky) return kx < ky;
+        }
+        return false;
+      });
+    }
     op->group_n[p] = (int)g.size();
     if (!uniform && !g.empty()) OC_TRY(upload(op, &op->d_group[p], g.data(), g.size()));
   }
