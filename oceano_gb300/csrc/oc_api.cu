@@ -155,6 +155,9 @@ struct oc_op {
   // degree groups
   int group_n[OC_MAXDEG + 1] = {0, 0, 0, 0, 0};
   int *d_group[OC_MAXDEG + 1] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  // the same groups in index order, where d_group is sorted (mixed form): the last
+  // stage of a host-vector step writes u^{n+1} over the host link in this order
+  int *d_group_idx[OC_MAXDEG + 1] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   int uniform_deg = 0;
   int conforming = 0;  // uniform degree, no hanging face, standard orientation
   // boundary conditions
@@ -610,15 +613,18 @@ oc_status oc_create(const oc_mesh_desc *m, const oc_params *prm, oc_op **out) {
     std::vector<int> g;
     for (int c = 0; c < nc; ++c)
       if (m->degree[c] == p) g.push_back(c);
-    // Cells of a group in the order of their face records (kind, neighbour degree,
-    // face points, side, subface, orientation, boundary id of each slot; the
-    // neighbour's face number aside): the cells of a warp then mostly take the
-    // same face paths, and fewer lanes idle on divergent branches (random hp mesh
-    // 0.383 -> 0.363 ms, ensemble 3.10 -> 3.00 ms per step, A/B).  Cells are
-    // independent within a stage, so the order changes no result, except through
-    // the batches of the zeta stop rule (batch_width > 1: cells batched in index
-    // order, as the oracle does), where it is kept.
-    if (!uniform && op->prm.batch_width == 1) {
+    // Mixed form: cells of a group in the order of their face records (kind,
+    // neighbour degree, face points, side, subface, orientation, boundary id of
+    // each slot; the neighbour's face number aside): the cells of a warp then
+    // mostly take the same face paths, and fewer lanes idle on divergent branches
+    // (random hp mesh 0.383 -> 0.363 ms, ensemble 3.10 -> 3.00 ms per step, A/B).
+    // Cells are independent within a stage, so the order changes no result,
+    // except through the batches of the zeta stop rule (batch_width > 1: cells
+    // batched in index order, as the oracle does), where it is kept.  The FP64
+    // form keeps the index order: its stage kernel copies the face pass's values,
+    // which neighbouring cells share (hp mesh 1.61 -> 1.24 G DoF-stage/s sorted).
+    if (!uniform && op->prm.batch_width == 1 && op->prm.precision == OC_PREC_MIXED) {
+      OC_TRY(upload(op, &op->d_group_idx[p], g.data(), g.size()));
       auto key = [&](int c, int sl) { return op->cfrec[16 * (size_t)c + 2 * sl + 1] & ~0xC; };
       std::stable_sort(g.begin(), g.end(), [&](int x, int y) {
         for (int sl = 0; sl < 8; ++sl) {
@@ -855,7 +861,11 @@ static oc_status check_boundaries(oc_op *op) {
 // launch the fused kernel over every degree group: one launch per group, or
 // (hp meshes, use_hp) one launch whose grid concatenates the groups, highest
 // degree first; variant 2 (the mixed reference-ABI stage) always per group
-static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
+// index_order: the groups in cell-index order (d_group_idx) where they are sorted
+static oc_status launch_groups(oc_op *op, StageArgs a, int variant, bool index_order = false) {
+  auto group = [&](int p) {
+    return index_order && op->d_group_idx[p] ? op->d_group_idx[p] : op->d_group[p];
+  };
   const int batch = op->prm.batch_width;
   for (int p = 1; p <= OC_MAXDEG; ++p)
     if (op->group_n[p] && (cells_per_warp(op, p) / batch) * batch == 0)
@@ -874,7 +884,7 @@ static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
       const int cpw = (cells_per_warp(op, p) / batch) * batch;
       a.hp_first_block[p] = b0;
       a.hp_n[p] = n;
-      a.hp_cells[p] = op->d_group[p];
+      a.hp_cells[p] = group(p);
       a.hp_blocks[p] = n ? (n + wpb * cpw - 1) / (wpb * cpw) : 0;
       b0 += a.hp_blocks[p];
     }
@@ -906,7 +916,7 @@ static oc_status launch_groups(oc_op *op, StageArgs a, int variant) {
     const int cpw = (cells_per_warp(op, p) / batch) * batch;
     const int wpb = op->wpb[p];
     a.n_group = n;
-    a.group_cells = op->uniform_deg ? nullptr : op->d_group[p];
+    a.group_cells = op->uniform_deg ? nullptr : group(p);
     a.group_first = 0;
     const int grid = (n + wpb * cpw - 1) / (wpb * cpw);
     if (conc) {
@@ -1213,7 +1223,11 @@ static oc_status enqueue_step(oc_op *op, const Scheme &sc, double *z, double *q,
       }
       continue;
     }
-    oc_status s = launch_groups(op, a, variant);
+    // the last stage writing into page-locked host vectors: cells in index order,
+    // so that each warp's writes over the host link are close together (ensemble
+    // e2e step 4.80 ms with the sorted order throughout, 4.55 with this, 4.63
+    // unsorted; A/B)
+    oc_status s = launch_groups(op, a, variant, oz != nullptr && st == sc.s - 1);
     if (s != OC_OK) return s;
   }
   return OC_OK;
