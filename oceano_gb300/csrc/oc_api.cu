@@ -1142,7 +1142,6 @@ static int step_variant(const oc_op *op, const Scheme &sc) {
   return lean ? (op->conforming ? 4 : 3) : 1;
 }
 
-// enqueue the stages of one time step on op->stream (capturable)
 // Chunks of the host-vector time step (mixed form, one degree, u^n of at least
 // kChunkMinBytes; otherwise n_chunks = 1): kChunks equal cell ranges and, per
 // chunk, the prefix of u^n that chunks 0..k read (own DoFs and those of the
@@ -1177,6 +1176,8 @@ static oc_status setup_chunks(oc_op *op) {
   return OC_OK;
 }
 
+// enqueue the stages of one time step on op->stream (capturable; the chunked step
+// and concurrent degree groups fork other streams from it and join them back)
 static oc_status enqueue_step(oc_op *op, const Scheme &sc, double *z, double *q,
                               double *oz = nullptr, double *oq = nullptr,
                               const double *hz = nullptr, const double *hq = nullptr) {
