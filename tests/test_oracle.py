@@ -5,7 +5,8 @@ pinned by properties the reference's scheme must have: free-stream
 preservation (also across hanging faces and degree jumps), the lake at rest to
 machine precision (well-balancing of OceanDG.h's hydrostatic reconstruction),
 global mass conservation of a stage, consistency of the explicit and additive
-stage drivers, and convergence to the analytic travelling vortex.  The
+stage drivers, invariance of the stage under periodic translations, and
+convergence to the analytic travelling vortex.  The
 properties that hold for any cell quadrature are checked for both rules of
 n_points_1d (floor(1.5 p) + 1 and p + 1).
 """
@@ -225,3 +226,38 @@ def test_apply_is_inverse_mass_of_the_residual(mesh_f):
         Mc = det * np.kron(M1, M1)
         r = Mc @ dz[off[c]:off[c + 1]] - kz[1][off[c]:off[c + 1]]
         assert np.abs(r).max() <= 1e-12 * max(1.0, np.abs(kz[1][off[c]:off[c + 1]]).max())
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+@pytest.mark.parametrize("degree", [1, 3])
+def test_residual_commutes_with_periodic_translation(degree, rule):
+    """On the x-periodic 20x10 mesh (walls in y), translating an arbitrary wet state
+    by k cells in x translates its stage residual and update: every cell, face and
+    boundary face is evaluated by the same operations, so the two agree to
+    rounding.  A wrong neighbour, face orientation or periodic link shows here."""
+    mesh = vortex_mesh(0, degree)
+    orc = O.Oracle(mesh, bcs={0: ("wall",)}, cell_rule=rule)
+    off = mesh.offsets()
+    nd = (degree + 1) ** 2
+    v = mesh.vertices
+    cx, cy = v[:, 0::2].mean(1), v[:, 1::2].mean(1)
+    rng = np.random.default_rng(7 + degree)
+    z = 1.0 + 0.1 * rng.random(orc.n)
+    q = 0.1 * rng.standard_normal(2 * orc.n)
+    rz, rq, nz, nq = residuals(orc, z, q)
+    for k in (1, 3):
+        tx = (cx + 0.1 * k) % 2.0  # cell c moves to the cell centred at (tx, cy)
+        key = {(round(x, 6), round(y, 6)): c for c, (x, y) in enumerate(zip(cx, cy))}
+        dst = np.array([key[(round(x, 6), round(y, 6))] for x, y in zip(tx, cy)])
+        zs, qs = np.empty_like(z), np.empty_like(q)
+        for c in range(mesh.n_cells):
+            d = dst[c]
+            zs[off[d]:off[d] + nd] = z[off[c]:off[c] + nd]
+            qs[2 * off[d]:2 * off[d] + 2 * nd] = q[2 * off[c]:2 * off[c] + 2 * nd]
+        sz, sq, snz, snq = residuals(orc, zs, qs)
+        for c in range(mesh.n_cells):
+            d = dst[c]
+            for a, b, s in ((rz, sz, 1), (nz, snz, 1), (rq, sq, 2), (nq, snq, 2)):
+                np.testing.assert_allclose(b[s * off[d]:s * off[d] + s * nd],
+                                           a[s * off[c]:s * off[c] + s * nd],
+                                           rtol=0, atol=1e-12 * (1 + np.abs(a).max()))
