@@ -5,8 +5,8 @@ pinned by properties the reference's scheme must have: free-stream
 preservation (also across hanging faces and degree jumps), the lake at rest to
 machine precision (well-balancing of OceanDG.h's hydrostatic reconstruction),
 global mass conservation of a stage, consistency of the explicit and additive
-stage drivers, invariance of the stage under periodic translations, and
-convergence to the analytic travelling vortex.  The
+stage drivers, invariance of the stage under periodic translations and
+mirroring, and convergence to the analytic travelling vortex.  The
 properties that hold for any cell quadrature are checked for both rules of
 n_points_1d (floor(1.5 p) + 1 and p + 1).
 """
@@ -261,3 +261,48 @@ def test_residual_commutes_with_periodic_translation(degree, rule):
                 np.testing.assert_allclose(b[s * off[d]:s * off[d] + s * nd],
                                            a[s * off[c]:s * off[c] + s * nd],
                                            rtol=0, atol=1e-12 * (1 + np.abs(a).max()))
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+@pytest.mark.parametrize("degree", [1, 2, 3])
+@pytest.mark.parametrize("axis", [0, 1])
+def test_residual_commutes_with_mirroring(axis, degree, rule):
+    """Mirroring the x-periodic, y-walled domain about x = 1 (axis 0) or y = 1/2
+    (axis 1) maps an arbitrary wet state to its mirror image (the normal discharge
+    component changes sign, the nodes of each cell are reversed along the axis);
+    the stage residual and update must be mirrored the same way.  This checks the
+    orientation of normals, face numbers and the wall flux on both sides."""
+    mesh = vortex_mesh(0, degree)
+    orc = O.Oracle(mesh, bcs={0: ("wall",)}, cell_rule=rule)
+    off = mesh.offsets()
+    N = degree + 1
+    nd = N * N
+    v = mesh.vertices
+    cx, cy = v[:, 0::2].mean(1), v[:, 1::2].mean(1)
+    key = {(round(x, 6), round(y, 6)): c for c, (x, y) in enumerate(zip(cx, cy))}
+    mx, my = (2.0 - cx, cy) if axis == 0 else (cx, 1.0 - cy)
+    dst = np.array([key[(round(x, 6), round(y, 6))] for x, y in zip(mx, my)])
+    i, j = np.meshgrid(np.arange(N), np.arange(N), indexing="xy")  # node i + N j
+    local = (i[:, ::-1] if axis == 0 else i[::-1, :]) + N * (j[:, ::-1] if axis == 0 else j[::-1, :])
+    perm = local.ravel()  # mirrored node of node k
+    sign = np.array([-1.0, 1.0]) if axis == 0 else np.array([1.0, -1.0])
+
+    def mirror(z, q):
+        zs, qs = np.empty_like(z), np.empty_like(q)
+        for c in range(mesh.n_cells):
+            d = dst[c]
+            zs[off[d] + perm] = z[off[c]:off[c] + nd]
+            for comp in range(2):
+                qs[2 * off[d] + comp * nd + perm] = sign[comp] * q[2 * off[c] + comp * nd:
+                                                                  2 * off[c] + (comp + 1) * nd]
+        return zs, qs
+
+    rng = np.random.default_rng(11 + degree)
+    z = 1.0 + 0.1 * rng.random(orc.n)
+    q = 0.1 * rng.standard_normal(2 * orc.n)
+    rz, rq, nz, nq = residuals(orc, z, q)
+    sz, sq, snz, snq = residuals(orc, *mirror(z, q))
+    mz, mq = mirror(rz, rq)
+    mnz, mnq = mirror(nz, nq)
+    for got, want in ((sz, mz), (sq, mq), (snz, mnz), (snq, mnq)):
+        np.testing.assert_allclose(got, want, rtol=0, atol=1e-12 * (1 + np.abs(want).max()))
