@@ -4,7 +4,8 @@ The reference ships no test suite and cannot be built here, so the oracle is
 pinned by properties the reference's scheme must have: free-stream
 preservation (also across hanging faces and degree jumps), the lake at rest to
 machine precision (well-balancing of OceanDG.h's hydrostatic reconstruction),
-global mass conservation of a stage, consistency of the explicit and additive
+global mass conservation of a stage, conservation of the x discharge between
+walls in y, consistency of the explicit and additive
 stage drivers, invariance of the stage under periodic translations and
 mirroring, and convergence to the analytic travelling vortex.  The
 properties that hold for any cell quadrature are checked for both rules of
@@ -306,3 +307,29 @@ def test_residual_commutes_with_mirroring(axis, degree, rule):
     mnz, mnq = mirror(nz, nq)
     for got, want in ((sz, mz), (sq, mq), (snz, mnz), (snq, mnq)):
         np.testing.assert_allclose(got, want, rtol=0, atol=1e-12 * (1 + np.abs(want).max()))
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+@pytest.mark.parametrize("degree", [1, 3])
+def test_x_discharge_conserved(degree, rule):
+    """On the x-periodic domain with walls at y = 0 and 1, no force acts in x (the
+    wall's pressure and Lax-Friedrichs terms act along its normal, y): whole SSP-RK3
+    steps keep the domain integral of hu of an arbitrary wet state to rounding."""
+    mesh = vortex_mesh(0, degree)
+    orc = O.Oracle(mesh, bcs={0: ("wall",)}, cell_rule=rule)
+    off = mesh.offsets()
+    nd = (degree + 1) ** 2
+    rng = np.random.default_rng(3 + degree)
+    z = 1.0 + 0.1 * rng.random(orc.n)
+    q = 0.1 * rng.standard_normal(2 * orc.n)
+
+    def hu(q):
+        return np.concatenate([q[2 * off[c]:2 * off[c] + nd] for c in range(mesh.n_cells)])
+
+    m0 = cell_integrals(mesh, hu(q))
+    tb = O.TABLEAUX["ssp33"]
+    dt = 0.05 / orc.transport_speed(z, q)
+    for it in range(3):
+        O.erk_step(orc, tb["a"], tb["b"], tb["c"], it * dt, dt, z, q)
+    scale = cell_integrals(mesh, np.abs(hu(q)))
+    assert abs(cell_integrals(mesh, hu(q)) - m0) < 1e-13 * scale
