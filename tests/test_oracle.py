@@ -2,7 +2,8 @@
 
 The reference ships no test suite and cannot be built here, so the oracle is
 pinned by properties the reference's scheme must have: free-stream
-preservation (also across hanging faces and degree jumps), the lake at rest to
+preservation (also across hanging faces and degree jumps, and through every
+kind of open boundary whose data matches the flow), the lake at rest to
 machine precision (well-balancing of OceanDG.h's hydrostatic reconstruction),
 global mass conservation of a stage, conservation of the x discharge between
 walls in y, consistency of the explicit and additive
@@ -333,3 +334,23 @@ def test_x_discharge_conserved(degree, rule):
         O.erk_step(orc, tb["a"], tb["b"], tb["c"], it * dt, dt, z, q)
     scale = cell_integrals(mesh, np.abs(hu(q)))
     assert abs(cell_integrals(mesh, hu(q)) - m0) < 1e-13 * scale
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+@pytest.mark.parametrize("left,right", [
+    (("supercritical_inflow", (1.0, 0.9, 0.0)), ("supercritical_outflow",)),
+    (("height_inflow", (1.0, 0.0, 0.0)), ("absorbing_outflow", (1.0, 0.9, 0.0))),
+    (("discharge_inflow", (0.0, 0.9, 0.0)), ("height_inflow", (1.0, 0.0, 0.0))),
+])
+def test_open_boundaries_keep_a_matching_uniform_flow(left, right, rule):
+    """A uniform flow (zeta 1 over a flat bottom, u = 0.9 along the walls) whose
+    values the inflow and outflow conditions reproduce is a steady state of every
+    boundary kind (OceanDG.h:1105-1339 with the ghost states of IcbcBase.h):
+    supercritical in/out, height inflow, absorbing outflow at the same far field,
+    discharge inflow of the same normal discharge."""
+    mesh = uniform_mesh(8, 4, (0.0, 2.0, 0.0, 1.0), False, 2)
+    orc = O.Oracle(mesh, bcs={0: ("wall",), 1: left, 2: right}, cell_rule=rule)
+    z, q = uniform_state(mesh, z=1.0, q=(0.9, 0.0))
+    rz, rq, nz, nq = residuals(orc, z, q)
+    assert np.abs(rz).max() < 1e-13 and np.abs(rq).max() < 1e-12
+    assert np.abs(nz - z).max() < 1e-14 and np.abs(nq - q).max() < 1e-14
