@@ -43,29 +43,36 @@ class TimeLoop:
         self.step_number = 0
         self.time_step = None
 
+    def _courant_step(self, speed: float) -> float:
+        # C++ semantics: a zero speed gives an infinite step, a NaN speed a NaN one
+        return self.courant / speed if speed != 0.0 else math.inf
+
     def start(self, z, q, time: float = 0.0):
         self.time = time
         self.step_number = 0
-        self.time_step = self.courant / self.op.compute_cell_transport_speed(z, q)
+        self.time_step = self._courant_step(self.op.compute_cell_transport_speed(z, q))
         return self.time_step
 
     def next_time_step(self, z, q) -> float:
         """Step size of the next step (main.cc:1550-1555)."""
         if (self.step_number + 1) % self.dt_every == 0:
             s = truncate_to_n_digits(self.op.compute_cell_transport_speed(z, q), self.digits)
-            self.time_step = self.courant / s
+            self.time_step = self._courant_step(s)
         return self.time_step
 
     def advance(self, z, q, velocity=None, dt: float | None = None):
-        """One step of the loop; returns the step size used."""
+        """One step of the loop; returns the step size used.  A step size that is
+        not finite (a blown-up state, main.cc:1526-1529) stops the loop before the
+        step."""
         if self.time_step is None:
             self.start(z, q)
         dt = self.next_time_step(z, q) if dt is None else dt
+        if not np.isfinite(dt):
+            raise FloatingPointError("time step is not finite (the Courant number is too large "
+                                     "or the state blew up)")
         self.op.perform_time_step(self.scheme, self.time, dt, z, q)
         if velocity is not None:
             self.op.evaluate_velocity_field(z, q, velocity)
         self.step_number += 1
         self.time += dt
-        if not np.isfinite(dt):
-            raise FloatingPointError("time step is not finite (the Courant number is too large)")
         return dt
